@@ -1,0 +1,184 @@
+/*
+ * polatory_gpu.h — C ABI of the GB300 RBF fit/evaluate library (libpolatory_gpu.so).
+ *
+ * Every entry point returns an int status (PGPU_OK == 0). On failure the message is
+ * available from pgpu_last_error() (thread-local). Buffers may be host or device
+ * pointers: the library inspects each pointer with cudaPointerGetAttributes and copies
+ * host buffers to the device itself. Points are row-major double[n * 3].
+ *
+ * Reference interfaces replaced (paths inside polatory/polatory):
+ *   - pgpu_rbf_*            : include/polatory/rbf/rbf.hpp:11-118, rbf/make_rbf.hpp:24-50
+ *   - pgpu_model_*          : include/polatory/model.hpp:23-183
+ *   - pgpu_evaluator_*      : include/polatory/fmm/fmm_evaluator.hpp:17-106 and
+ *                             include/polatory/fmm/fmm_symmetric_evaluator.hpp:15-86
+ *                             (factories src/fmm/make_fmm_evaluator.cpp:40-279)
+ *   - pgpu_interpolant_*    : include/polatory/interpolant.hpp:54-218
+ *   - pgpu_fit_batch        : no single reference counterpart; it runs Interpolant::fit
+ *                             (interpolant.hpp:77-113) over many independent problems.
+ *   - pgpu_server_*         : no reference counterpart; serving loop over Interpolant
+ *                             fit/evaluate.
+ */
+#ifndef POLATORY_GPU_H_
+#define POLATORY_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------ */
+enum {
+  PGPU_OK = 0,
+  PGPU_INVALID_ARGUMENT = 1, /* std::invalid_argument in the reference */
+  PGPU_RUNTIME_ERROR = 2,    /* std::runtime_error in the reference */
+  PGPU_CUDA_ERROR = 3,
+  PGPU_OUT_OF_MEMORY = 4,
+  PGPU_NOT_IMPLEMENTED = 5,
+  PGPU_MAX_ITER = 6,         /* "reached the maximum number of iterations" (runtime_error) */
+  PGPU_TIMEOUT = 7,          /* a bounded device wait ran out */
+  PGPU_REJECTED = 8          /* serving admission refused (HBM budget) */
+};
+
+/* ---- RBF kernels (reference short names, rbf/make_rbf.hpp:28-43) --------------------- */
+enum {
+  PGPU_RBF_BH2 = 0,  /* Biharmonic2D        rbf/polyharmonic_even.hpp */
+  PGPU_RBF_BH3 = 1,  /* Biharmonic3D        rbf/polyharmonic_odd.hpp  */
+  PGPU_RBF_CUB = 2,  /* CovCubic            rbf/cov_cubic.hpp */
+  PGPU_RBF_EXP = 3,  /* CovExponential      rbf/cov_exponential.hpp */
+  PGPU_RBF_GAU = 4,  /* CovGaussian         rbf/cov_gaussian.hpp */
+  PGPU_RBF_GC3 = 5,  /* CovGeneralizedCauchy3 */
+  PGPU_RBF_GC5 = 6,  /* CovGeneralizedCauchy5 */
+  PGPU_RBF_GC7 = 7,  /* CovGeneralizedCauchy7 */
+  PGPU_RBF_GC9 = 8,  /* CovGeneralizedCauchy9 */
+  PGPU_RBF_SPH = 9,  /* CovSpherical */
+  PGPU_RBF_SP3 = 10, /* CovSpheroidal3 */
+  PGPU_RBF_SP5 = 11, /* CovSpheroidal5 */
+  PGPU_RBF_SP7 = 12, /* CovSpheroidal7 */
+  PGPU_RBF_SP9 = 13, /* CovSpheroidal9 */
+  PGPU_RBF_TH2 = 14, /* Triharmonic2D */
+  PGPU_RBF_TH3 = 15, /* Triharmonic3D */
+  PGPU_RBF_COUNT = 16
+};
+
+#define PGPU_MAX_RBFS 4
+
+/* One RBF: kind, its two parameters (scale/c or psill/range) and the row-major 3x3
+ * anisotropy matrix A (the kernel is evaluated at A * (x - y)). */
+typedef struct pgpu_rbf {
+  int32_t kind;
+  int32_t reserved;
+  double params[2];
+  double aniso[9];
+} pgpu_rbf;
+
+/* Model<3>: a sum of RBFs, the polynomial degree (-1 = none .. 2) and the nugget. */
+typedef struct pgpu_model {
+  int32_t n_rbfs;
+  int32_t poly_degree;
+  double nugget;
+  pgpu_rbf rbfs[PGPU_MAX_RBFS];
+} pgpu_model;
+
+/* Arithmetic of the fit/evaluate path. PLAIN: all FP64 (the drop-in). MIXED: FP32 near
+ * field and far field with FP64 Krylov, residual recomputation and polynomial block. */
+enum { PGPU_PRECISION_PLAIN = 0, PGPU_PRECISION_MIXED = 1 };
+
+/* FMM evaluator flavours (fmm/kernel.hpp, gradient_kernel.hpp, gradient_transpose_kernel.hpp,
+ * hessian_kernel.hpp). */
+enum {
+  PGPU_KERNEL_VALUE = 0,              /* km=1, kn=1 */
+  PGPU_KERNEL_GRADIENT = 1,           /* km=3, kn=1 */
+  PGPU_KERNEL_GRADIENT_TRANSPOSE = 2, /* km=1, kn=3 */
+  PGPU_KERNEL_HESSIAN = 3             /* km=3, kn=3 */
+};
+
+/* ---- library ----------------------------------------------------------------------- */
+const char* pgpu_last_error(void);
+int pgpu_version(void);
+/* Selects the CUDA device used by later calls of this thread (default 0). */
+int pgpu_set_device(int device);
+/* Releases cached device memory held by the library's pool. */
+int pgpu_release_cached_memory(void);
+
+/* ---- RBF pointwise evaluation (rbf/rbf_base.hpp:40-53) -------------------------------- */
+/* Evaluates the anisotropic kernel at n difference vectors (host buffers). Any of values
+ * (n), gradients (n*3) or hessians (n*9, row-major) may be NULL. Runs on the host; used to
+ * check the device formulas. Kinds without a Hessian (cub, sph) return
+ * PGPU_RUNTIME_ERROR when hessians != NULL, as rbf/cov_cubic.hpp:59 throws. */
+int pgpu_rbf_evaluate(const pgpu_rbf* rbf, const double* diffs, int64_t n, double* values,
+                      double* gradients, double* hessians);
+/* cpd_order (rbf_base.hpp:37) and support radius (rbf_base.hpp:97) of a kernel. */
+int pgpu_rbf_cpd_order(const pgpu_rbf* rbf, int* out);
+int pgpu_rbf_support_radius_isotropic(const pgpu_rbf* rbf, double* out);
+/* Model validation: poly_degree within [cpd_order-1, 2] (model.hpp:37-50), nugget >= 0. */
+int pgpu_model_validate(const pgpu_model* model);
+int pgpu_model_poly_basis_size(const pgpu_model* model, int64_t* out);
+
+/* ---- FMM evaluator (fmm/fmm_evaluator.hpp:17-41, fmm_symmetric_evaluator.hpp:15-37) ---- */
+typedef struct pgpu_evaluator pgpu_evaluator;
+/* bbox = {minx, miny, minz, maxx, maxy, maxz}. symmetric != 0 selects the symmetric
+ * evaluator (sources == targets, set_points). Only VALUE and HESSIAN kinds exist as
+ * symmetric evaluators, as in the reference factories. */
+int pgpu_evaluator_create(const pgpu_rbf* rbf, int kernel_kind, int symmetric,
+                          const double bbox[6], int precision, pgpu_evaluator** out);
+int pgpu_evaluator_destroy(pgpu_evaluator* ev);
+int pgpu_evaluator_set_accuracy(pgpu_evaluator* ev, double accuracy);
+int pgpu_evaluator_set_source_points(pgpu_evaluator* ev, const double* points, int64_t n);
+int pgpu_evaluator_set_target_points(pgpu_evaluator* ev, const double* points, int64_t n);
+int pgpu_evaluator_set_points(pgpu_evaluator* ev, const double* points, int64_t n);
+/* weights: km * n_sources values in the caller's point order. */
+int pgpu_evaluator_set_weights(pgpu_evaluator* ev, const double* weights, int64_t n);
+/* out: kn * n_targets values in the caller's target order. */
+int pgpu_evaluator_evaluate(pgpu_evaluator* ev, double* out, int64_t n);
+
+/* ---- Interpolant (interpolant.hpp:54-218) --------------------------------------------- */
+typedef struct pgpu_interpolant pgpu_interpolant;
+
+/* Fit statistics of the last fit: FGMRES iterations, final residuals, timings (s). */
+typedef struct pgpu_fit_stats {
+  int32_t iterations;
+  int32_t levels;          /* RAS levels */
+  double residual;         /* inf-norm residual at the data points of the accepted fit */
+  double grad_residual;
+  double setup_seconds;    /* tree + preconditioner setup */
+  double solve_seconds;    /* FGMRES loop */
+  int64_t n_domains;       /* RAS domains over all fine levels */
+} pgpu_fit_stats;
+
+int pgpu_interpolant_create(const pgpu_model* model, pgpu_interpolant** out);
+int pgpu_interpolant_destroy(pgpu_interpolant* it);
+/* precision: PGPU_PRECISION_PLAIN (default) or PGPU_PRECISION_MIXED. */
+int pgpu_interpolant_set_precision(pgpu_interpolant* it, int precision);
+/* Interpolant::fit (interpolant.hpp:82-113). grad_points may be NULL when sigma == 0.
+ * values: mu + 3 * sigma entries. initial may be NULL (warm start otherwise). */
+int pgpu_interpolant_fit(pgpu_interpolant* it, const double* points, int64_t mu,
+                         const double* grad_points, int64_t sigma, const double* values,
+                         double tolerance, double grad_tolerance, int max_iter, double accuracy,
+                         double grad_accuracy, const pgpu_interpolant* initial);
+/* Interpolant::evaluate (interpolant.hpp:58-67). out: m + 3 * mg entries. */
+int pgpu_interpolant_evaluate(pgpu_interpolant* it, const double* points, int64_t m,
+                              const double* grad_points, int64_t mg, double accuracy,
+                              double grad_accuracy, double* out);
+/* Interpolant::evaluate_impl (interpolant.hpp:69-75): reuses the evaluator built by the
+ * last evaluate / set_evaluation_bbox. */
+int pgpu_interpolant_evaluate_impl(pgpu_interpolant* it, const double* points, int64_t m,
+                                   const double* grad_points, int64_t mg, double* out);
+/* Interpolant::set_evaluation_bbox_impl (interpolant.hpp:201-210). */
+int pgpu_interpolant_set_evaluation_bbox(pgpu_interpolant* it, const double bbox[6],
+                                         double accuracy, double grad_accuracy);
+int pgpu_interpolant_is_fitted(const pgpu_interpolant* it, int* out);
+int pgpu_interpolant_num_weights(const pgpu_interpolant* it, int64_t* out);
+/* weights layout [lambda (mu), lambda_grad (3 sigma, row-major), c (l)] (interpolant.hpp:88). */
+int pgpu_interpolant_weights(const pgpu_interpolant* it, double* out, int64_t n);
+int pgpu_interpolant_num_centers(const pgpu_interpolant* it, int64_t* mu, int64_t* sigma);
+int pgpu_interpolant_centers(const pgpu_interpolant* it, double* centers, double* grad_centers);
+int pgpu_interpolant_bbox(const pgpu_interpolant* it, double bbox[6]);
+int pgpu_interpolant_fit_stats(const pgpu_interpolant* it, pgpu_fit_stats* out);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* POLATORY_GPU_H_ */

@@ -1,0 +1,318 @@
+"""Python host API of the GB300 RBF fit/evaluate library.
+
+Mirrors the reference's Python binding (python/python_binding.cpp:33-137): rbf classes taking a
+parameter list, Model(rbf, poly_degree), Interpolant(model).fit/evaluate. Every call goes through
+the C ABI of libpolatory_gpu.so (include/polatory_gpu.h); there is no CPU code path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import PolatoryError, as_points, check, lib, ptr
+
+__all__ = [
+    "Rbf", "Biharmonic2D", "Biharmonic3D", "CovCubic", "CovExponential", "CovGaussian",
+    "CovGeneralizedCauchy3", "CovGeneralizedCauchy5", "CovGeneralizedCauchy7",
+    "CovGeneralizedCauchy9", "CovSpherical", "CovSpheroidal3", "CovSpheroidal5",
+    "CovSpheroidal7", "CovSpheroidal9", "Triharmonic2D", "Triharmonic3D", "Model", "Interpolant",
+    "FmmEvaluator", "PolatoryError", "make_rbf", "PLAIN", "MIXED",
+]
+
+PLAIN = _lib.PRECISION_PLAIN
+MIXED = _lib.PRECISION_MIXED
+INF = math.inf
+
+
+class Rbf:
+    """rbf::Rbf<3> (include/polatory/rbf/rbf.hpp:11-118)."""
+
+    short_name = ""
+    _kind = -1
+    _polyharmonic = False
+
+    def __init__(self, params=()):
+        params = [float(p) for p in params]
+        if self._polyharmonic:
+            # PolyharmonicOdd/Even::set_parameters: {} -> {1, 0}; {s} -> {s, 0}.
+            if len(params) == 0:
+                params = [1.0, 0.0]
+            elif len(params) == 1:
+                params = [params[0], 0.0]
+        if len(params) != 2:
+            raise ValueError("params.size() must be 2")
+        self._params = params
+        self._aniso = np.eye(3)
+
+    @property
+    def parameters(self):
+        return list(self._params)
+
+    @parameters.setter
+    def parameters(self, p):
+        self.__init__(p)
+
+    @property
+    def anisotropy(self):
+        return self._aniso.copy()
+
+    @anisotropy.setter
+    def anisotropy(self, a):
+        a = np.asarray(a, dtype=np.float64).reshape(3, 3)
+        if not np.linalg.det(a) > 0.0:
+            raise ValueError("aniso must have a positive determinant")
+        self._aniso = a.copy()
+
+    @property
+    def num_parameters(self):
+        return 2
+
+    def _c(self) -> _lib.PgpuRbf:
+        r = _lib.PgpuRbf()
+        r.kind = self._kind
+        r.params[0], r.params[1] = self._params
+        for i, v in enumerate(self._aniso.reshape(-1)):
+            r.aniso[i] = float(v)
+        return r
+
+    @property
+    def cpd_order(self) -> int:
+        out = C.c_int()
+        check(lib.pgpu_rbf_cpd_order(C.byref(self._c()), C.byref(out)))
+        return out.value
+
+    @property
+    def is_covariance_function(self) -> bool:
+        return self.cpd_order == 0
+
+    def support_radius_isotropic(self) -> float:
+        out = C.c_double()
+        check(lib.pgpu_rbf_support_radius_isotropic(C.byref(self._c()), C.byref(out)))
+        return out.value
+
+    def _eval(self, diff, want):
+        d = np.ascontiguousarray(np.asarray(diff, dtype=np.float64).reshape(-1, 3))
+        n = d.shape[0]
+        v = np.empty(n) if want == "v" else None
+        g = np.empty((n, 3)) if want == "g" else None
+        h = np.empty((n, 3, 3)) if want == "h" else None
+        check(lib.pgpu_rbf_evaluate(C.byref(self._c()), ptr(d), n, ptr(v), ptr(g), ptr(h)))
+        return {"v": v, "g": g, "h": h}[want]
+
+    def evaluate(self, diff):
+        out = self._eval(diff, "v")
+        return float(out[0]) if np.asarray(diff).ndim == 1 else out
+
+    def evaluate_gradient(self, diff):
+        out = self._eval(diff, "g")
+        return out[0] if np.asarray(diff).ndim == 1 else out
+
+    def evaluate_hessian(self, diff):
+        out = self._eval(diff, "h")
+        return out[0] if np.asarray(diff).ndim == 1 else out
+
+
+def _make(name, kind, polyharmonic):
+    return type(name, (Rbf,), {"short_name": _lib.RBF_KINDS[kind], "_kind": kind,
+                               "_polyharmonic": polyharmonic})
+
+
+Biharmonic2D = _make("Biharmonic2D", 0, True)
+Biharmonic3D = _make("Biharmonic3D", 1, True)
+CovCubic = _make("CovCubic", 2, False)
+CovExponential = _make("CovExponential", 3, False)
+CovGaussian = _make("CovGaussian", 4, False)
+CovGeneralizedCauchy3 = _make("CovGeneralizedCauchy3", 5, False)
+CovGeneralizedCauchy5 = _make("CovGeneralizedCauchy5", 6, False)
+CovGeneralizedCauchy7 = _make("CovGeneralizedCauchy7", 7, False)
+CovGeneralizedCauchy9 = _make("CovGeneralizedCauchy9", 8, False)
+CovSpherical = _make("CovSpherical", 9, False)
+CovSpheroidal3 = _make("CovSpheroidal3", 10, False)
+CovSpheroidal5 = _make("CovSpheroidal5", 11, False)
+CovSpheroidal7 = _make("CovSpheroidal7", 12, False)
+CovSpheroidal9 = _make("CovSpheroidal9", 13, False)
+Triharmonic2D = _make("Triharmonic2D", 14, True)
+Triharmonic3D = _make("Triharmonic3D", 15, True)
+
+_BY_NAME = {c.short_name: c for c in [
+    Biharmonic2D, Biharmonic3D, CovCubic, CovExponential, CovGaussian, CovGeneralizedCauchy3,
+    CovGeneralizedCauchy5, CovGeneralizedCauchy7, CovGeneralizedCauchy9, CovSpherical,
+    CovSpheroidal3, CovSpheroidal5, CovSpheroidal7, CovSpheroidal9, Triharmonic2D,
+    Triharmonic3D]}
+
+
+def make_rbf(name: str, params) -> Rbf:
+    """rbf::make_rbf (include/polatory/rbf/make_rbf.hpp:24-50)."""
+    if name not in _BY_NAME:
+        raise RuntimeError(f"unknown RBF name: '{name}'")
+    return _BY_NAME[name](params)
+
+
+class Model:
+    """Model<3> (include/polatory/model.hpp:23-183)."""
+
+    MIN_REQUIRED_POLY_DEGREE = -2
+
+    def __init__(self, rbf, poly_degree: int = MIN_REQUIRED_POLY_DEGREE):
+        rbfs = list(rbf) if isinstance(rbf, (list, tuple)) else [rbf]
+        if not rbfs:
+            raise ValueError("rbfs must not be empty")
+        self.rbfs = rbfs
+        self._nugget = 0.0
+        m = self._c(poly_degree)
+        check(lib.pgpu_model_validate(C.byref(m)))
+        min_deg = self.cpd_order - 1
+        self.poly_degree = min_deg if poly_degree == self.MIN_REQUIRED_POLY_DEGREE else poly_degree
+
+    @property
+    def cpd_order(self) -> int:
+        return max(r.cpd_order for r in self.rbfs)
+
+    @property
+    def nugget(self) -> float:
+        return self._nugget
+
+    @nugget.setter
+    def nugget(self, v: float):
+        if not v >= 0.0:
+            raise ValueError("nugget must be non-negative")
+        self._nugget = float(v)
+
+    def set_nugget(self, v: float):
+        self.nugget = v
+
+    @property
+    def poly_basis_size(self) -> int:
+        d = self.poly_degree
+        return 0 if d < 0 else (d + 1) * (d + 2) * (d + 3) // 6
+
+    def _c(self, poly_degree=None) -> _lib.PgpuModel:
+        m = _lib.PgpuModel()
+        m.n_rbfs = len(self.rbfs)
+        m.poly_degree = self.poly_degree if poly_degree is None else poly_degree
+        m.nugget = self._nugget
+        for i, r in enumerate(self.rbfs):
+            m.rbfs[i] = r._c()
+        return m
+
+
+class Interpolant:
+    """Interpolant<3> (include/polatory/interpolant.hpp:54-218) on the GPU library."""
+
+    def __init__(self, model: Model, precision: int = PLAIN):
+        self.model = model
+        self._h = C.c_void_p()
+        check(lib.pgpu_interpolant_create(C.byref(model._c()), C.byref(self._h)))
+        check(lib.pgpu_interpolant_set_precision(self._h, precision))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.pgpu_interpolant_destroy(h)
+            self._h = None
+
+    def set_precision(self, precision: int):
+        check(lib.pgpu_interpolant_set_precision(self._h, precision))
+
+    def fit(self, points, values, tolerance, max_iter=100, accuracy=INF, initial=None, *,
+            grad_points=None, grad_tolerance=INF, grad_accuracy=INF):
+        pts = as_points(points)
+        gpts = as_points(np.zeros((0, 3)) if grad_points is None else grad_points)
+        vals = np.ascontiguousarray(np.asarray(values, dtype=np.float64).reshape(-1))
+        check(lib.pgpu_interpolant_fit(
+            self._h, ptr(pts), pts.shape[0], ptr(gpts) if gpts.shape[0] else None, gpts.shape[0],
+            ptr(vals), float(tolerance), float(grad_tolerance), int(max_iter), float(accuracy),
+            float(grad_accuracy), initial._h if initial is not None else None))
+
+    def evaluate(self, points, accuracy=INF, *, grad_points=None, grad_accuracy=INF):
+        pts = as_points(points)
+        gpts = as_points(np.zeros((0, 3)) if grad_points is None else grad_points)
+        out = np.empty(pts.shape[0] + 3 * gpts.shape[0])
+        check(lib.pgpu_interpolant_evaluate(
+            self._h, ptr(pts), pts.shape[0], ptr(gpts) if gpts.shape[0] else None, gpts.shape[0],
+            float(accuracy), float(grad_accuracy), ptr(out)))
+        return out
+
+    def evaluate_impl(self, points, grad_points=None):
+        pts = as_points(points)
+        gpts = as_points(np.zeros((0, 3)) if grad_points is None else grad_points)
+        out = np.empty(pts.shape[0] + 3 * gpts.shape[0])
+        check(lib.pgpu_interpolant_evaluate_impl(
+            self._h, ptr(pts), pts.shape[0], ptr(gpts) if gpts.shape[0] else None, gpts.shape[0],
+            ptr(out)))
+        return out
+
+    @property
+    def weights(self) -> np.ndarray:
+        n = C.c_int64()
+        check(lib.pgpu_interpolant_num_weights(self._h, C.byref(n)))
+        out = np.empty(n.value)
+        check(lib.pgpu_interpolant_weights(self._h, ptr(out), n.value))
+        return out
+
+    @property
+    def centers(self) -> np.ndarray:
+        mu, sg = C.c_int64(), C.c_int64()
+        check(lib.pgpu_interpolant_num_centers(self._h, C.byref(mu), C.byref(sg)))
+        c = np.empty((mu.value, 3))
+        check(lib.pgpu_interpolant_centers(self._h, ptr(c), None))
+        return c
+
+    @property
+    def bbox(self):
+        b = np.empty(6)
+        check(lib.pgpu_interpolant_bbox(self._h, ptr(b)))
+        return b[:3].copy(), b[3:].copy()
+
+    @property
+    def fit_stats(self) -> dict:
+        s = _lib.PgpuFitStats()
+        check(lib.pgpu_interpolant_fit_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+
+class FmmEvaluator:
+    """fmm::FmmGenericEvaluatorBase<3> (include/polatory/fmm/fmm_evaluator.hpp:17-41)."""
+
+    def __init__(self, rbf: Rbf, bbox, kernel=_lib.KERNEL_VALUE, symmetric=False, precision=PLAIN):
+        b = np.ascontiguousarray(np.asarray(bbox, dtype=np.float64).reshape(6))
+        self._h = C.c_void_p()
+        self._rbf = rbf._c()
+        check(lib.pgpu_evaluator_create(C.byref(self._rbf), kernel, int(symmetric), ptr(b),
+                                        precision, C.byref(self._h)))
+        self._n_trg = 0
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.pgpu_evaluator_destroy(h)
+            self._h = None
+
+    def set_accuracy(self, acc: float):
+        check(lib.pgpu_evaluator_set_accuracy(self._h, float(acc)))
+
+    def set_source_points(self, pts):
+        p = as_points(pts)
+        check(lib.pgpu_evaluator_set_source_points(self._h, ptr(p), p.shape[0]))
+
+    def set_target_points(self, pts):
+        p = as_points(pts)
+        self._n_trg = p.shape[0]
+        check(lib.pgpu_evaluator_set_target_points(self._h, ptr(p), p.shape[0]))
+
+    def set_points(self, pts):
+        p = as_points(pts)
+        self._n_trg = p.shape[0]
+        check(lib.pgpu_evaluator_set_points(self._h, ptr(p), p.shape[0]))
+
+    def set_weights(self, w):
+        w = np.ascontiguousarray(np.asarray(w, dtype=np.float64).reshape(-1))
+        check(lib.pgpu_evaluator_set_weights(self._h, ptr(w), w.shape[0]))
+
+    def evaluate(self) -> np.ndarray:
+        out = np.empty(self._n_trg)
+        check(lib.pgpu_evaluator_evaluate(self._h, ptr(out), self._n_trg))
+        return out

@@ -1,0 +1,586 @@
+// The C ABI (include/polatory_gpu.h): status codes, thread-local error messages, handles.
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <unordered_map>
+
+#include "common.hpp"
+#include "evaluator.hpp"
+#include "model.hpp"
+#include "rbf.cuh"
+#include "solver.hpp"
+
+namespace pgpu {
+void set_device(int device);
+void release_cached_memory();
+}  // namespace pgpu
+
+using namespace pgpu;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    f();
+    g_last_error.clear();
+    return PGPU_OK;
+  } catch (const Error& e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc& e) {
+    g_last_error = "out of host memory";
+    return PGPU_OUT_OF_MEMORY;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return PGPU_RUNTIME_ERROR;
+  } catch (...) {
+    g_last_error = "unknown error";
+    return PGPU_RUNTIME_ERROR;
+  }
+}
+
+void check_ptr(const void* p, const char* name) {
+  if (p == nullptr) throw_invalid(std::string(name) + " must not be null");
+}
+
+}  // namespace
+
+struct pgpu_evaluator {
+  ModelDesc model;
+  int kernel_kind = PGPU_KERNEL_VALUE;
+  bool symmetric = false;
+  int precision = PGPU_PRECISION_PLAIN;
+  Bbox3 bbox;
+  double accuracy = INFINITY;
+  Index n_src = 0, n_trg = 0;
+  DevBuf<double> src, trg, w, out;
+  std::unique_ptr<Evaluator<double>> e64;
+  std::unique_ptr<Evaluator<float>> e32;
+  bool weights_set = false;
+};
+
+struct pgpu_interpolant {
+  ModelDesc model;
+  int precision = PGPU_PRECISION_PLAIN;
+  bool fitted = false;
+  DevBuf<double> centers, grad_centers, weights;
+  std::vector<double> centers_host;
+  Index mu = 0, sigma = 0;
+  Bbox3 bbox;
+  pgpu_fit_stats stats{};
+  // Evaluation state (Interpolant::set_evaluation_bbox_impl).
+  bool eval_ready = false;
+  Bbox3 eval_bbox;
+  double eval_accuracy = INFINITY, eval_grad_accuracy = INFINITY;
+};
+
+extern "C" {
+
+const char* pgpu_last_error(void) { return g_last_error.c_str(); }
+
+int pgpu_version(void) { return 100; }
+
+int pgpu_set_device(int device) {
+  return guarded([&] { set_device(device); });
+}
+
+int pgpu_release_cached_memory(void) {
+  return guarded([&] { release_cached_memory(); });
+}
+
+int pgpu_rbf_evaluate(const pgpu_rbf* rbf, const double* diffs, int64_t n, double* values,
+                      double* gradients, double* hessians) {
+  return guarded([&] {
+    check_ptr(rbf, "rbf");
+    if (n < 0) throw_invalid("n must be non-negative");
+    if (n > 0) check_ptr(diffs, "diffs");
+    if (rbf->kind < 0 || rbf->kind >= PGPU_RBF_COUNT) throw_invalid("unknown RBF kind");
+    if (hessians && !kind_has_hessian(rbf->kind)) {
+      throw_runtime(std::string(rbf->kind == PGPU_RBF_CUB ? "cov_cubic" : "cov_spherical") +
+                    "::evaluate_hessian_isotropic is not implemented");
+    }
+    const double* a = rbf->aniso;
+    KParams<double> kp{rbf->params[0], rbf->params[1]};
+    for (int64_t i = 0; i < n; ++i) {
+      const double* d = diffs + 3 * i;
+      double t[3];
+      for (int r = 0; r < 3; ++r) t[r] = a[3 * r] * d[0] + a[3 * r + 1] * d[1] + a[3 * r + 2] * d[2];
+      const double r2 = t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
+      dispatch_kind(rbf->kind, [&]<int K>() {
+        if (values) values[i] = rbf_value<K>(r2, kp);
+        if (gradients) {
+          double c = rbf_gcoef<K>(r2, kp);
+          double g[3] = {c * t[0], c * t[1], c * t[2]};
+          // row vector g * A (rbf_base.hpp:45-48)
+          for (int k = 0; k < 3; ++k) gradients[3 * i + k] = g[0] * a[k] + g[1] * a[3 + k] + g[2] * a[6 + k];
+        }
+        if (hessians) {
+          double ha, hb;
+          rbf_hess<K>(r2, kp, ha, hb);
+          double h[9];
+          for (int p = 0; p < 3; ++p)
+            for (int q = 0; q < 3; ++q) h[3 * p + q] = (p == q ? ha : 0.0) + hb * t[p] * t[q];
+          // A^T H A (rbf_base.hpp:50-53)
+          for (int p = 0; p < 3; ++p)
+            for (int q = 0; q < 3; ++q) {
+              double s = 0;
+              for (int u = 0; u < 3; ++u)
+                for (int v = 0; v < 3; ++v) s += a[3 * u + p] * h[3 * u + v] * a[3 * v + q];
+              hessians[9 * i + 3 * p + q] = s;
+            }
+        }
+        return 0;
+      });
+    }
+  });
+}
+
+int pgpu_rbf_cpd_order(const pgpu_rbf* rbf, int* out) {
+  return guarded([&] {
+    check_ptr(rbf, "rbf");
+    check_ptr(out, "out");
+    if (rbf->kind < 0 || rbf->kind >= PGPU_RBF_COUNT) throw_invalid("unknown RBF kind");
+    *out = kind_cpd_order(rbf->kind);
+  });
+}
+
+int pgpu_rbf_support_radius_isotropic(const pgpu_rbf* rbf, double* out) {
+  return guarded([&] {
+    check_ptr(rbf, "rbf");
+    check_ptr(out, "out");
+    if (rbf->kind < 0 || rbf->kind >= PGPU_RBF_COUNT) throw_invalid("unknown RBF kind");
+    *out = support_radius_isotropic(rbf->kind, rbf->params);
+  });
+}
+
+int pgpu_model_validate(const pgpu_model* model) {
+  return guarded([&] { model_from_c(model); });
+}
+
+int pgpu_model_poly_basis_size(const pgpu_model* model, int64_t* out) {
+  return guarded([&] {
+    check_ptr(out, "out");
+    *out = model_from_c(model).l();
+  });
+}
+
+// ---- evaluator ------------------------------------------------------------------------
+
+int pgpu_evaluator_create(const pgpu_rbf* rbf, int kernel_kind, int symmetric,
+                          const double bbox[6], int precision, pgpu_evaluator** out) {
+  return guarded([&] {
+    check_ptr(rbf, "rbf");
+    check_ptr(out, "out");
+    check_ptr(bbox, "bbox");
+    if (kernel_kind != PGPU_KERNEL_VALUE)
+      throw Error(PGPU_NOT_IMPLEMENTED, "only the value kernel is exposed as an evaluator so far");
+    pgpu_model m{};
+    m.n_rbfs = 1;
+    m.rbfs[0] = *rbf;
+    m.poly_degree = -1;
+    // Validation of the kernel alone (no polynomial constraint on a bare evaluator).
+    if (rbf->kind < 0 || rbf->kind >= PGPU_RBF_COUNT) throw_invalid("unknown RBF kind");
+    ModelDesc d;
+    RbfDesc rd;
+    rd.kind = rbf->kind;
+    rd.p[0] = rbf->params[0];
+    rd.p[1] = rbf->params[1];
+    for (int k = 0; k < 9; ++k) rd.a[k] = rbf->aniso[k];
+    if (!(det3(rd.a) > 0.0)) throw_invalid("aniso must have a positive determinant");
+    d.rbfs.push_back(rd);
+    d.poly_degree = -1;
+    auto ev = std::make_unique<pgpu_evaluator>();
+    ev->model = d;
+    ev->kernel_kind = kernel_kind;
+    ev->symmetric = symmetric != 0;
+    ev->precision = precision;
+    for (int k = 0; k < 3; ++k) {
+      ev->bbox.min[k] = bbox[k];
+      ev->bbox.max[k] = bbox[3 + k];
+    }
+    *out = ev.release();
+  });
+}
+
+int pgpu_evaluator_destroy(pgpu_evaluator* ev) {
+  return guarded([&] { delete ev; });
+}
+
+int pgpu_evaluator_set_accuracy(pgpu_evaluator* ev, double accuracy) {
+  return guarded([&] {
+    check_ptr(ev, "evaluator");
+    ev->accuracy = accuracy;
+    ev->e64.reset();
+    ev->e32.reset();
+  });
+}
+
+namespace {
+void rebuild(pgpu_evaluator* ev) {
+  if (ev->precision == PGPU_PRECISION_PLAIN) {
+    ev->e64 = std::make_unique<Evaluator<double>>(ev->model, ev->bbox, ev->accuracy, ev->accuracy);
+    if (ev->symmetric) ev->e64->set_points(ev->src.data(), ev->n_src, nullptr, 0);
+    else {
+      ev->e64->set_sources(ev->src.data(), ev->n_src, nullptr, 0);
+      ev->e64->set_targets(ev->trg.data(), ev->n_trg, nullptr, 0);
+    }
+  } else {
+    ev->e32 = std::make_unique<Evaluator<float>>(ev->model, ev->bbox, ev->accuracy, ev->accuracy);
+    if (ev->symmetric) ev->e32->set_points(ev->src.data(), ev->n_src, nullptr, 0);
+    else {
+      ev->e32->set_sources(ev->src.data(), ev->n_src, nullptr, 0);
+      ev->e32->set_targets(ev->trg.data(), ev->n_trg, nullptr, 0);
+    }
+  }
+}
+}  // namespace
+
+int pgpu_evaluator_set_source_points(pgpu_evaluator* ev, const double* points, int64_t n) {
+  return guarded([&] {
+    check_ptr(ev, "evaluator");
+    if (ev->symmetric) throw_invalid("symmetric evaluators take set_points");
+    if (n < 0) throw_invalid("n must be non-negative");
+    copy_in(ev->src, points, 3 * n);
+    ev->n_src = n;
+    ev->e64.reset();
+    ev->e32.reset();
+    ev->weights_set = false;
+  });
+}
+
+int pgpu_evaluator_set_target_points(pgpu_evaluator* ev, const double* points, int64_t n) {
+  return guarded([&] {
+    check_ptr(ev, "evaluator");
+    if (ev->symmetric) throw_invalid("symmetric evaluators take set_points");
+    if (n < 0) throw_invalid("n must be non-negative");
+    copy_in(ev->trg, points, 3 * n);
+    ev->n_trg = n;
+    ev->e64.reset();
+    ev->e32.reset();
+  });
+}
+
+int pgpu_evaluator_set_points(pgpu_evaluator* ev, const double* points, int64_t n) {
+  return guarded([&] {
+    check_ptr(ev, "evaluator");
+    if (!ev->symmetric) throw_invalid("set_points needs a symmetric evaluator");
+    if (n < 0) throw_invalid("n must be non-negative");
+    copy_in(ev->src, points, 3 * n);
+    ev->n_src = ev->n_trg = n;
+    ev->e64.reset();
+    ev->e32.reset();
+    ev->weights_set = false;
+  });
+}
+
+int pgpu_evaluator_set_weights(pgpu_evaluator* ev, const double* weights, int64_t n) {
+  return guarded([&] {
+    check_ptr(ev, "evaluator");
+    if (n != ev->n_src) throw_invalid("weights must have km * n_sources entries");
+    copy_in(ev->w, weights, n);
+    ev->weights_set = true;
+  });
+}
+
+int pgpu_evaluator_evaluate(pgpu_evaluator* ev, double* out, int64_t n) {
+  return guarded([&] {
+    check_ptr(ev, "evaluator");
+    if (n != ev->n_trg) throw_invalid("out must have kn * n_targets entries");
+    if (!ev->weights_set) throw_runtime("weights have not been set");
+    if (!ev->e64 && !ev->e32) rebuild(ev);
+    ev->out.resize(std::max<int64_t>(n, 1));
+    if (ev->e64) {
+      ev->e64->set_weights(ev->w.data());
+      ev->e64->evaluate(ev->out.data(), false);
+    } else {
+      ev->e32->set_weights(ev->w.data());
+      ev->e32->evaluate(ev->out.data(), false);
+    }
+    copy_out(out, ev->out.data(), n);
+  });
+}
+
+// ---- interpolant ----------------------------------------------------------------------
+
+int pgpu_interpolant_create(const pgpu_model* model, pgpu_interpolant** out) {
+  return guarded([&] {
+    check_ptr(out, "out");
+    auto it = std::make_unique<pgpu_interpolant>();
+    it->model = model_from_c(model);
+    *out = it.release();
+  });
+}
+
+int pgpu_interpolant_destroy(pgpu_interpolant* it) {
+  return guarded([&] { delete it; });
+}
+
+int pgpu_interpolant_set_precision(pgpu_interpolant* it, int precision) {
+  return guarded([&] {
+    check_ptr(it, "interpolant");
+    if (precision != PGPU_PRECISION_PLAIN && precision != PGPU_PRECISION_MIXED)
+      throw_invalid("unknown precision");
+    it->precision = precision;
+  });
+}
+
+namespace {
+
+std::vector<double> host_copy(const double* p, size_t n) {
+  std::vector<double> v(n);
+  if (n == 0) return v;
+  if (is_device_pointer(p)) {
+    PGPU_CUDA(cudaMemcpy(v.data(), p, n * sizeof(double), cudaMemcpyDeviceToHost));
+  } else {
+    std::memcpy(v.data(), p, n * sizeof(double));
+  }
+  return v;
+}
+
+// Interpolant::check_* (interpolant.hpp:275-315).
+void check_fit_args(const ModelDesc& m, int64_t mu, int64_t sigma, double tol, double grad_tol,
+                    int max_iter, double acc, double grad_acc) {
+  const int l = m.l();
+  if (mu < 0 || sigma < 0) throw_invalid("point counts must be non-negative");
+  if (!(m.poly_degree == 1 && mu == 1 && sigma >= 1) && mu < l)
+    throw_invalid("points.rows() must be greater than or equal to " + std::to_string(l));
+  if (!(tol > 0.0)) throw_invalid("tolerance must be positive");
+  if (!(grad_tol > 0.0)) throw_invalid("grad_tolerance must be positive");
+  if (max_iter < 0) throw_invalid("max_iter must be nonnegative");
+  if (!(acc > 0.0)) throw_invalid("accuracy must be positive");
+  if (!(grad_acc > 0.0)) throw_invalid("grad_accuracy must be positive");
+}
+
+}  // namespace
+
+int pgpu_interpolant_fit(pgpu_interpolant* it, const double* points, int64_t mu,
+                         const double* grad_points, int64_t sigma, const double* values,
+                         double tolerance, double grad_tolerance, int max_iter, double accuracy,
+                         double grad_accuracy, const pgpu_interpolant* initial) {
+  return guarded([&] {
+    check_ptr(it, "interpolant");
+    check_fit_args(it->model, mu, sigma, tolerance, grad_tolerance, max_iter, accuracy,
+                   grad_accuracy);
+    if (mu > 0) check_ptr(points, "points");
+    if (sigma > 0) check_ptr(grad_points, "grad_points");
+    check_ptr(values, "values");
+    const int l = it->model.l();
+    auto pts = host_copy(points, 3 * mu);
+    auto gpts = host_copy(grad_points, 3 * sigma);
+    auto vals = host_copy(values, mu + 3 * sigma);
+
+    std::vector<double> init;
+    if (initial != nullptr && initial->fitted) {
+      // Interpolant::build_initial_weights (interpolant.hpp:232-273): copy the weights of the
+      // centres that reappear (exact coordinate match) and the polynomial coefficients.
+      init.assign(mu + 3 * sigma + l, 0.0);
+      const bool same_model = initial->model.poly_degree == it->model.poly_degree &&
+                              initial->model.nugget == it->model.nugget &&
+                              initial->model.rbfs.size() == it->model.rbfs.size();
+      if (same_model) {
+        auto iw = initial->weights.to_host();
+        std::unordered_map<std::string, Index> pos;
+        for (Index i = 0; i < initial->mu; ++i)
+          pos.emplace(std::string(reinterpret_cast<const char*>(&initial->centers_host[3 * i]),
+                                  3 * sizeof(double)),
+                      i);
+        for (Index i = 0; i < mu; ++i) {
+          auto f = pos.find(std::string(reinterpret_cast<const char*>(&pts[3 * i]), 3 * sizeof(double)));
+          if (f != pos.end()) init[i] = iw[f->second];
+        }
+        for (int k = 0; k < l; ++k) init[mu + 3 * sigma + k] = iw[iw.size() - l + k];
+      }
+    }
+
+    it->fitted = false;
+    FitRequest req;
+    req.model = &it->model;
+    req.points_host = pts.data();
+    req.mu = mu;
+    req.grad_points_host = gpts.data();
+    req.sigma = sigma;
+    req.values_host = vals.data();
+    req.tolerance = tolerance;
+    req.grad_tolerance = grad_tolerance;
+    req.max_iter = max_iter;
+    req.accuracy = accuracy;
+    req.grad_accuracy = grad_accuracy;
+    req.initial_weights = init.empty() ? nullptr : init.data();
+    req.precision = it->precision;
+    req.verbose = std::getenv("PGPU_VERBOSE") != nullptr;
+    FitResult r = fit(req);
+
+    it->weights.upload(r.weights);
+    it->centers.upload(pts);
+    it->grad_centers.upload(gpts);
+    it->centers_host = std::move(pts);
+    it->mu = mu;
+    it->sigma = sigma;
+    it->bbox = Bbox3::from_host_points(it->centers_host.data(), mu)
+                   .hull(Bbox3::from_host_points(gpts.data(), sigma));
+    it->stats.iterations = r.iterations;
+    it->stats.levels = r.levels;
+    it->stats.residual = r.residual;
+    it->stats.grad_residual = r.grad_residual;
+    it->stats.setup_seconds = r.setup_seconds;
+    it->stats.solve_seconds = r.solve_seconds;
+    it->stats.n_domains = r.n_domains;
+    it->fitted = true;
+    it->eval_ready = false;
+  });
+}
+
+namespace {
+void throw_if_not_fitted(const pgpu_interpolant* it) {
+  check_ptr(it, "interpolant");
+  if (!it->fitted) throw_runtime("interpolant has not been fitted");
+}
+
+void run_evaluate(pgpu_interpolant* it, const double* points, int64_t m, const double* grad_points,
+                  int64_t mg, double* out) {
+  if (m < 0 || mg < 0) throw_invalid("point counts must be non-negative");
+  if (m > 0) check_ptr(points, "points");
+  if (mg > 0) check_ptr(grad_points, "grad_points");
+  if (m + 3 * mg > 0) check_ptr(out, "out");
+  DevBuf<double> q, gq, o;
+  copy_in(q, points, 3 * m);
+  copy_in(gq, grad_points, 3 * mg);
+  o.resize(std::max<int64_t>(m + 3 * mg, 1));
+  EvaluateRequest req;
+  req.model = &it->model;
+  req.centers_dev = it->centers.data();
+  req.mu = it->mu;
+  req.grad_centers_dev = it->grad_centers.data();
+  req.sigma = it->sigma;
+  req.weights_dev = it->weights.data();
+  req.bbox = it->eval_bbox;
+  req.points_dev = q.data();
+  req.m = m;
+  req.grad_points_dev = gq.data();
+  req.mg = mg;
+  req.accuracy = it->eval_accuracy;
+  req.grad_accuracy = it->eval_grad_accuracy;
+  req.precision = it->precision;
+  req.out_dev = o.data();
+  evaluate(req);
+  copy_out(out, o.data(), m + 3 * mg);
+}
+}  // namespace
+
+int pgpu_interpolant_set_evaluation_bbox(pgpu_interpolant* it, const double bbox[6],
+                                         double accuracy, double grad_accuracy) {
+  return guarded([&] {
+    throw_if_not_fitted(it);
+    check_ptr(bbox, "bbox");
+    Bbox3 b;
+    for (int k = 0; k < 3; ++k) {
+      b.min[k] = bbox[k];
+      b.max[k] = bbox[3 + k];
+    }
+    it->eval_bbox = b.hull(it->bbox);
+    it->eval_accuracy = accuracy;
+    it->eval_grad_accuracy = grad_accuracy;
+    it->eval_ready = true;
+  });
+}
+
+int pgpu_interpolant_evaluate(pgpu_interpolant* it, const double* points, int64_t m,
+                              const double* grad_points, int64_t mg, double accuracy,
+                              double grad_accuracy, double* out) {
+  return guarded([&] {
+    throw_if_not_fitted(it);
+    if (!(accuracy > 0.0)) throw_invalid("accuracy must be positive");
+    if (!(grad_accuracy > 0.0)) throw_invalid("grad_accuracy must be positive");
+    Bbox3 b;
+    if (m > 0) {
+      auto hp = host_copy(points, 3 * m);
+      b = Bbox3::from_host_points(hp.data(), m);
+    }
+    if (mg > 0) {
+      auto hg = host_copy(grad_points, 3 * mg);
+      b = b.hull(Bbox3::from_host_points(hg.data(), mg));
+    }
+    it->eval_bbox = b.hull(it->bbox);
+    it->eval_accuracy = accuracy;
+    it->eval_grad_accuracy = grad_accuracy;
+    it->eval_ready = true;
+    run_evaluate(it, points, m, grad_points, mg, out);
+  });
+}
+
+int pgpu_interpolant_evaluate_impl(pgpu_interpolant* it, const double* points, int64_t m,
+                                   const double* grad_points, int64_t mg, double* out) {
+  return guarded([&] {
+    throw_if_not_fitted(it);
+    if (!it->eval_ready) {
+      it->eval_bbox = it->bbox;
+      it->eval_ready = true;
+    }
+    run_evaluate(it, points, m, grad_points, mg, out);
+  });
+}
+
+int pgpu_interpolant_is_fitted(const pgpu_interpolant* it, int* out) {
+  return guarded([&] {
+    check_ptr(it, "interpolant");
+    check_ptr(out, "out");
+    *out = it->fitted ? 1 : 0;
+  });
+}
+
+int pgpu_interpolant_num_weights(const pgpu_interpolant* it, int64_t* out) {
+  return guarded([&] {
+    throw_if_not_fitted(it);
+    check_ptr(out, "out");
+    *out = static_cast<int64_t>(it->weights.size());
+  });
+}
+
+int pgpu_interpolant_weights(const pgpu_interpolant* it, double* out, int64_t n) {
+  return guarded([&] {
+    throw_if_not_fitted(it);
+    if (n != static_cast<int64_t>(it->weights.size())) throw_invalid("wrong weights length");
+    copy_out(out, it->weights.data(), n);
+  });
+}
+
+int pgpu_interpolant_num_centers(const pgpu_interpolant* it, int64_t* mu, int64_t* sigma) {
+  return guarded([&] {
+    throw_if_not_fitted(it);
+    if (mu) *mu = it->mu;
+    if (sigma) *sigma = it->sigma;
+  });
+}
+
+int pgpu_interpolant_centers(const pgpu_interpolant* it, double* centers, double* grad_centers) {
+  return guarded([&] {
+    throw_if_not_fitted(it);
+    if (centers && it->mu) copy_out(centers, it->centers.data(), 3 * it->mu);
+    if (grad_centers && it->sigma) copy_out(grad_centers, it->grad_centers.data(), 3 * it->sigma);
+  });
+}
+
+int pgpu_interpolant_bbox(const pgpu_interpolant* it, double bbox[6]) {
+  return guarded([&] {
+    throw_if_not_fitted(it);
+    check_ptr(bbox, "bbox");
+    for (int k = 0; k < 3; ++k) {
+      bbox[k] = it->bbox.min[k];
+      bbox[3 + k] = it->bbox.max[k];
+    }
+  });
+}
+
+int pgpu_interpolant_fit_stats(const pgpu_interpolant* it, pgpu_fit_stats* out) {
+  return guarded([&] {
+    throw_if_not_fitted(it);
+    check_ptr(out, "out");
+    *out = it->stats;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,132 @@
+// Internal infrastructure of libpolatory_gpu: error type, CUDA checks, device buffers and the
+// per-thread library context (device, stream). Host-only header (also included by .cu files).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "polatory_gpu.h"
+
+namespace pgpu {
+
+using Index = int64_t;
+
+// Internal exception; converted to a status code at the C ABI.
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& msg) : std::runtime_error(msg), code(c) {}
+};
+
+[[noreturn]] inline void throw_invalid(const std::string& msg) {
+  throw Error(PGPU_INVALID_ARGUMENT, msg);
+}
+[[noreturn]] inline void throw_runtime(const std::string& msg) {
+  throw Error(PGPU_RUNTIME_ERROR, msg);
+}
+
+#define PGPU_CUDA(expr)                                                                    \
+  do {                                                                                     \
+    cudaError_t e_ = (expr);                                                               \
+    if (e_ != cudaSuccess) {                                                               \
+      throw ::pgpu::Error(e_ == cudaErrorMemoryAllocation ? PGPU_OUT_OF_MEMORY             \
+                                                          : PGPU_CUDA_ERROR,               \
+                          std::string(#expr) + ": " + cudaGetErrorString(e_) + " at " +    \
+                              __FILE__ + ":" + std::to_string(__LINE__));                  \
+    }                                                                                      \
+  } while (0)
+
+#define PGPU_LAUNCH_CHECK() PGPU_CUDA(cudaGetLastError())
+
+// Library stream (one per host thread; the reference's evaluators are single-thread-affine).
+cudaStream_t stream();
+void set_stream(cudaStream_t s);
+
+// Device memory from the stream-ordered pool of the current device.
+void* dev_alloc(size_t bytes);
+void dev_free(void* p);
+
+template <class T>
+class DevBuf {
+ public:
+  DevBuf() = default;
+  explicit DevBuf(size_t n) { resize(n); }
+  ~DevBuf() { release(); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p_(o.p_), n_(o.n_) {
+    o.p_ = nullptr;
+    o.n_ = 0;
+  }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p_ = o.p_;
+      n_ = o.n_;
+      o.p_ = nullptr;
+      o.n_ = 0;
+    }
+    return *this;
+  }
+  void resize(size_t n) {
+    if (n == n_) return;
+    release();
+    if (n > 0) p_ = static_cast<T*>(dev_alloc(n * sizeof(T)));
+    n_ = n;
+  }
+  void release() {
+    if (p_) dev_free(p_);
+    p_ = nullptr;
+    n_ = 0;
+  }
+  void zero() {
+    if (n_) PGPU_CUDA(cudaMemsetAsync(p_, 0, n_ * sizeof(T), stream()));
+  }
+  void upload(const T* h, size_t n) {
+    resize(n);
+    if (n) PGPU_CUDA(cudaMemcpyAsync(p_, h, n * sizeof(T), cudaMemcpyHostToDevice, stream()));
+  }
+  void upload(const std::vector<T>& v) { upload(v.data(), v.size()); }
+  void download(T* h, size_t n) const {
+    if (n) PGPU_CUDA(cudaMemcpyAsync(h, p_, n * sizeof(T), cudaMemcpyDeviceToHost, stream()));
+  }
+  std::vector<T> to_host() const {
+    std::vector<T> v(n_);
+    download(v.data(), n_);
+    PGPU_CUDA(cudaStreamSynchronize(stream()));
+    return v;
+  }
+  T* data() { return p_; }
+  const T* data() const { return p_; }
+  size_t size() const { return n_; }
+
+ private:
+  T* p_ = nullptr;
+  size_t n_ = 0;
+};
+
+// True when p is a device (or managed) pointer.
+bool is_device_pointer(const void* p);
+
+// Copies n doubles from a host-or-device pointer into a device buffer.
+void copy_in(DevBuf<double>& dst, const double* src, size_t n);
+// Copies n doubles from a device buffer to a host-or-device pointer (synchronizes).
+void copy_out(double* dst, const double* src_dev, size_t n);
+
+inline void sync() { PGPU_CUDA(cudaStreamSynchronize(stream())); }
+
+inline int blocks_for(Index n, int threads) {
+  Index b = (n + threads - 1) / threads;
+  return static_cast<int>(b < 1 ? 1 : b);
+}
+
+int num_sms();
+
+// Monotonic host clock in seconds.
+double wall_seconds();
+
+}  // namespace pgpu

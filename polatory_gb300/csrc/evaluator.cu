@@ -1,0 +1,272 @@
+// Evaluator<T> implementation: per-RBF frames (A-transformed, centred positions), weight
+// preparation, and the choice between the exact direct backend and the FMM backend.
+#include <algorithm>
+
+#include "direct.hpp"
+#include "evaluator.hpp"
+#include "fmm.hpp"
+#include "linalg.hpp"
+
+namespace pgpu {
+
+namespace {
+
+template <class T>
+__global__ void to_frame_kernel(const double* __restrict__ pts, Index n, Mat3 a, double ox,
+                                double oy, double oz, P4<T>* __restrict__ out) {
+  Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x = pts[3 * i], y = pts[3 * i + 1], z = pts[3 * i + 2];
+  double tx, ty, tz;
+  mat3_vec(a.a, x, y, z, tx, ty, tz);
+  out[i] = P4<T>{static_cast<T>(tx - ox), static_cast<T>(ty - oy), static_cast<T>(tz - oz), T(0)};
+}
+
+template <class T>
+__global__ void prep_weights_kernel(const double* __restrict__ w, Index mu, Index sigma, Mat3 a,
+                                    T* __restrict__ vw, T* __restrict__ gg) {
+  Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < mu) {
+    vw[i] = static_cast<T>(w[i]);
+  } else if (i < mu + sigma) {
+    Index j = i - mu;
+    const double* g = w + mu + 3 * j;
+    double gx, gy, gz;
+    mat3_vec(a.a, g[0], g[1], g[2], gx, gy, gz);
+    gg[3 * j] = static_cast<T>(gx);
+    gg[3 * j + 1] = static_cast<T>(gy);
+    gg[3 * j + 2] = static_cast<T>(gz);
+  }
+}
+
+__global__ void bbox_kernel(const double* __restrict__ pts, Index n, double* __restrict__ part) {
+  __shared__ double sh[6][256];
+  double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<Index>(gridDim.x) * blockDim.x) {
+    for (int k = 0; k < 3; ++k) {
+      double v = pts[3 * i + k];
+      mn[k] = fmin(mn[k], v);
+      mx[k] = fmax(mx[k], v);
+    }
+  }
+  for (int k = 0; k < 3; ++k) {
+    sh[k][threadIdx.x] = mn[k];
+    sh[3 + k][threadIdx.x] = mx[k];
+  }
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      for (int k = 0; k < 3; ++k) {
+        sh[k][threadIdx.x] = fmin(sh[k][threadIdx.x], sh[k][threadIdx.x + s]);
+        sh[3 + k][threadIdx.x] = fmax(sh[3 + k][threadIdx.x], sh[3 + k][threadIdx.x + s]);
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 6; ++k) part[6 * blockIdx.x + k] = sh[k][0];
+}
+
+// Transformed bbox (geometry/bbox3d.hpp:66: Bbox::transform from the 8 corners).
+void transformed_bbox(const Bbox3& b, const double* a, double* tmin, double* tmax) {
+  for (int k = 0; k < 3; ++k) {
+    tmin[k] = INFINITY;
+    tmax[k] = -INFINITY;
+  }
+  for (int c = 0; c < 8; ++c) {
+    double p[3] = {(c & 1) ? b.max[0] : b.min[0], (c & 2) ? b.max[1] : b.min[1],
+                   (c & 4) ? b.max[2] : b.min[2]};
+    for (int r = 0; r < 3; ++r) {
+      double v = a[3 * r] * p[0] + a[3 * r + 1] * p[1] + a[3 * r + 2] * p[2];
+      tmin[r] = std::min(tmin[r], v);
+      tmax[r] = std::max(tmax[r], v);
+    }
+  }
+}
+
+}  // namespace
+
+Bbox3 bbox_of_device_points(const double* pts, Index n) {
+  Bbox3 b;
+  if (n == 0) return b;
+  const int nblk = std::min<Index>(blocks_for(n, 256), 1024);
+  DevBuf<double> part(6 * nblk);
+  bbox_kernel<<<nblk, 256, 0, stream()>>>(pts, n, part.data());
+  PGPU_LAUNCH_CHECK();
+  auto h = part.to_host();
+  for (int i = 0; i < nblk; ++i)
+    for (int k = 0; k < 3; ++k) {
+      b.min[k] = std::min(b.min[k], h[6 * i + k]);
+      b.max[k] = std::max(b.max[k], h[6 * i + 3 + k]);
+    }
+  return b;
+}
+
+template <class T>
+struct Evaluator<T>::Term {
+  RbfDesc rbf;
+  Mat3 a;
+  double origin[3];
+  double box_min[3];
+  double box_width;
+  KParams<T> kp;
+  DevBuf<P4<T>> spos, sgpos, tpos, tgpos;
+  DevBuf<T> vw, gg;
+  std::unique_ptr<Fmm<T>> fmm;
+  bool fmm_sources_dirty = true;
+  bool fmm_targets_dirty = true;
+};
+
+template <class T>
+Evaluator<T>::Evaluator(const ModelDesc& model, const Bbox3& bbox, double accuracy,
+                        double grad_accuracy)
+    : model_(model), bbox_(bbox), accuracy_(accuracy), grad_accuracy_(grad_accuracy) {
+  for (const auto& r : model_.rbfs) {
+    auto t = std::make_unique<Term>();
+    t->rbf = r;
+    for (int k = 0; k < 9; ++k) t->a.a[k] = r.a[k];
+    double tmin[3], tmax[3];
+    if (bbox_.empty()) {
+      for (int k = 0; k < 3; ++k) tmin[k] = tmax[k] = 0.0;
+    } else {
+      transformed_bbox(bbox_, r.a, tmin, tmax);
+    }
+    // The cube of src/fmm/utility.hpp:18-33 (make_box): 1.01 x the largest side.
+    double w = 0;
+    for (int k = 0; k < 3; ++k) w = std::max(w, tmax[k] - tmin[k]);
+    w *= 1.01;
+    if (w == 0.0) w = 1.0;
+    for (int k = 0; k < 3; ++k) {
+      t->origin[k] = 0.5 * (tmin[k] + tmax[k]);
+      t->box_min[k] = t->origin[k] - 0.5 * w;
+    }
+    t->box_width = w;
+    t->kp = KParams<T>{static_cast<T>(r.p[0]), static_cast<T>(r.p[1])};
+    terms_.push_back(std::move(t));
+  }
+}
+
+template <class T>
+Evaluator<T>::~Evaluator() = default;
+
+template <class T>
+void Evaluator<T>::set_sources(const double* pts, Index mu, const double* gpts, Index sigma) {
+  symmetric_ = false;
+  mu_ = mu;
+  sigma_ = sigma;
+  spts_ = pts;
+  sgpts_ = gpts;
+  for (auto& t : terms_) {
+    t->spos.resize(mu);
+    t->sgpos.resize(sigma);
+    if (mu)
+      to_frame_kernel<T><<<blocks_for(mu, 256), 256, 0, stream()>>>(
+          pts, mu, t->a, t->origin[0], t->origin[1], t->origin[2], t->spos.data());
+    if (sigma)
+      to_frame_kernel<T><<<blocks_for(sigma, 256), 256, 0, stream()>>>(
+          gpts, sigma, t->a, t->origin[0], t->origin[1], t->origin[2], t->sgpos.data());
+    PGPU_LAUNCH_CHECK();
+    t->vw.resize(mu);
+    t->gg.resize(3 * sigma);
+    t->fmm_sources_dirty = true;
+  }
+}
+
+template <class T>
+void Evaluator<T>::set_targets(const double* pts, Index m, const double* gpts, Index mg) {
+  m_ = m;
+  mg_ = mg;
+  tpts_ = pts;
+  tgpts_ = gpts;
+  for (auto& t : terms_) {
+    t->tpos.resize(m);
+    t->tgpos.resize(mg);
+    if (m)
+      to_frame_kernel<T><<<blocks_for(m, 256), 256, 0, stream()>>>(
+          pts, m, t->a, t->origin[0], t->origin[1], t->origin[2], t->tpos.data());
+    if (mg)
+      to_frame_kernel<T><<<blocks_for(mg, 256), 256, 0, stream()>>>(
+          gpts, mg, t->a, t->origin[0], t->origin[1], t->origin[2], t->tgpos.data());
+    PGPU_LAUNCH_CHECK();
+    t->fmm_targets_dirty = true;
+  }
+}
+
+template <class T>
+void Evaluator<T>::set_points(const double* pts, Index mu, const double* gpts, Index sigma) {
+  set_sources(pts, mu, gpts, sigma);
+  set_targets(pts, mu, gpts, sigma);
+  symmetric_ = true;
+}
+
+template <class T>
+void Evaluator<T>::set_weights(const double* w) {
+  const int l = model_.l();
+  for (auto& t : terms_) {
+    if (mu_ + sigma_ > 0) {
+      prep_weights_kernel<T><<<blocks_for(mu_ + sigma_, 256), 256, 0, stream()>>>(
+          w, mu_, sigma_, t->a, t->vw.data(), t->gg.data());
+      PGPU_LAUNCH_CHECK();
+    }
+  }
+  poly_c_.assign(l, 0.0);
+  if (l > 0) {
+    PGPU_CUDA(cudaMemcpyAsync(poly_c_.data(), w + mu_ + 3 * sigma_, l * sizeof(double),
+                              cudaMemcpyDeviceToHost, stream()));
+    sync();
+  }
+}
+
+// Direct sums are exact and, on this GPU, cheaper than building a tree until the pair count
+// reaches a few hundred million; the reference's CPU threshold is N*M < 2^20
+// (src/fmm/fmm_evaluator.hpp:227).
+constexpr double kDirectPairLimit = 1.0 * (1 << 26);
+
+template <class T>
+void Evaluator<T>::evaluate(double* out, bool with_poly) {
+  const Index nout = m_ + 3 * mg_;
+  fill(out, nout, 0.0);
+  double* out_v = out;
+  double* out_g = out + m_;
+  stats_ = EvalStats{};
+  const double pairs = static_cast<double>(mu_ + sigma_) * static_cast<double>(m_ + mg_);
+  for (auto& tp : terms_) {
+    Term& t = *tp;
+    bool use_fmm = !force_direct_ && pairs > kDirectPairLimit && Fmm<T>::supported(t.rbf.kind);
+    if (!use_fmm) {
+      DirectSources<T> src{t.spos.data(), t.vw.data(), mu_, t.sgpos.data(), t.gg.data(), sigma_};
+      DirectTargets<T> trg{t.tpos.data(), m_, out_v, t.tgpos.data(), mg_, out_g};
+      direct_evaluate<T>(t.rbf.kind, t.kp, t.a, src, trg, stream());
+      stats_.direct_pairs += static_cast<Index>(pairs);
+    } else {
+      if (!t.fmm) {
+        double acc = std::min(accuracy_, grad_accuracy_);
+        double rel_min[3];
+        for (int k = 0; k < 3; ++k) rel_min[k] = t.box_min[k] - t.origin[k];
+        t.fmm = std::make_unique<Fmm<T>>(t.rbf.kind, t.kp, t.a, rel_min, t.box_width, acc);
+        if (ff_set_) t.fmm->set_config(ff_);
+      }
+      if (t.fmm_sources_dirty || t.fmm_targets_dirty) {
+        if (symmetric_) {
+          t.fmm->set_points(t.spos.data(), mu_, t.sgpos.data(), sigma_);
+        } else {
+          if (t.fmm_sources_dirty) t.fmm->set_sources(t.spos.data(), mu_, t.sgpos.data(), sigma_);
+          if (t.fmm_targets_dirty) t.fmm->set_targets(t.tpos.data(), m_, t.tgpos.data(), mg_);
+        }
+        t.fmm_sources_dirty = t.fmm_targets_dirty = false;
+      }
+      t.fmm->evaluate(t.vw.data(), t.gg.data(), out_v, out_g);
+      stats_.near_pairs += t.fmm->near_pairs();
+      stats_.backend = 1;
+    }
+  }
+  if (with_poly && model_.l() > 0) {
+    poly_eval_add(model_.poly_degree, poly_c_.data(), tpts_, m_, tgpts_, mg_, out);
+  }
+}
+
+template class Evaluator<double>;
+template class Evaluator<float>;
+
+}  // namespace pgpu

@@ -1,0 +1,767 @@
+// Device part of the RAS preconditioner: batched assembly of Q^T A Q, batched blocked
+// Cholesky (right-looking, 32x32 blocks, one launch per step for all domains of a level),
+// batched fine/coarse solves with the inner-point scatter, and the multilevel sweep.
+//
+// Q^T A Q entries are formed without materialising A: with L_i the Lagrange-basis row of
+// point i, u_i[k] = A(p_k, x_i) and v_i = A11 L_i (p_k the polynomial points),
+//   (Q^T A Q)_ij = A(x_i, x_j) - u_i.L_j - L_i.u_j + L_i.v_j,
+// which equals the four-block product of fine_grid.hpp:80-84 with q_top = -L^T.
+#include <algorithm>
+#include <cmath>
+
+#include "kernels.cuh"
+#include "linalg.hpp"
+#include "ras.hpp"
+
+namespace pgpu {
+
+namespace {
+
+constexpr int NB = 32;
+
+template <class T>
+__device__ __forceinline__ T rbf_value_rt(int kind, T r2, const KParams<T>& kp) {
+  return dispatch_kind(kind, [&]<int K>() { return rbf_value<K>(r2, kp); });
+}
+
+struct RbfSet {
+  int n;
+  int kind[PGPU_MAX_RBFS];
+  double p0[PGPU_MAX_RBFS], p1[PGPU_MAX_RBFS];
+  double a[PGPU_MAX_RBFS][9];
+};
+
+__device__ __forceinline__ double kernel_sum(const RbfSet& rs, const double* x, const double* y) {
+  double s = 0;
+  for (int r = 0; r < rs.n; ++r) {
+    double d0 = x[0] - y[0], d1 = x[1] - y[1], d2 = x[2] - y[2];
+    const double* a = rs.a[r];
+    double t0 = a[0] * d0 + a[1] * d1 + a[2] * d2;
+    double t1 = a[3] * d0 + a[4] * d1 + a[5] * d2;
+    double t2 = a[6] * d0 + a[7] * d1 + a[8] * d2;
+    KParams<double> kp{rs.p0[r], rs.p1[r]};
+    s += rbf_value_rt<double>(rs.kind[r], t0 * t0 + t1 * t1 + t2 * t2, kp);
+  }
+  return s;
+}
+
+// u_i[k] = sum_r K_r(p_k - x_i), v_i = A11 L_i, per global point i.
+__global__ void uv_kernel(RbfSet rs, const double* __restrict__ pts, Index mu,
+                          const double* __restrict__ poly_pts, int l,
+                          const double* __restrict__ a11, const double* __restrict__ lag,
+                          double* __restrict__ u, double* __restrict__ v) {
+  Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= mu) return;
+  const double* x = pts + 3 * i;
+  for (int k = 0; k < l; ++k) u[i * l + k] = kernel_sum(rs, poly_pts + 3 * k, x);
+  for (int k = 0; k < l; ++k) {
+    double s = 0;
+    for (int kk = 0; kk < l; ++kk) s += a11[k * l + kk] * lag[i * l + kk];
+    v[i * l + k] = s;
+  }
+}
+
+// Lagrange rows: lag_i = monomials(x_i) * coeffs.
+__global__ void lagrange_kernel(int degree, int l, const double* __restrict__ pts, Index mu,
+                                const double* __restrict__ coeffs, double* __restrict__ lag) {
+  Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= mu) return;
+  const double x = pts[3 * i], y = pts[3 * i + 1], z = pts[3 * i + 2];
+  double m[10] = {1, x, y, z, x * x, x * y, x * z, y * y, y * z, z * z};
+  (void)degree;
+  for (int c = 0; c < l; ++c) {
+    double s = 0;
+    for (int r = 0; r < l; ++r) s += m[r] * coeffs[r * l + c];
+    lag[i * l + c] = s;
+  }
+}
+
+template <class T>
+__global__ void frame_kernel(const double* __restrict__ pts, Index n, Mat3 a, double ox, double oy,
+                             double oz, P4<T>* __restrict__ out) {
+  Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double tx, ty, tz;
+  mat3_vec(a.a, pts[3 * i], pts[3 * i + 1], pts[3 * i + 2], tx, ty, tz);
+  out[i] = P4<T>{static_cast<T>(tx - ox), static_cast<T>(ty - oy), static_cast<T>(tz - oz), T(0)};
+}
+
+__device__ __forceinline__ void tile_of(Index t, int& bi, int& bj) {
+  // Lower-triangular tile enumeration: t = bi (bi + 1) / 2 + bj, bj <= bi.
+  int b = static_cast<int>((sqrt(8.0 * static_cast<double>(t) + 1.0) - 1.0) * 0.5);
+  while (static_cast<Index>(b + 1) * (b + 2) / 2 <= t) ++b;
+  while (static_cast<Index>(b) * (b + 1) / 2 > t) --b;
+  bi = b;
+  bj = static_cast<int>(t - static_cast<Index>(b) * (b + 1) / 2);
+}
+
+// Assembles Q^T A Q (lower tiles) for all domains; padding rows/columns become identity.
+template <class T, int KIND>
+__global__ void assemble_kernel(KParams<T> kp, const P4<T>* __restrict__ frame,
+                                const int* __restrict__ nsz, const int* __restrict__ lds,
+                                const Index* __restrict__ mat_off, T* __restrict__ mats,
+                                const Index* __restrict__ pt_off, const Index* __restrict__ pts,
+                                int l, int first, int last, double nugget,
+                                const double* __restrict__ lag, const double* __restrict__ u,
+                                const double* __restrict__ v) {
+  const Index d = blockIdx.x;
+  const int n = nsz[d], ld = lds[d];
+  int bi, bj;
+  tile_of(blockIdx.y, bi, bj);
+  if (bi * NB >= ld) return;
+  T* m = mats + mat_off[d];
+  const Index* dp = pts + pt_off[d] + l;  // non-polynomial points
+  const int r = bi * NB + (threadIdx.x & 31);  // lanes walk down a column (coalesced)
+  for (int cc = threadIdx.x >> 5; cc < NB; cc += blockDim.x >> 5) {
+    const int c = bj * NB + cc;
+    T* dst = m + r + static_cast<Index>(c) * ld;
+    if (r >= n || c >= n) {
+      *dst = (r == c) ? T(1) : T(0);
+      continue;
+    }
+    const Index gr = dp[r], gc = dp[c];
+    P4<T> xr = frame[gr], xc = frame[gc];
+    T dx = xr.x - xc.x, dy = xr.y - xc.y, dz = xr.z - xc.z;
+    T val = rbf_value<KIND>(dx * dx + dy * dy + dz * dz, kp);
+    double acc = first ? 0.0 : static_cast<double>(*dst);
+    acc += static_cast<double>(val);
+    if (last) {
+      if (r == c) acc += nugget;
+      const double* lr = lag + gr * l;
+      const double* lc = lag + gc * l;
+      const double* ur = u + gr * l;
+      const double* uc = u + gc * l;
+      const double* vc = v + gc * l;
+      double corr = 0;
+      for (int k = 0; k < l; ++k) corr += -ur[k] * lc[k] - lr[k] * uc[k] + lr[k] * vc[k];
+      acc += corr;
+    }
+    *dst = static_cast<T>(acc);
+  }
+}
+
+template <class T>
+__global__ void potrf_diag_kernel(int kb, const int* __restrict__ lds,
+                                  const Index* __restrict__ mat_off, T* __restrict__ mats,
+                                  int* __restrict__ info) {
+  const Index d = blockIdx.x;
+  const int ld = lds[d];
+  if (kb * NB >= ld) return;
+  __shared__ T a[NB][NB + 1];
+  T* m = mats + mat_off[d] + static_cast<Index>(kb * NB) * ld + kb * NB;
+  const int lane = threadIdx.x;
+  for (int c = 0; c < NB; ++c) a[lane][c] = m[lane + static_cast<Index>(c) * ld];
+  __syncwarp();
+  int modified = 0;
+  for (int j = 0; j < NB; ++j) {
+    if (lane == 0) {
+      T dj = a[j][j];
+      if (!(dj > T(0))) {
+        // Modified pivot (the matrix lost definiteness to rounding): the preconditioner only
+        // needs an approximate factor, so continue with |d| (or 1 when d vanished).
+        dj = fabs(dj) > T(0) ? T(fabs(dj)) : T(1);
+        ++modified;
+      }
+      a[j][j] = sqrt(dj);
+    }
+    __syncwarp();
+    if (lane > j) a[lane][j] /= a[j][j];
+    __syncwarp();
+    if (lane > j) {
+      const T lj = a[lane][j];
+      for (int c = j + 1; c <= lane; ++c) a[lane][c] -= lj * a[c][j];
+    }
+    __syncwarp();
+  }
+  for (int c = 0; c < NB; ++c) {
+    m[lane + static_cast<Index>(c) * ld] = (lane >= c) ? a[lane][c] : T(0);
+  }
+  if (lane == 0 && modified) atomicAdd(info + d, modified);
+}
+
+template <class T>
+__global__ void trsm_panel_kernel(int kb, const int* __restrict__ lds,
+                                  const Index* __restrict__ mat_off, T* __restrict__ mats) {
+  const Index d = blockIdx.x;
+  const int ld = lds[d];
+  const int r = (kb + 1) * NB + blockIdx.y * blockDim.x + threadIdx.x;
+  __shared__ T lkk[NB][NB + 1];
+  if ((kb + 1) * NB + static_cast<int>(blockIdx.y * blockDim.x) >= ld) return;
+  T* m = mats + mat_off[d];
+  for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
+    int rr = e % NB, cc = e / NB;
+    lkk[rr][cc] = m[(kb * NB + rr) + static_cast<Index>(kb * NB + cc) * ld];
+  }
+  __syncthreads();
+  if (r >= ld) return;
+  T x[NB];
+#pragma unroll
+  for (int c = 0; c < NB; ++c) x[c] = m[r + static_cast<Index>(kb * NB + c) * ld];
+#pragma unroll
+  for (int c = 0; c < NB; ++c) {
+    T s = x[c];
+#pragma unroll
+    for (int k = 0; k < c; ++k) s -= x[k] * lkk[c][k];
+    x[c] = s / lkk[c][c];
+  }
+#pragma unroll
+  for (int c = 0; c < NB; ++c) m[r + static_cast<Index>(kb * NB + c) * ld] = x[c];
+}
+
+template <class T>
+__global__ void syrk_update_kernel(int kb, const int* __restrict__ lds,
+                                   const Index* __restrict__ mat_off, T* __restrict__ mats) {
+  const Index d = blockIdx.x;
+  const int ld = lds[d];
+  const int nbd = ld / NB;
+  const int rem = nbd - kb - 1;
+  if (rem <= 0) return;
+  const Index ntiles = static_cast<Index>(rem) * (rem + 1) / 2;
+  if (static_cast<Index>(blockIdx.y) >= ntiles) return;
+  int ti, tj;
+  tile_of(blockIdx.y, ti, tj);
+  const int bi = kb + 1 + ti, bj = kb + 1 + tj;
+  T* m = mats + mat_off[d];
+  __shared__ T pi[NB][NB + 1];  // pi[k][i] = L(bi*NB + i, kb*NB + k)
+  __shared__ T pj[NB][NB + 1];
+  for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
+    int rr = e % NB, kk = e / NB;
+    pi[kk][rr] = m[(bi * NB + rr) + static_cast<Index>(kb * NB + kk) * ld];
+    pj[kk][rr] = m[(bj * NB + rr) + static_cast<Index>(kb * NB + kk) * ld];
+  }
+  __syncthreads();
+  const int i = threadIdx.x & 31;
+  const int jy = threadIdx.x >> 5;  // 0..7
+  T acc[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll 8
+  for (int k = 0; k < NB; ++k) {
+    const T a = pi[k][i];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[q] += a * pj[k][jy + 8 * q];
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int j = jy + 8 * q;
+    m[(bi * NB + i) + static_cast<Index>(bj * NB + j) * ld] -= acc[q];
+  }
+}
+
+// Fine (or coarse) solve of every domain: gather the residuals, form Q^T d, solve with the
+// Cholesky factor, expand lambda = Q gamma and scatter the owned entries
+// (fine_grid.hpp:97-156, coarse_grid.hpp:91-131).
+template <class T>
+__global__ void ras_solve_kernel(const int* __restrict__ nsz, const int* __restrict__ lds,
+                                 const Index* __restrict__ mat_off, const T* __restrict__ mats,
+                                 const Index* __restrict__ pt_off, const Index* __restrict__ pts,
+                                 const char* __restrict__ inner, int l,
+                                 const double* __restrict__ lag, const double* __restrict__ u,
+                                 const double* __restrict__ resid, double* __restrict__ weights,
+                                 int coarse, double* __restrict__ coarse_out) {
+  extern __shared__ double sh[];
+  const Index d = blockIdx.x;
+  const int n = nsz[d], ld = lds[d];
+  const Index* dp = pts + pt_off[d];
+  const char* din = inner + pt_off[d];
+  const T* m = mats + mat_off[d];
+  double* x = sh;            // ld
+  double* dh = sh + ld;      // l (polynomial-point residuals)
+  double* red = dh + 16;     // 32 * 16 reduction scratch
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+
+  for (int k = tid; k < l; k += blockDim.x) dh[k] = resid[dp[k]];
+  __syncthreads();
+  for (int i = tid; i < ld; i += blockDim.x) {
+    double s = 0;
+    if (i < n) {
+      const Index g = dp[l + i];
+      s = resid[g];
+      for (int k = 0; k < l; ++k) s -= lag[g * l + k] * dh[k];
+    }
+    x[i] = s;
+  }
+  __syncthreads();
+  const int nb = ld / NB;
+  // Forward: L y = b.
+  for (int kb = 0; kb < nb; ++kb) {
+    if (warp == 0) {
+      const int base = kb * NB;
+      double xi = x[base + lane];
+      for (int jj = 0; jj < NB; ++jj) {
+        double yj = __shfl_sync(0xffffffffu, xi, jj) /
+                    static_cast<double>(m[(base + jj) + static_cast<Index>(base + jj) * ld]);
+        if (lane == jj) xi = yj;
+        if (lane > jj) xi -= static_cast<double>(m[(base + lane) + static_cast<Index>(base + jj) * ld]) * yj;
+      }
+      x[base + lane] = xi;
+    }
+    __syncthreads();
+    for (int r = (kb + 1) * NB + tid; r < ld; r += blockDim.x) {
+      double s = 0;
+#pragma unroll 8
+      for (int c = 0; c < NB; ++c) s += static_cast<double>(m[r + static_cast<Index>(kb * NB + c) * ld]) * x[kb * NB + c];
+      x[r] -= s;
+    }
+    __syncthreads();
+  }
+  // Backward: L^T x = y.
+  for (int kb = nb - 1; kb >= 0; --kb) {
+    const int base = kb * NB;
+    for (int c = warp; c < NB; c += nw) {
+      const int col = base + c;
+      double s = 0;
+      for (int r = (kb + 1) * NB + lane; r < ld; r += 32)
+        s += static_cast<double>(m[r + static_cast<Index>(col) * ld]) * x[r];
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) x[col] -= s;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      double xi = x[base + lane];
+      for (int jj = NB - 1; jj >= 0; --jj) {
+        double zj = __shfl_sync(0xffffffffu, xi, jj) /
+                    static_cast<double>(m[(base + jj) + static_cast<Index>(base + jj) * ld]);
+        if (lane == jj) xi = zj;
+        if (lane < jj) xi -= static_cast<double>(m[(base + jj) + static_cast<Index>(base + lane) * ld]) * zj;
+      }
+      x[base + lane] = xi;
+    }
+    __syncthreads();
+  }
+  // lambda_head_k = -sum_i L_ik gamma_i ; for the coarse grid also s_k = sum_i u_ik gamma_i.
+  for (int k = 0; k < l; ++k) {
+    double s1 = 0, s2 = 0;
+    for (int i = tid; i < n; i += blockDim.x) {
+      const Index g = dp[l + i];
+      s1 += lag[g * l + k] * x[i];
+      if (coarse) s2 += u[g * l + k] * x[i];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if (lane == 0) {
+      red[warp] = s1;
+      red[32 + warp] = s2;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double a = 0, b = 0;
+      for (int w = 0; w < nw; ++w) {
+        a += red[w];
+        b += red[32 + w];
+      }
+      dh[k] = -a;  // lambda_head
+      if (coarse) {
+        coarse_out[k] = -a;
+        coarse_out[16 + k] = b;
+      }
+    }
+    __syncthreads();
+  }
+  if (n == 0) {
+    for (int k = tid; k < l; k += blockDim.x) dh[k] = 0.0;
+    if (coarse && tid < l) {
+      coarse_out[tid] = 0.0;
+      coarse_out[16 + tid] = 0.0;
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < n; i += blockDim.x)
+    if (coarse || din[l + i]) weights[dp[l + i]] = x[i];
+  for (int k = tid; k < l; k += blockDim.x)
+    if (coarse || din[k]) weights[dp[k]] = dh[k];
+}
+
+RbfSet rbf_set(const ModelDesc& m) {
+  RbfSet rs{};
+  rs.n = static_cast<int>(m.rbfs.size());
+  for (int r = 0; r < rs.n; ++r) {
+    rs.kind[r] = m.rbfs[r].kind;
+    rs.p0[r] = m.rbfs[r].p[0];
+    rs.p1[r] = m.rbfs[r].p[1];
+    for (int k = 0; k < 9; ++k) rs.a[r][k] = m.rbfs[r].a[k];
+  }
+  return rs;
+}
+
+}  // namespace
+
+template <class T>
+RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* points_host,
+                                        const double* points_dev, Index mu, const Bbox3& bbox)
+    : model_(model), l_(model.l()), mu_(mu), bbox_(bbox), points_dev_(points_dev) {
+  constexpr double kFineToCoarseRatio = 10.0;
+  constexpr Index kNCoarsestPoints = 2048;
+  n_levels_ = std::max(static_cast<int>(std::ceil(std::log(static_cast<double>(mu_) / kNCoarsestPoints) /
+                                                  std::log(kFineToCoarseRatio))),
+                       0) +
+              1;
+  point_idcs_.resize(n_levels_);
+  fine_.resize(n_levels_);
+
+  // Polynomial points and the Lagrange basis (ras_preconditioner.hpp:76-106).
+  if (l_ > 0) {
+    poly_idcs_ = unisolvent_point_set(points_host, mu_, model_.poly_degree);
+    std::vector<double> pp;
+    for (auto i : poly_idcs_)
+      for (int k = 0; k < 3; ++k) pp.push_back(points_host[3 * i + k]);
+    lagrange_coeffs_ = lagrange_coeffs(model_.poly_degree, pp.data(), l_);
+    auto& top = point_idcs_[n_levels_ - 1];
+    top = poly_idcs_;
+    top.reserve(mu_);
+    std::vector<char> is_poly(mu_, 0);
+    for (auto i : poly_idcs_) is_poly[i] = 1;
+    for (Index i = 0; i < mu_; ++i)
+      if (!is_poly[i]) top.push_back(i);
+  } else {
+    auto& top = point_idcs_[n_levels_ - 1];
+    top.resize(mu_);
+    for (Index i = 0; i < mu_; ++i) top[i] = i;
+  }
+
+  // Points used for the geometric division: A-transformed when the model has one
+  // anisotropic RBF (ras_preconditioner.hpp:108-119).
+  std::vector<double> a_points;
+  const double* div_points = points_host;
+  if (model_.rbfs.size() == 1 && !model_.rbfs[0].aniso_is_identity()) {
+    const double* a = model_.rbfs[0].a;
+    a_points.resize(3 * mu_);
+    for (Index i = 0; i < mu_; ++i) {
+      const double* p = points_host + 3 * i;
+      for (int r = 0; r < 3; ++r) a_points[3 * i + r] = a[3 * r] * p[0] + a[3 * r + 1] * p[1] + a[3 * r + 2] * p[2];
+    }
+    div_points = a_points.data();
+  }
+
+  std::vector<std::vector<Domain>> level_domains(n_levels_);
+  for (int level = n_levels_ - 1; level >= 1; --level) {
+    std::vector<Index> no_grad;
+    DomainDivider divider(div_points, nullptr, point_idcs_[level], no_grad, poly_idcs_);
+    double finest = std::log(static_cast<double>(mu_)) / std::log(kFineToCoarseRatio);
+    double coarsest = std::log(static_cast<double>(kNCoarsestPoints)) / std::log(kFineToCoarseRatio);
+    Index n_coarse = static_cast<Index>(std::pow(
+        kFineToCoarseRatio, coarsest + (level - 1) * (finest - coarsest) / (n_levels_ - 1)));
+    point_idcs_[level - 1] = divider.choose_coarse_points(n_coarse).first;
+    level_domains[level] = std::move(divider.domains());
+  }
+
+  // Device-side per-point data.
+  const int l = l_;
+  if (l > 0) {
+    DevBuf<double> coeffs;
+    coeffs.upload(lagrange_coeffs_);
+    lagrange_.resize(mu_ * l);
+    lagrange_kernel<<<blocks_for(mu_, 256), 256, 0, stream()>>>(model_.poly_degree, l, points_dev,
+                                                                mu_, coeffs.data(), lagrange_.data());
+    PGPU_LAUNCH_CHECK();
+    // A11 on the host (l x l, nugget on the diagonal).
+    a11_.assign(l * l, 0.0);
+    for (int i = 0; i < l; ++i)
+      for (int j = 0; j < l; ++j) {
+        const double* x = points_host + 3 * poly_idcs_[i];
+        const double* y = points_host + 3 * poly_idcs_[j];
+        double s = (i == j) ? model_.nugget : 0.0;
+        for (const auto& rb : model_.rbfs) {
+          double dd[3] = {x[0] - y[0], x[1] - y[1], x[2] - y[2]};
+          double t[3];
+          for (int r = 0; r < 3; ++r) t[r] = rb.a[3 * r] * dd[0] + rb.a[3 * r + 1] * dd[1] + rb.a[3 * r + 2] * dd[2];
+          KParams<double> kp{rb.p[0], rb.p[1]};
+          s += dispatch_kind(rb.kind, [&]<int K>() { return rbf_value<K>(t[0] * t[0] + t[1] * t[1] + t[2] * t[2], kp); });
+        }
+        a11_[i * l + j] = s;
+      }
+    std::vector<double> pp;
+    for (auto i : poly_idcs_)
+      for (int k = 0; k < 3; ++k) pp.push_back(points_host[3 * i + k]);
+    DevBuf<double> dpp, da11;
+    dpp.upload(pp);
+    da11.upload(a11_);
+    u_.resize(mu_ * l);
+    v_.resize(mu_ * l);
+    uv_kernel<<<blocks_for(mu_, 128), 128, 0, stream()>>>(rbf_set(model_), points_dev, mu_, dpp.data(),
+                                                          l, da11.data(), lagrange_.data(), u_.data(),
+                                                          v_.data());
+    PGPU_LAUNCH_CHECK();
+    sync();
+  }
+
+  for (int level = n_levels_ - 1; level >= 1; --level) {
+    fine_[level] = std::make_unique<DomainBatch<T>>();
+    build_batch(*fine_[level], level_domains[level]);
+  }
+  {
+    Domain cd;
+    cd.point_indices = point_idcs_[0];
+    cd.inner_point.assign(cd.point_indices.size(), 1);
+    std::vector<Domain> v{cd};
+    build_batch(coarse_, v);
+  }
+
+  // Level point sets on the device (for the residual-update evaluators).
+  level_idx_dev_.resize(n_levels_);
+  level_pts_dev_.resize(n_levels_);
+  for (int level = 0; level < n_levels_; ++level) {
+    const auto& idx = point_idcs_[level];
+    level_idx_dev_[level].upload(idx);
+    std::vector<double> lp(3 * idx.size());
+    for (size_t i = 0; i < idx.size(); ++i)
+      for (int k = 0; k < 3; ++k) lp[3 * i + k] = points_host[3 * idx[i] + k];
+    level_pts_dev_[level].upload(lp);
+  }
+
+  if (n_levels_ > 1 && l > 0) {
+    // Orthonormalised monomials and their images (ras_preconditioner.hpp:168-188).
+    p_.resize(mu_ * l);
+    monomial_basis(model_.poly_degree, points_dev, mu_, nullptr, 0, p_.data());
+    for (int i = 0; i < l; ++i) {
+      double* ci = p_.data() + static_cast<Index>(i) * mu_;
+      double nrm = norm2(ci, mu_);
+      scal(mu_, 1.0 / nrm, ci);
+      for (int j = i + 1; j < l; ++j) {
+        double* cj = p_.data() + static_cast<Index>(j) * mu_;
+        axpy(mu_, -dot(ci, cj, mu_), ci, cj);
+      }
+    }
+    ap_.resize(mu_ * l);
+    Evaluator<T> ev(model_, bbox_, INFINITY, INFINITY);
+    ev.set_points(points_dev, mu_, nullptr, 0);
+    DevBuf<double> w(mu_ + l);
+    for (int i = 0; i < l; ++i) {
+      w.zero();
+      copy(w.data(), p_.data() + static_cast<Index>(i) * mu_, mu_);
+      ev.set_weights(w.data());
+      ev.evaluate(ap_.data() + static_cast<Index>(i) * mu_, false);
+    }
+  }
+  work_res_.resize(mu_);
+  work_w_.resize(mu_ + l);
+  work_tot_.resize(mu_ + l);
+  work_fit_.resize(mu_);
+  work_src_w_.resize(mu_ + l);
+  sync();
+}
+
+template <class T>
+RasPreconditioner<T>::~RasPreconditioner() = default;
+
+template <class T>
+Index RasPreconditioner<T>::n_domains() const {
+  Index s = 0;
+  for (const auto& f : fine_)
+    if (f) s += f->n_dom;
+  return s;
+}
+
+template <class T>
+void RasPreconditioner<T>::build_batch(DomainBatch<T>& b, const std::vector<Domain>& domains) {
+  const int l = l_;
+  b.n_dom = static_cast<Index>(domains.size());
+  std::vector<int> n(b.n_dom), ld(b.n_dom);
+  std::vector<Index> mat_off(b.n_dom + 1), pt_off(b.n_dom + 1);
+  std::vector<Index> pts;
+  std::vector<char> inner;
+  Index moff = 0, poff = 0;
+  b.max_n = 0;
+  for (Index d = 0; d < b.n_dom; ++d) {
+    const auto& dom = domains[d];
+    const int m = static_cast<int>(dom.point_indices.size());
+    n[d] = std::max(m - l, 0);
+    ld[d] = std::max(NB, ((n[d] + NB - 1) / NB) * NB);
+    b.max_n = std::max(b.max_n, ld[d]);
+    mat_off[d] = moff;
+    moff += static_cast<Index>(ld[d]) * ld[d];
+    pt_off[d] = poff;
+    poff += m;
+    pts.insert(pts.end(), dom.point_indices.begin(), dom.point_indices.end());
+    inner.insert(inner.end(), dom.inner_point.begin(), dom.inner_point.end());
+  }
+  mat_off[b.n_dom] = moff;
+  pt_off[b.n_dom] = poff;
+  b.total_points = poff;
+  b.n.upload(n);
+  b.ld.upload(ld);
+  b.mat_off.upload(mat_off);
+  b.pt_off.upload(pt_off);
+  b.pts.upload(pts);
+  b.inner.resize(inner.size());
+  if (!inner.empty())
+    PGPU_CUDA(cudaMemcpyAsync(b.inner.data(), inner.data(), inner.size(), cudaMemcpyHostToDevice,
+                              stream()));
+  b.mats.resize(moff);
+  b.info.resize(b.n_dom);
+  b.info.zero();
+  if (b.n_dom == 0) return;
+
+  // Assembly, one pass per RBF in its own frame.
+  const int nbmax = b.max_n / NB;
+  const Index ntiles = static_cast<Index>(nbmax) * (nbmax + 1) / 2;
+  for (size_t r = 0; r < model_.rbfs.size(); ++r) {
+    const auto& rb = model_.rbfs[r];
+    Mat3 a;
+    for (int k = 0; k < 9; ++k) a.a[k] = rb.a[k];
+    double tmin[3] = {INFINITY, INFINITY, INFINITY}, tmax[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int c = 0; c < 8; ++c) {
+      double p[3] = {(c & 1) ? bbox_.max[0] : bbox_.min[0], (c & 2) ? bbox_.max[1] : bbox_.min[1],
+                     (c & 4) ? bbox_.max[2] : bbox_.min[2]};
+      for (int q = 0; q < 3; ++q) {
+        double v = a.a[3 * q] * p[0] + a.a[3 * q + 1] * p[1] + a.a[3 * q + 2] * p[2];
+        tmin[q] = std::min(tmin[q], v);
+        tmax[q] = std::max(tmax[q], v);
+      }
+    }
+    double o[3];
+    for (int q = 0; q < 3; ++q) o[q] = bbox_.empty() ? 0.0 : 0.5 * (tmin[q] + tmax[q]);
+    DevBuf<P4<T>> frame(mu_);
+    frame_kernel<T><<<blocks_for(mu_, 256), 256, 0, stream()>>>(points_dev_, mu_, a, o[0], o[1], o[2],
+                                                                frame.data());
+    PGPU_LAUNCH_CHECK();
+    KParams<T> kp{static_cast<T>(rb.p[0]), static_cast<T>(rb.p[1])};
+    const int first = r == 0, last = r + 1 == model_.rbfs.size();
+    if (ntiles > 65535) throw_runtime("domain too large for the batched assembly");
+    dim3 grid(static_cast<unsigned>(b.n_dom), static_cast<unsigned>(ntiles));
+    dispatch_kind(rb.kind, [&]<int K>() {
+      assemble_kernel<T, K><<<grid, 256, 0, stream()>>>(
+          kp, frame.data(), b.n.data(), b.ld.data(), b.mat_off.data(), b.mats.data(),
+          b.pt_off.data(), b.pts.data(), l, first, last, model_.nugget, lagrange_.data(),
+          u_.data(), v_.data());
+      return 0;
+    });
+    PGPU_LAUNCH_CHECK();
+  }
+
+  // Blocked Cholesky over all domains.
+  for (int kb = 0; kb < nbmax; ++kb) {
+    potrf_diag_kernel<T><<<static_cast<unsigned>(b.n_dom), 32, 0, stream()>>>(
+        kb, b.ld.data(), b.mat_off.data(), b.mats.data(), b.info.data());
+    PGPU_LAUNCH_CHECK();
+    const int rows_below = b.max_n - (kb + 1) * NB;
+    if (rows_below <= 0) continue;
+    dim3 gp(static_cast<unsigned>(b.n_dom), static_cast<unsigned>((rows_below + 127) / 128));
+    trsm_panel_kernel<T><<<gp, 128, 0, stream()>>>(kb, b.ld.data(), b.mat_off.data(), b.mats.data());
+    PGPU_LAUNCH_CHECK();
+    const int rem = nbmax - kb - 1;
+    dim3 gs(static_cast<unsigned>(b.n_dom), static_cast<unsigned>(static_cast<Index>(rem) * (rem + 1) / 2));
+    syrk_update_kernel<T><<<gs, 256, 0, stream()>>>(kb, b.ld.data(), b.mat_off.data(), b.mats.data());
+    PGPU_LAUNCH_CHECK();
+  }
+}
+
+template <class T>
+void RasPreconditioner<T>::solve_level(int level, const double* residuals, double* weights) {
+  fill(weights, mu_ + l_, 0.0);
+  DomainBatch<T>& b = level == 0 ? coarse_ : *fine_[level];
+  if (b.n_dom == 0) return;
+  const size_t smem = (static_cast<size_t>(b.max_n) + 16 + 64) * sizeof(double);
+  DevBuf<double> cout(32);
+  ras_solve_kernel<T><<<static_cast<unsigned>(b.n_dom), 256, smem, stream()>>>(
+      b.n.data(), b.ld.data(), b.mat_off.data(), b.mats.data(), b.pt_off.data(), b.pts.data(),
+      b.inner.data(), l_, lagrange_.data(), u_.data(), residuals, weights, level == 0 ? 1 : 0,
+      cout.data());
+  PGPU_LAUNCH_CHECK();
+  if (level == 0 && l_ > 0) {
+    // Polynomial part: solve P_top c = d_head - A_top lambda (coarse_grid.hpp:124-127).
+    auto h = cout.to_host();
+    const int l = l_;
+    std::vector<double> dh(l);
+    std::vector<Index> pidx(point_idcs_[0].begin(), point_idcs_[0].begin() + l);
+    DevBuf<Index> dpi;
+    dpi.upload(pidx);
+    DevBuf<double> dd(l);
+    gather(residuals, dpi.data(), l, dd.data());
+    dd.download(dh.data(), l);
+    sync();
+    std::vector<double> rhs(l);
+    for (int k = 0; k < l; ++k) {
+      double a_lambda = h[16 + k];
+      for (int j = 0; j < l; ++j) a_lambda += a11_[k * l + j] * h[j];
+      rhs[k] = dh[k] - a_lambda;
+    }
+    // c = P_top^{-1} rhs; lagrange_coeffs_ holds P_top^{-1} (row-major).
+    std::vector<double> c(l, 0.0);
+    for (int i = 0; i < l; ++i)
+      for (int k = 0; k < l; ++k) c[i] += lagrange_coeffs_[i * l + k] * rhs[k];
+    PGPU_CUDA(cudaMemcpyAsync(weights + mu_, c.data(), l * sizeof(double), cudaMemcpyHostToDevice,
+                              stream()));
+    sync();
+  }
+}
+
+template <class T>
+Evaluator<T>& RasPreconditioner<T>::evaluator(int src_level, int trg_level) {
+  auto key = std::make_pair(src_level, trg_level);
+  auto it = evaluators_.find(key);
+  if (it == evaluators_.end()) {
+    auto ev = std::make_unique<Evaluator<T>>(model_, bbox_, INFINITY, INFINITY);
+    ev->set_sources(level_pts_dev_[src_level].data(),
+                    static_cast<Index>(point_idcs_[src_level].size()), nullptr, 0);
+    ev->set_targets(level_pts_dev_[trg_level].data(),
+                    static_cast<Index>(point_idcs_[trg_level].size()), nullptr, 0);
+    it = evaluators_.emplace(key, std::move(ev)).first;
+  }
+  return *it->second;
+}
+
+template <class T>
+void RasPreconditioner<T>::update_residuals(int src_level, int trg_level, const double* weights,
+                                            double* residuals) {
+  const Index ns = static_cast<Index>(point_idcs_[src_level].size());
+  const Index nt = static_cast<Index>(point_idcs_[trg_level].size());
+  gather(weights, level_idx_dev_[src_level].data(), ns, work_src_w_.data());
+  if (l_ > 0) copy(work_src_w_.data() + ns, weights + mu_, l_);
+  auto& ev = evaluator(src_level, trg_level);
+  ev.set_weights(work_src_w_.data());
+  ev.evaluate(work_fit_.data());
+  scal(nt, -1.0, work_fit_.data());
+  scatter_add(work_fit_.data(), level_idx_dev_[trg_level].data(), nt, residuals);
+}
+
+template <class T>
+void RasPreconditioner<T>::orthogonalize(double* weights, double* residuals) {
+  if (l_ == 0) return;
+  std::vector<double> dotv(l_);
+  tall_gemv_t(p_.data(), mu_, l_, weights, dotv.data());
+  std::vector<double> neg(l_);
+  for (int k = 0; k < l_; ++k) neg[k] = -dotv[k];
+  tall_gemv_add(p_.data(), mu_, l_, neg.data(), weights);
+  tall_gemv_add(ap_.data(), mu_, l_, dotv.data(), residuals);
+}
+
+template <class T>
+void RasPreconditioner<T>::apply(const double* v, double* out) {
+  double* r = work_res_.data();
+  copy(r, v, mu_);
+  if (n_levels_ == 1) {
+    solve_level(0, r, out);
+    return;
+  }
+  double* w = work_w_.data();
+  double* tot = out;
+  fill(tot, mu_ + l_, 0.0);
+  const int L = n_levels_;
+  solve_level(0, r, w);
+  update_residuals(0, L - 1, w, r);
+  axpy(mu_ + l_, 1.0, w, tot);
+  for (int level = 1; level < L - 1; ++level) {
+    solve_level(level, r, w);
+    update_residuals(level, L - 1, w, r);
+    axpy(mu_ + l_, 1.0, w, tot);
+    orthogonalize(tot, r);
+    solve_level(0, r, w);
+    update_residuals(0, L - 1, w, r);
+    axpy(mu_ + l_, 1.0, w, tot);
+  }
+  for (int level = L - 1; level >= 1; --level) {
+    solve_level(level, r, w);
+    update_residuals(level, level - 1, w, r);
+    axpy(mu_ + l_, 1.0, w, tot);
+    orthogonalize(tot, r);
+    solve_level(0, r, w);
+    if (level > 1) update_residuals(0, level - 1, w, r);
+    axpy(mu_ + l_, 1.0, w, tot);
+  }
+}
+
+template class RasPreconditioner<double>;
+template class RasPreconditioner<float>;
+
+}  // namespace pgpu

@@ -1,0 +1,80 @@
+// Multilevel restricted additive Schwarz (RAS) preconditioner on the device: the GPU form of
+// preconditioner::RasPreconditioner (include/polatory/preconditioner/ras_preconditioner.hpp:
+// 35-364) with FineGrid (fine_grid.hpp:36-195) and CoarseGrid (coarse_grid.hpp:19-159). The
+// per-domain factors of Q^T A Q stay resident in HBM (the reference packs them into a temp
+// file); all domains of a level are assembled, factorised and solved by batched kernels.
+#pragma once
+
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "common.hpp"
+#include "evaluator.hpp"
+#include "model.hpp"
+#include "ras_host.hpp"
+
+namespace pgpu {
+
+// All domains of one level (or the single coarse domain) with their factors.
+template <class T>
+struct DomainBatch {
+  Index n_dom = 0;
+  int max_n = 0;                 // largest Q^T A Q size
+  DevBuf<int> n;                 // Q^T A Q size per domain (m - l)
+  DevBuf<int> ld;                // padded leading dimension (multiple of 32)
+  DevBuf<Index> mat_off;         // offset of each factor in mats
+  DevBuf<T> mats;                // column-major padded factors
+  DevBuf<Index> pt_off;          // CSR offsets into pts
+  DevBuf<Index> pts;             // global point indices, polynomial points first
+  DevBuf<char> inner;            // inner flag per entry of pts
+  DevBuf<int> info;              // per-domain count of modified pivots
+  Index total_points = 0;
+};
+
+template <class T>
+class RasPreconditioner {
+ public:
+  // points_host / points_dev: the mu data points (xyz rows). Value points only.
+  RasPreconditioner(const ModelDesc& model, const double* points_host, const double* points_dev,
+                    Index mu, const Bbox3& bbox);
+  ~RasPreconditioner();
+
+  // out (M) = RAS(v (M)), M = mu + l (ras_preconditioner.hpp:191-250).
+  void apply(const double* v, double* out);
+
+  int levels() const { return n_levels_; }
+  Index n_domains() const;
+  Index size() const { return mu_ + l_; }
+
+ private:
+  void solve_level(int level, const double* residuals, double* weights);
+  void update_residuals(int src_level, int trg_level, const double* weights, double* residuals);
+  void orthogonalize(double* weights, double* residuals);
+  void build_batch(DomainBatch<T>& b, const std::vector<Domain>& domains);
+  Evaluator<T>& evaluator(int src_level, int trg_level);
+
+  ModelDesc model_;
+  int l_;
+  Index mu_;
+  int n_levels_;
+  Bbox3 bbox_;
+  const double* points_dev_;
+  std::vector<Index> poly_idcs_;
+  std::vector<double> lagrange_coeffs_;  // l x l row-major inverse of the poly-point monomials
+  std::vector<double> a11_;              // A restricted to the polynomial points (l x l)
+  std::vector<std::vector<Index>> point_idcs_;
+  std::vector<DevBuf<Index>> level_idx_dev_;
+  std::vector<DevBuf<double>> level_pts_dev_;
+  DevBuf<double> lagrange_;  // mu x l row-major
+  DevBuf<double> u_;         // mu x l: sum_r K_r(p_k, x_i)
+  DevBuf<double> v_;         // mu x l: A11 L_i
+  std::vector<std::unique_ptr<DomainBatch<T>>> fine_;  // per level (index 0 unused)
+  DomainBatch<T> coarse_;
+  DevBuf<double> p_;   // mu x l orthonormalised monomials (column-major)
+  DevBuf<double> ap_;  // mu x l
+  std::map<std::pair<int, int>, std::unique_ptr<Evaluator<T>>> evaluators_;
+  DevBuf<double> work_res_, work_w_, work_tot_, work_src_w_, work_fit_;
+};
+
+}  // namespace pgpu

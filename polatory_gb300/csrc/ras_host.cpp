@@ -1,0 +1,492 @@
+// Host-side RAS set-up: domain decomposition, coarse-point selection, unisolvent points.
+// The splitting rules restate include/polatory/preconditioner/domain_divider.hpp:161-313; a
+// selection (nth_element) replaces the full sort wherever only the partition into
+// [0, k) / [k, n) of the sorted order matters, which yields the same point sets.
+#include "ras_host.hpp"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <numeric>
+#include <queue>
+#include <random>
+#include <set>
+
+namespace pgpu {
+
+namespace {
+
+struct MixedPoint {
+  Index index;
+  bool inner;
+  bool grad;
+  int mult() const { return grad ? 3 : 1; }
+};
+
+struct Geo {
+  const double* pts;
+  const double* gpts;
+  const double* at(const MixedPoint& p) const {
+    return p.grad ? gpts + 3 * p.index : pts + 3 * p.index;
+  }
+};
+
+// Axes ordered by decreasing width (domain_divider.hpp:192-196).
+std::array<int, 3> axes_by_width(const double* wmin, const double* wmax) {
+  double width[3] = {wmax[0] - wmin[0], wmax[1] - wmin[1], wmax[2] - wmin[2]};
+  std::array<int, 3> axes{0, 1, 2};
+  std::sort(axes.begin(), axes.end(), [&](int i, int j) { return width[i] > width[j]; });
+  return axes;
+}
+
+struct LexLess {
+  const Geo* g;
+  std::array<int, 3> axes;
+  bool operator()(const MixedPoint& a, const MixedPoint& b) const {
+    const double* p = g->at(a);
+    const double* q = g->at(b);
+    for (int ax : axes) {
+      if (p[ax] != q[ax]) return p[ax] < q[ax];
+    }
+    return false;
+  }
+};
+
+void bbox_of(const Geo& g, const std::vector<MixedPoint>& pts, double* mn, double* mx) {
+  for (int k = 0; k < 3; ++k) {
+    mn[k] = INFINITY;
+    mx[k] = -INFINITY;
+  }
+  for (const auto& p : pts) {
+    const double* c = g.at(p);
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = std::min(mn[k], c[k]);
+      mx[k] = std::max(mx[k], c[k]);
+    }
+  }
+}
+
+// std::ceil((d - 0.5) / 2.0) + std::floor((d + 0.5) / 2.0) (domain_divider.hpp:311-313).
+double round_half_to_even(double d) { return std::ceil((d - 0.5) / 2.0) + std::floor((d + 0.5) / 2.0); }
+
+// Index of the last prefix-sum entry <= v (upper_bound - 1).
+Index last_le(const std::vector<Index>& prefix, Index v) {
+  return static_cast<Index>(std::upper_bound(prefix.begin(), prefix.end(), v) - prefix.begin()) - 1;
+}
+
+// Splits one domain into two overlapping halves (domain_divider.hpp:161-269).
+void divide_domain(const Geo& g, const Domain& d, Domain& left, Domain& right) {
+  const Index mu = d.num_points(), sigma = d.num_grad_points();
+  std::vector<MixedPoint> mp;
+  mp.reserve(mu + sigma);
+  for (Index i = 0; i < mu; ++i) mp.push_back({d.point_indices[i], d.inner_point[i] != 0, false});
+  for (Index i = 0; i < sigma; ++i)
+    mp.push_back({d.grad_point_indices[i], d.inner_grad_point[i] != 0, true});
+
+  double mn[3], mx[3];
+  bbox_of(g, mp, mn, mx);
+  LexLess less{&g, axes_by_width(mn, mx)};
+
+  const Index n_points = mu + sigma;
+  const Index n_mult = mu + 3 * sigma;
+  const double q = DomainDivider::kOverlapQuota * 1024.0 / static_cast<double>(n_mult);
+  const Index n_sub = static_cast<Index>(round_half_to_even((1.0 + q) / 2.0 * static_cast<double>(n_mult)));
+  const Index left_mult = n_mult - n_sub;
+  const Index right_mult = n_sub;
+  const Index mid_mult =
+      static_cast<Index>(round_half_to_even(static_cast<double>(left_mult + right_mult) / 2.0));
+
+  Index left_part, right_part, mid;
+  if (sigma == 0) {
+    // Multiplicities are all one: the partition points are the multiplicity targets.
+    left_part = left_mult;
+    right_part = right_mult;
+    mid = mid_mult;
+    std::nth_element(mp.begin(), mp.begin() + mid, mp.end(), less);
+    if (left_part < mid) std::nth_element(mp.begin(), mp.begin() + left_part, mp.begin() + mid, less);
+    if (right_part > mid && right_part < n_points)
+      std::nth_element(mp.begin() + mid, mp.begin() + right_part, mp.end(), less);
+  } else {
+    std::sort(mp.begin(), mp.end(), less);
+    std::vector<Index> prefix{0};
+    prefix.reserve(n_points + 1);
+    for (const auto& p : mp) prefix.push_back(prefix.back() + p.mult());
+    left_part = last_le(prefix, left_mult);
+    right_part = last_le(prefix, right_mult);
+    mid = last_le(prefix, mid_mult);
+  }
+
+  for (Index i = 0; i < right_part; ++i) {
+    const auto& p = mp[i];
+    const char inner = (p.inner && i < mid) ? 1 : 0;
+    if (p.grad) {
+      left.grad_point_indices.push_back(p.index);
+      left.inner_grad_point.push_back(inner);
+    } else {
+      left.point_indices.push_back(p.index);
+      left.inner_point.push_back(inner);
+    }
+  }
+  for (Index i = left_part; i < n_points; ++i) {
+    const auto& p = mp[i];
+    const char inner = (p.inner && i >= mid) ? 1 : 0;
+    if (p.grad) {
+      right.grad_point_indices.push_back(p.index);
+      right.inner_grad_point.push_back(inner);
+    } else {
+      right.point_indices.push_back(p.index);
+      right.inner_point.push_back(inner);
+    }
+  }
+}
+
+// Domain::merge_poly_points (domain.hpp:27-49): sort by index, put the polynomial points
+// first (inner only where the domain already owned them).
+void merge_poly_points(Domain& d, const std::vector<Index>& poly) {
+  std::vector<std::pair<Index, char>> z(d.point_indices.size());
+  for (size_t i = 0; i < z.size(); ++i) z[i] = {d.point_indices[i], d.inner_point[i]};
+  std::sort(z.begin(), z.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+  const Index np = static_cast<Index>(poly.size());
+  std::vector<char> poly_inner(np, 0);
+  std::vector<char> erase(z.size(), 0);
+  for (Index i = 0; i < np; ++i) {
+    auto it = std::lower_bound(z.begin(), z.end(), poly[i],
+                               [](const auto& a, Index v) { return a.first < v; });
+    if (it == z.end() || it->first != poly[i]) continue;
+    poly_inner[i] = it->second;
+    erase[it - z.begin()] = 1;
+  }
+  d.point_indices.clear();
+  d.inner_point.clear();
+  for (Index i = 0; i < np; ++i) {
+    d.point_indices.push_back(poly[i]);
+    d.inner_point.push_back(poly_inner[i]);
+  }
+  for (size_t i = 0; i < z.size(); ++i) {
+    if (erase[i]) continue;
+    d.point_indices.push_back(z[i].first);
+    d.inner_point.push_back(z[i].second);
+  }
+}
+
+struct Cluster {
+  int level = 0;
+  double volume = 0;
+  std::vector<MixedPoint> points;
+  MixedPoint center{};
+  bool has_grad = false;
+};
+
+struct ClusterLess {
+  // priority_queue top = highest priority: lowest level, then largest bbox volume
+  // (domain_divider.hpp:151-158).
+  bool operator()(const Cluster* a, const Cluster* b) const {
+    if (a->level != b->level) return a->level > b->level;
+    return a->volume < b->volume;
+  }
+};
+
+// initialize_cluster (domain_divider.hpp:277-308): bbox, the point nearest to the bbox centre,
+// and (for clusters holding gradient points) the lexicographic sort used by the next split.
+void initialize_cluster(const Geo& g, Cluster& c) {
+  double mn[3], mx[3];
+  bbox_of(g, c.points, mn, mx);
+  c.volume = (mx[0] - mn[0]) * (mx[1] - mn[1]) * (mx[2] - mn[2]);
+  double ctr[3];
+  for (int k = 0; k < 3; ++k) ctr[k] = mn[k] + (mx[k] - mn[k]) / 2.0;
+  double best = INFINITY;
+  c.has_grad = false;
+  for (const auto& p : c.points) {
+    const double* q = g.at(p);
+    double dx = q[0] - ctr[0], dy = q[1] - ctr[1], dz = q[2] - ctr[2];
+    double d2 = dx * dx + dy * dy + dz * dz;
+    if (d2 < best) {
+      best = d2;
+      c.center = p;
+    }
+    c.has_grad |= p.grad;
+  }
+  if (c.has_grad) {
+    // Clusters without gradient points are partitioned lazily (nth_element) at split time.
+    LexLess less{&g, axes_by_width(mn, mx)};
+    std::sort(c.points.begin(), c.points.end(), less);
+  }
+}
+
+}  // namespace
+
+DomainDivider::DomainDivider(const double* points, const double* grad_points,
+                             const std::vector<Index>& point_indices,
+                             const std::vector<Index>& grad_point_indices,
+                             const std::vector<Index>& poly_point_indices)
+    : points_(points),
+      grad_points_(grad_points),
+      point_idcs_(point_indices),
+      grad_point_idcs_(grad_point_indices),
+      poly_point_idcs_(poly_point_indices) {
+  Geo g{points_, grad_points_};
+  Domain root;
+  root.point_indices = point_indices;
+  root.grad_point_indices = grad_point_indices;
+  root.inner_point.assign(point_indices.size(), 1);
+  root.inner_grad_point.assign(grad_point_indices.size(), 1);
+
+  // Breadth-first: every generation is split in parallel; leaves are kept in order.
+  std::vector<Domain> current;
+  current.push_back(std::move(root));
+  while (!current.empty()) {
+    const Index n = static_cast<Index>(current.size());
+    std::vector<char> split(n, 0);
+    std::vector<Domain> lefts(n), rights(n);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (Index i = 0; i < n; ++i) {
+      auto& d = current[i];
+      if (d.num_points() + 3 * d.num_grad_points() <= kMaxLeafSize) continue;
+      split[i] = 1;
+      divide_domain(g, d, lefts[i], rights[i]);
+    }
+    std::vector<Domain> next;
+    for (Index i = 0; i < n; ++i) {
+      if (!split[i]) {
+        domains_.push_back(std::move(current[i]));
+      } else {
+        next.push_back(std::move(lefts[i]));
+        next.push_back(std::move(rights[i]));
+      }
+    }
+    current = std::move(next);
+  }
+  const Index nd = static_cast<Index>(domains_.size());
+#pragma omp parallel for schedule(dynamic, 16)
+  for (Index i = 0; i < nd; ++i) merge_poly_points(domains_[i], poly_point_idcs_);
+}
+
+std::pair<std::vector<Index>, std::vector<Index>> DomainDivider::choose_coarse_points(
+    Index n_coarse) const {
+  Geo g{points_, grad_points_};
+  std::vector<Index> idcs(poly_point_idcs_);
+  std::vector<Index> grad_idcs;
+
+  std::vector<char> is_poly;
+  {
+    Index maxi = 0;
+    for (auto i : point_idcs_) maxi = std::max(maxi, i);
+    is_poly.assign(maxi + 1, 0);
+    for (auto i : poly_point_idcs_)
+      if (i <= maxi) is_poly[i] = 1;
+  }
+
+  auto* root = new Cluster;
+  for (auto i : point_idcs_)
+    if (!is_poly[i]) root->points.push_back({i, true, false});
+  for (auto i : grad_point_idcs_) root->points.push_back({i, true, true});
+  root->level = 0;
+  initialize_cluster(g, *root);
+
+  std::priority_queue<Cluster*, std::vector<Cluster*>, ClusterLess> pq;
+  Index current_size = root->center.mult();
+  pq.push(root);
+
+  while (current_size < n_coarse && !pq.empty()) {
+    Cluster* c = pq.top();
+    auto& pts = c->points;
+    const Index n = static_cast<Index>(pts.size());
+    // Split position minimising |2 prefix(i) - size|, ties resolved as std::min_element with
+    // the comparator of domain_divider.hpp:82-88.
+    Index mid = 0;
+    if (c->has_grad) {
+      std::vector<Index> prefix{0};
+      prefix.reserve(n + 1);
+      for (const auto& p : pts) prefix.push_back(prefix.back() + p.mult());
+      const Index size = prefix.back();
+      Index best = 0;
+      Index bestd = std::llabs(2 * prefix[0] - size);
+      for (Index i = 1; i < n; ++i) {
+        Index di = std::llabs(2 * prefix[i] - size);
+        if (di < bestd || (di == bestd && i % 2 == 0)) {
+          best = i;
+          bestd = di;
+        }
+      }
+      mid = best;
+    } else {
+      const Index size = n;
+      Index best = 0;
+      Index bestd = size;
+      for (Index i = 1; i < n; ++i) {
+        Index di = std::llabs(2 * i - size);
+        if (di < bestd || (di == bestd && i % 2 == 0)) {
+          best = i;
+          bestd = di;
+        }
+      }
+      mid = best;
+      if (mid > 0 && mid < n) {
+        double mn[3], mx[3];
+        bbox_of(g, pts, mn, mx);
+        LexLess less{&g, axes_by_width(mn, mx)};
+        std::nth_element(pts.begin(), pts.begin() + mid, pts.end(), less);
+      }
+    }
+    auto* left = new Cluster;
+    auto* right = new Cluster;
+    left->points.assign(pts.begin(), pts.begin() + mid);
+    right->points.assign(pts.begin() + mid, pts.end());
+    left->level = right->level = c->level + 1;
+    current_size -= c->center.mult();
+    pq.pop();
+    delete c;
+    if (!left->points.empty()) {
+      initialize_cluster(g, *left);
+      current_size += left->center.mult();
+      pq.push(left);
+    } else {
+      delete left;
+    }
+    if (!right->points.empty()) {
+      initialize_cluster(g, *right);
+      current_size += right->center.mult();
+      pq.push(right);
+    } else {
+      delete right;
+    }
+  }
+
+  while (!pq.empty()) {
+    Cluster* c = pq.top();
+    (c->center.grad ? grad_idcs : idcs).push_back(c->center.index);
+    pq.pop();
+    delete c;
+  }
+  return {std::move(idcs), std::move(grad_idcs)};
+}
+
+void monomial_row(int degree, const double* p, double* out) {
+  out[0] = 1.0;
+  if (degree >= 1) {
+    out[1] = p[0];
+    out[2] = p[1];
+    out[3] = p[2];
+  }
+  if (degree >= 2) {
+    out[4] = p[0] * p[0];
+    out[5] = p[0] * p[1];
+    out[6] = p[0] * p[2];
+    out[7] = p[1] * p[1];
+    out[8] = p[1] * p[2];
+    out[9] = p[2] * p[2];
+  }
+}
+
+namespace {
+
+// Full-pivoting LU inverse with Eigen's default rank threshold (epsilon * size * max pivot).
+// Returns false when the matrix is rank deficient.
+bool full_piv_inverse(std::vector<double> a, int n, std::vector<double>& inv) {
+  std::vector<int> rp(n), cp(n);
+  std::iota(rp.begin(), rp.end(), 0);
+  std::iota(cp.begin(), cp.end(), 0);
+  double max_pivot = 0;
+  int rank = 0;
+  for (int k = 0; k < n; ++k) {
+    int bi = k, bj = k;
+    double best = -1;
+    for (int i = k; i < n; ++i)
+      for (int j = k; j < n; ++j) {
+        double v = std::fabs(a[i * n + j]);
+        if (v > best) {
+          best = v;
+          bi = i;
+          bj = j;
+        }
+      }
+    if (k == 0) max_pivot = best;
+    if (bi != k) {
+      for (int j = 0; j < n; ++j) std::swap(a[k * n + j], a[bi * n + j]);
+      std::swap(rp[k], rp[bi]);
+    }
+    if (bj != k) {
+      for (int i = 0; i < n; ++i) std::swap(a[i * n + k], a[i * n + bj]);
+      std::swap(cp[k], cp[bj]);
+    }
+    double piv = a[k * n + k];
+    if (std::fabs(piv) > std::numeric_limits<double>::epsilon() * n * max_pivot) ++rank;
+    if (piv == 0.0) continue;
+    for (int i = k + 1; i < n; ++i) {
+      double f = a[i * n + k] / piv;
+      a[i * n + k] = f;
+      for (int j = k + 1; j < n; ++j) a[i * n + j] -= f * a[k * n + j];
+    }
+  }
+  if (rank < n) return false;
+  // Solve for each unit vector: P A Q = L U  =>  A^{-1} = Q U^{-1} L^{-1} P.
+  inv.assign(n * n, 0.0);
+  std::vector<double> x(n);
+  for (int c = 0; c < n; ++c) {
+    for (int i = 0; i < n; ++i) x[i] = (rp[i] == c) ? 1.0 : 0.0;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < i; ++j) x[i] -= a[i * n + j] * x[j];
+    for (int i = n - 1; i >= 0; --i) {
+      for (int j = i + 1; j < n; ++j) x[i] -= a[i * n + j] * x[j];
+      x[i] /= a[i * n + i];
+    }
+    for (int i = 0; i < n; ++i) inv[cp[i] * n + c] = x[i];
+  }
+  return true;
+}
+
+double l1_norm(const std::vector<double>& a, int n) {
+  double best = 0;
+  for (int j = 0; j < n; ++j) {
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += std::fabs(a[i * n + j]);
+    best = std::max(best, s);
+  }
+  return best;
+}
+
+}  // namespace
+
+std::vector<double> lagrange_coeffs(int degree, const double* poly_points, Index l,
+                                    double* rcond_out) {
+  const int n = static_cast<int>(l);
+  std::vector<double> p(n * n);
+  for (int i = 0; i < n; ++i) monomial_row(degree, poly_points + 3 * i, p.data() + i * n);
+  std::vector<double> inv;
+  if (!full_piv_inverse(p, n, inv)) throw_invalid("the set of points is not unisolvent");
+  if (rcond_out) *rcond_out = 1.0 / (l1_norm(p, n) * l1_norm(inv, n));
+  return inv;
+}
+
+std::vector<Index> unisolvent_point_set(const double* points, Index n, int degree) {
+  std::vector<Index> out;
+  if (degree < 0) return out;
+  const int l = (degree + 1) * (degree + 2) * (degree + 3) / 6;
+  std::mt19937 gen;
+  std::uniform_int_distribution<Index> dist(Index{0}, n - 1);
+  std::set<Index> best_set;
+  double best_rcond = 0.0;
+  bool found = false;
+  for (int trial = 0; trial < 100; ++trial) {
+    std::set<Index> set;
+    while (static_cast<Index>(set.size()) < l) set.insert(dist(gen));
+    std::vector<double> pp;
+    for (auto i : set)
+      for (int k = 0; k < 3; ++k) pp.push_back(points[3 * i + k]);
+    try {
+      double rc = 0;
+      lagrange_coeffs(degree, pp.data(), l, &rc);
+      if (best_rcond < rc) {
+        best_rcond = rc;
+        best_set = std::move(set);
+      }
+      found = true;
+    } catch (const Error&) {
+    }
+  }
+  if (!found) throw_runtime("could not find a unisolvent set of points");
+  out.assign(best_set.begin(), best_set.end());
+  return out;
+}
+
+}  // namespace pgpu

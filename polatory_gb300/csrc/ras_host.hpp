@@ -1,0 +1,64 @@
+// Host-side set-up of the RAS preconditioner: unisolvent polynomial points, Lagrange basis
+// coefficients and the overlapping domain decomposition with coarse-point selection.
+#pragma once
+
+#include <utility>
+#include <vector>
+
+#include "common.hpp"
+
+namespace pgpu {
+
+// One overlapping domain: indices into the full point arrays, value points first (the
+// polynomial points lead the list) and inner flags (points whose solution the domain owns).
+struct Domain {
+  std::vector<Index> point_indices;
+  std::vector<Index> grad_point_indices;
+  std::vector<char> inner_point;
+  std::vector<char> inner_grad_point;
+  Index num_points() const { return static_cast<Index>(point_indices.size()); }
+  Index num_grad_points() const { return static_cast<Index>(grad_point_indices.size()); }
+};
+
+// Restatement of preconditioner::DomainDivider (include/polatory/preconditioner/
+// domain_divider.hpp:18-321): recursive splits along the widest axes with an overlap quota of
+// 0.5 down to at most 1024 points (gradient points count three times); coarse points chosen by
+// priority-queue bisection. points/grad_points: host xyz rows of the full point sets.
+class DomainDivider {
+ public:
+  DomainDivider(const double* points, const double* grad_points,
+                const std::vector<Index>& point_indices,
+                const std::vector<Index>& grad_point_indices,
+                const std::vector<Index>& poly_point_indices);
+
+  std::pair<std::vector<Index>, std::vector<Index>> choose_coarse_points(Index n_coarse) const;
+
+  std::vector<Domain>& domains() { return domains_; }
+
+  static constexpr double kOverlapQuota = 0.5;
+  static constexpr Index kMaxLeafSize = 1024;
+
+ private:
+  const double* points_;
+  const double* grad_points_;
+  std::vector<Index> point_idcs_;
+  std::vector<Index> grad_point_idcs_;
+  std::vector<Index> poly_point_idcs_;
+  std::vector<Domain> domains_;
+};
+
+// Monomial basis rows of one point (3-D, degree <= 2; monomial_basis.hpp:171-247 order).
+void monomial_row(int degree, const double* p, double* out);
+
+// polynomial::UnisolventPointSet (unisolvent_point_set.hpp:25-66): 100 random trials of l
+// distinct points (std::mt19937 default seed, uniform_int_distribution), keeping the set with
+// the best reciprocal condition number. Returns sorted indices. Throws runtime error
+// "could not find a unisolvent set of points" when no trial is invertible.
+std::vector<Index> unisolvent_point_set(const double* points, Index n, int degree);
+
+// Inverse of the monomial matrix of l unisolvent points (lagrange_basis.hpp:28-45).
+// Throws invalid_argument "the set of points is not unisolvent".
+std::vector<double> lagrange_coeffs(int degree, const double* poly_points, Index l,
+                                    double* rcond_out = nullptr);
+
+}  // namespace pgpu

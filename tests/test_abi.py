@@ -1,0 +1,95 @@
+"""CPU checks of the C ABI: the library loads, exports every function include/polatory_gpu.h
+declares, and its host-side entry points (kernel formulas, model validation) agree with the
+oracle. No GPU compute is called here."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+import polatory_gb300 as pg
+from polatory_gb300 import _lib
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_functions():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"\b(pgpu_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol():
+    lib = C.CDLL(str(_lib.LIB_PATH))
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    assert len(declared_functions()) >= 30
+
+
+def test_version():
+    assert _lib.lib.pgpu_version() >= 100
+
+
+RBFS = [pg.Biharmonic2D, pg.Biharmonic3D, pg.CovCubic, pg.CovExponential, pg.CovGaussian,
+        pg.CovGeneralizedCauchy3, pg.CovGeneralizedCauchy5, pg.CovGeneralizedCauchy7,
+        pg.CovGeneralizedCauchy9, pg.CovSpherical, pg.CovSpheroidal3, pg.CovSpheroidal5,
+        pg.CovSpheroidal7, pg.CovSpheroidal9, pg.Triharmonic2D, pg.Triharmonic3D]
+
+
+@pytest.mark.parametrize("cls", RBFS, ids=lambda c: c.short_name)
+def test_kernel_formulas_match_oracle(cls):
+    g = np.random.Generator(np.random.PCG64(123))
+    params = [1.3, 0.2] if cls._polyharmonic else [1.3, 0.8]
+    rbf = cls(params)
+    a = np.diag([1.2, 0.9, 1 / 1.08]) @ np.linalg.qr(g.standard_normal((3, 3)))[0]
+    if np.linalg.det(a) < 0:
+        a[:, 0] *= -1
+    rbf.anisotropy = a
+    diffs = g.uniform(-1.5, 1.5, (200, 3))
+    vals = rbf.evaluate(diffs)
+    grads = rbf.evaluate_gradient(diffs)
+    has_h = cls.short_name not in ("cub", "sph")
+    if has_h:
+        hess = rbf.evaluate_hessian(diffs)
+    else:
+        with pytest.raises(pg.PolatoryError):
+            rbf.evaluate_hessian(diffs)
+    for i, d in enumerate(diffs):
+        v, gr, h = oracle.rbf_evaluate(rbf._kind, params, a, d)
+        assert vals[i] == pytest.approx(v, rel=1e-13, abs=1e-14)
+        np.testing.assert_allclose(grads[i], gr, rtol=1e-12, atol=1e-13)
+        if has_h:
+            np.testing.assert_allclose(hess[i], h, rtol=1e-11, atol=1e-12)
+
+
+def test_model_validation_errors():
+    with pytest.raises(pg.PolatoryError, match="poly_degree must be within 0 to 2"):
+        pg.Model(pg.Biharmonic3D([1.0]), -1)
+    with pytest.raises(pg.PolatoryError, match="poly_degree must be within 2 to 2"):
+        pg.Model(pg.Triharmonic2D([1.0]), 1)
+    m = pg.Model(pg.Biharmonic3D([1.0]))
+    assert m.poly_degree == 0 and m.poly_basis_size == 1
+    m = pg.Model(pg.CovExponential([1.0, 0.2]))
+    assert m.poly_degree == -1 and m.poly_basis_size == 0
+    with pytest.raises(ValueError):
+        m.nugget = -1.0
+    with pytest.raises(ValueError, match="positive determinant"):
+        pg.Biharmonic3D([1.0]).anisotropy = np.diag([1.0, 1.0, -1.0])
+    with pytest.raises(RuntimeError, match="unknown RBF name"):
+        pg.make_rbf("xyz", [])
+
+
+def test_cpd_orders_and_support():
+    assert pg.Biharmonic3D([1.0]).cpd_order == 1
+    assert pg.Triharmonic3D([1.0]).cpd_order == 2
+    assert pg.Biharmonic2D([1.0]).cpd_order == 2
+    assert pg.Triharmonic2D([1.0]).cpd_order == 3
+    assert pg.CovExponential([1.0, 0.5]).cpd_order == 0
+    assert pg.CovCubic([1.0, 0.5]).support_radius_isotropic() == 0.5
+    assert pg.CovSpherical([1.0, 0.7]).support_radius_isotropic() == 0.7
+    assert np.isinf(pg.CovExponential([1.0, 0.5]).support_radius_isotropic())

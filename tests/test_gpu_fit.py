@@ -1,0 +1,97 @@
+"""GPU fits against the oracle: the fitted weights reproduce the data to the requested absolute
+tolerance (interpolation/solver.hpp convergence test; test/interpolation/test_fitter.cpp), the
+device evaluation agrees with the oracle's exact sums for the same weights, and the interpolant
+agrees with the exact solution of the fit system at query points."""
+import numpy as np
+import pytest
+
+import oracle
+import polatory_gb300 as pg
+from polatory_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def check_fit(interp, model, pts, vals, tol, queries):
+    w = interp.weights
+    l = model.poly_basis_size
+    assert w.shape == (pts.shape[0] + l,)
+    # Residual at every data point with exact FP64 sums (oracle).
+    fit_vals = oracle.direct_evaluate(model, pts, w, pts) + model.nugget * w[: pts.shape[0]]
+    assert np.max(np.abs(fit_vals - vals)) <= tol
+    # Device evaluation == oracle evaluation for the same weights.
+    got = interp.evaluate(queries)
+    want = oracle.direct_evaluate(model, pts, w, queries)
+    return got, want
+
+
+@pytest.mark.parametrize("precision", [pg.PLAIN, pg.MIXED], ids=["plain", "mixed"])
+def test_fit_small_biharmonic(precision):
+    # Fewer than 2048 points: one RAS level (the coarse solve alone).
+    g = np.random.Generator(np.random.PCG64(21))
+    pts = g.random((1500, 3))
+    vals = workloads.f_c1(pts)
+    model = pg.Model(pg.Biharmonic3D([1.0]), 1)
+    interp = pg.Interpolant(model, precision)
+    tol = 1e-5
+    interp.fit(pts, vals, tol)
+    q = g.random((700, 3))
+    got, want = check_fit(interp, model, pts, vals, tol, q)
+    tol_eval = 1e-10 if precision == pg.PLAIN else 1e-5
+    assert np.max(np.abs(got - want)) <= tol_eval
+    exact = oracle.fit_exact(model, pts, vals)
+    ref = oracle.direct_evaluate(model, pts, exact, q)
+    assert np.max(np.abs(got - ref)) <= 1e-3
+
+
+@pytest.mark.parametrize("precision", [pg.PLAIN, pg.MIXED], ids=["plain", "mixed"])
+def test_fit_c1_two_levels(precision):
+    # The C1 workload: 10,000 points, biharmonic, degree 1, tol 1e-5 (two RAS levels).
+    pts, vals, grid = workloads.c1()
+    model = pg.Model(pg.Biharmonic3D([1.0]), 1)
+    interp = pg.Interpolant(model, precision)
+    tol = 1e-5
+    interp.fit(pts, vals, tol)
+    stats = interp.fit_stats
+    assert stats["levels"] == 2
+    assert stats["iterations"] <= 60
+    q = grid[::97]
+    got, want = check_fit(interp, model, pts, vals, tol, q)
+    assert np.max(np.abs(got - want)) <= (1e-9 if precision == pg.PLAIN else 1e-5)
+
+
+def test_fit_covariance_with_nugget():
+    g = np.random.Generator(np.random.PCG64(22))
+    pts = g.random((3000, 3))
+    vals = np.sin(4 * pts[:, 0]) + pts[:, 1]
+    rbf = pg.CovExponential([1.0, 0.5])
+    rbf.anisotropy = np.diag([1.0, 1.0, 2.0])
+    model = pg.Model(rbf, 0)
+    model.nugget = 1e-3
+    interp = pg.Interpolant(model)
+    tol = 1e-4
+    interp.fit(pts, vals, tol)
+    q = g.random((500, 3))
+    got, want = check_fit(interp, model, pts, vals, tol, q)
+    assert np.max(np.abs(got - want)) <= 1e-10
+
+
+def test_fit_argument_errors():
+    model = pg.Model(pg.Biharmonic3D([1.0]), 1)
+    interp = pg.Interpolant(model)
+    pts = np.random.default_rng(0).random((10, 3))
+    with pytest.raises(pg.PolatoryError, match="tolerance must be positive"):
+        interp.fit(pts, np.zeros(10), 0.0)
+    with pytest.raises(pg.PolatoryError, match="greater than or equal to 4"):
+        interp.fit(pts[:3], np.zeros(3), 1e-3)
+    with pytest.raises(pg.PolatoryError, match="has not been fitted"):
+        interp.evaluate(pts)
+
+
+def test_max_iter_reached():
+    g = np.random.Generator(np.random.PCG64(23))
+    pts = g.random((5000, 3))
+    vals = workloads.f_c1(pts)
+    interp = pg.Interpolant(pg.Model(pg.Biharmonic3D([1.0]), 1))
+    with pytest.raises(pg.PolatoryError, match="reached the maximum number of iterations"):
+        interp.fit(pts, vals, 1e-12, max_iter=2)
