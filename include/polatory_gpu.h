@@ -128,6 +128,11 @@ int pgpu_evaluator_set_accuracy(pgpu_evaluator* ev, double accuracy);
 int pgpu_evaluator_set_source_points(pgpu_evaluator* ev, const double* points, int64_t n);
 int pgpu_evaluator_set_target_points(pgpu_evaluator* ev, const double* points, int64_t n);
 int pgpu_evaluator_set_points(pgpu_evaluator* ev, const double* points, int64_t n);
+/* Tuning (no reference counterpart; the reference picks everything from the accuracy):
+ * backend 0 = automatic, 1 = exact direct sums, 2 = FMM where the kernel supports it;
+ * order = Chebyshev nodes per axis (4, 6 or 8; 0 = from the accuracy); leaf_level = octree
+ * depth of the leaves (-1 = automatic). */
+int pgpu_evaluator_configure(pgpu_evaluator* ev, int backend, int order, int leaf_level);
 /* weights: km * n_sources values in the caller's point order. */
 int pgpu_evaluator_set_weights(pgpu_evaluator* ev, const double* weights, int64_t n);
 /* out: kn * n_targets values in the caller's target order. */

@@ -291,6 +291,10 @@ class FmmEvaluator:
             lib.pgpu_evaluator_destroy(h)
             self._h = None
 
+    def configure(self, backend: int = 0, order: int = 0, leaf_level: int = -1):
+        """backend 0 auto, 1 direct, 2 FMM; order 4/6/8 (0 = from accuracy); leaf_level -1 auto."""
+        check(lib.pgpu_evaluator_configure(self._h, backend, order, leaf_level))
+
     def set_accuracy(self, acc: float):
         check(lib.pgpu_evaluator_set_accuracy(self._h, float(acc)))
 

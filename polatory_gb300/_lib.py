@@ -82,6 +82,7 @@ def _load():
         "pgpu_evaluator_set_target_points": ([P, P, I64], C.c_int),
         "pgpu_evaluator_set_points": ([P, P, I64], C.c_int),
         "pgpu_evaluator_set_weights": ([P, P, I64], C.c_int),
+        "pgpu_evaluator_configure": ([P, C.c_int, C.c_int, C.c_int], C.c_int),
         "pgpu_evaluator_evaluate": ([P, P, I64], C.c_int),
         "pgpu_interpolant_create": ([C.POINTER(PgpuModel), C.POINTER(P)], C.c_int),
         "pgpu_interpolant_destroy": ([P], C.c_int),

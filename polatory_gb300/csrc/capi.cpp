@@ -61,6 +61,8 @@ struct pgpu_evaluator {
   std::unique_ptr<Evaluator<double>> e64;
   std::unique_ptr<Evaluator<float>> e32;
   bool weights_set = false;
+  int backend = 0;
+  FarFieldConfig ff;
 };
 
 struct pgpu_interpolant {
@@ -219,10 +221,26 @@ int pgpu_evaluator_set_accuracy(pgpu_evaluator* ev, double accuracy) {
   });
 }
 
+int pgpu_evaluator_configure(pgpu_evaluator* ev, int backend, int order, int leaf_level) {
+  return guarded([&] {
+    check_ptr(ev, "evaluator");
+    if (backend < 0 || backend > 2) throw_invalid("unknown backend");
+    if (order != 0 && order != 4 && order != 6 && order != 8) throw_invalid("order must be 4, 6 or 8");
+    if (leaf_level < -1 || leaf_level > 20) throw_invalid("leaf_level out of range");
+    ev->backend = backend;
+    ev->ff.order = order;
+    ev->ff.leaf_level = leaf_level;
+    ev->e64.reset();
+    ev->e32.reset();
+  });
+}
+
 namespace {
 void rebuild(pgpu_evaluator* ev) {
   if (ev->precision == PGPU_PRECISION_PLAIN) {
     ev->e64 = std::make_unique<Evaluator<double>>(ev->model, ev->bbox, ev->accuracy, ev->accuracy);
+    ev->e64->set_backend(ev->backend);
+    ev->e64->set_far_field(ev->ff);
     if (ev->symmetric) ev->e64->set_points(ev->src.data(), ev->n_src, nullptr, 0);
     else {
       ev->e64->set_sources(ev->src.data(), ev->n_src, nullptr, 0);
@@ -230,6 +248,8 @@ void rebuild(pgpu_evaluator* ev) {
     }
   } else {
     ev->e32 = std::make_unique<Evaluator<float>>(ev->model, ev->bbox, ev->accuracy, ev->accuracy);
+    ev->e32->set_backend(ev->backend);
+    ev->e32->set_far_field(ev->ff);
     if (ev->symmetric) ev->e32->set_points(ev->src.data(), ev->n_src, nullptr, 0);
     else {
       ev->e32->set_sources(ev->src.data(), ev->n_src, nullptr, 0);

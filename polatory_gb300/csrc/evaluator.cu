@@ -221,7 +221,11 @@ void Evaluator<T>::set_weights(const double* w) {
 // Direct sums are exact and, on this GPU, cheaper than building a tree until the pair count
 // reaches a few hundred million; the reference's CPU threshold is N*M < 2^20
 // (src/fmm/fmm_evaluator.hpp:227).
-constexpr double kDirectPairLimit = 1.0 * (1 << 26);
+// FP64 pairs cost ~60x more than FP32 pairs on this GPU, but the FP64 far field costs more too.
+template <class T>
+constexpr double direct_pair_limit() {
+  return sizeof(T) == 8 ? 536870912.0 /* 2^29 */ : 4294967296.0 /* 2^32 */;
+}
 
 template <class T>
 void Evaluator<T>::evaluate(double* out, bool with_poly) {
@@ -233,7 +237,9 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
   const double pairs = static_cast<double>(mu_ + sigma_) * static_cast<double>(m_ + mg_);
   for (auto& tp : terms_) {
     Term& t = *tp;
-    bool use_fmm = !force_direct_ && pairs > kDirectPairLimit && Fmm<T>::supported(t.rbf.kind);
+    const bool fmm_ok = Fmm<T>::supported(t.rbf.kind) && sigma_ == 0 && mg_ == 0;
+    bool use_fmm = fmm_ok && (backend_ == kBackendFmm ||
+                              (backend_ == kBackendAuto && pairs > direct_pair_limit<T>()));
     if (!use_fmm) {
       DirectSources<T> src{t.spos.data(), t.vw.data(), mu_, t.sgpos.data(), t.gg.data(), sigma_};
       DirectTargets<T> trg{t.tpos.data(), m_, out_v, t.tgpos.data(), mg_, out_g};

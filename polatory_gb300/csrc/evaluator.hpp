@@ -44,7 +44,7 @@ Bbox3 bbox_of_device_points(const double* pts, Index n);
 
 // FMM / direct configuration selected from an accuracy (fmm_accuracy_estimator.hpp:74-121).
 struct FarFieldConfig {
-  int order = 6;          // interpolation nodes per axis
+  int order = 0;          // interpolation nodes per axis (0: from the accuracy)
   int leaf_level = -1;    // -1: automatic
 };
 
@@ -78,8 +78,10 @@ class Evaluator {
   Index n_sources() const { return mu_ + 3 * sigma_; }
   Index n_targets() const { return m_ + 3 * mg_; }
   const EvalStats& stats() const { return stats_; }
-  // Forces the direct backend (exact sums), e.g. for the residual probe.
-  void force_direct(bool f) { force_direct_ = f; }
+  // Backend choice: automatic (by pair count), exact direct sums, or the FMM where supported.
+  static constexpr int kBackendAuto = 0, kBackendDirect = 1, kBackendFmm = 2;
+  void set_backend(int b) { backend_ = b; }
+  void force_direct(bool f) { backend_ = f ? kBackendDirect : kBackendAuto; }
   void set_far_field(const FarFieldConfig& c) { ff_ = c; ff_set_ = true; }
 
  private:
@@ -89,7 +91,7 @@ class Evaluator {
   Bbox3 bbox_;
   double accuracy_, grad_accuracy_;
   bool symmetric_ = false;
-  bool force_direct_ = false;
+  int backend_ = kBackendAuto;
   bool ff_set_ = false;
   FarFieldConfig ff_;
   Index mu_ = 0, sigma_ = 0, m_ = 0, mg_ = 0;

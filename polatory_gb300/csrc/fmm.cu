@@ -1,35 +1,930 @@
-// Interpolation-based FMM (placeholder until the tree and passes land): reports no support, so
-// every evaluator uses the exact direct backend.
+// Interpolation-based FMM on the GPU (value sources -> value targets).
+//
+// Tree: points (already in the anisotropy frame) get 3 x Lf-bit Morton keys of their leaf cell in
+// the cube of src/fmm/utility.hpp:18-33 (make_box); keys are radix-sorted and run-length encoded
+// into the non-empty cells of every level (the uniform-depth tree of the reference's group tree).
+// Far field: tensor-product Chebyshev interpolation of order p (p^3 nodes per cell):
+//   P2M   M_c[a]  = sum_j w_j S_a(xi_j)                       (leaf cells)
+//   M2M   M_P[a] += sum_b M_c[b] S_a(child node b in P)        (separable, 3 passes)
+//   M2L   L_t[a] += sum_b K_o[a][b] M_s[b]  for the cells s of t's interaction list, where o is
+//         the offset s - t in cell units and K_o[a][b] = phi(r_k (x_a - x_b) - 2 r_k o) depends
+//         only on (level, o): one dense p^3 x p^3 matrix per offset, shared by all pairs.
+//   L2L   L_c[b] += sum_a L_P[a] S_a(child node b in P)
+//   L2P   u(x)  += sum_a L_t[a] S_a(xi)
+// Near field (P2P): the 27 neighbour leaves (separation criterion 1, fmm/kernel.hpp:71),
+// sources staged in shared memory one tile at a time.
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
 #include "fmm.hpp"
+#include "linalg.hpp"
 
 namespace pgpu {
 
-template <class T>
-struct Fmm<T>::Impl {};
+namespace {
+
+constexpr int kMaxP = 8;
+constexpr int kNOff = 343;  // 7^3 offsets in [-3, 3]^3
+constexpr int kTT = 32;     // target cells per M2L tile
 
 template <class T>
-bool Fmm<T>::supported(int) { return false; }
+struct Cheb {
+  int p;
+  T tkm[kMaxP][kMaxP];   // T_k(x_m) [m][k]
+  T wlo[kMaxP][kMaxP];   // S_a(-0.5 + 0.5 x_b) [a][b]
+  T whi[kMaxP][kMaxP];   // S_a(+0.5 + 0.5 x_b) [a][b]
+};
 
-template <class T>
-Fmm<T>::Fmm(int, const KParams<T>&, const Mat3&, const double*, double, double) : impl_(new Impl) {}
+// 1-D Chebyshev interpolation basis S_m(x) = 1/p + 2/p sum_{k>=1} T_k(x_m) T_k(x).
+double cheb_node(int p, int m) { return std::cos((2.0 * m + 1.0) * M_PI / (2.0 * p)); }
 
-template <class T>
-Fmm<T>::~Fmm() { delete impl_; }
-
-template <class T>
-void Fmm<T>::set_config(const FarFieldConfig&) {}
-template <class T>
-void Fmm<T>::set_points(const P4<T>*, Index, const P4<T>*, Index) {}
-template <class T>
-void Fmm<T>::set_sources(const P4<T>*, Index, const P4<T>*, Index) {}
-template <class T>
-void Fmm<T>::set_targets(const P4<T>*, Index, const P4<T>*, Index) {}
-template <class T>
-void Fmm<T>::evaluate(const T*, const T*, double*, double*) {
-  throw_runtime("FMM backend unavailable");
+double cheb_s_host(int p, int m, double x) {
+  double xm = cheb_node(p, m);
+  double s = 1.0 / p;
+  double t0 = 1.0, t1 = x, u0 = 1.0, u1 = xm;
+  for (int k = 1; k < p; ++k) {
+    s += 2.0 / p * t1 * u1;
+    double t2 = 2 * x * t1 - t0;
+    double u2 = 2 * xm * u1 - u0;
+    t0 = t1;
+    t1 = t2;
+    u0 = u1;
+    u1 = u2;
+  }
+  return s;
 }
+
 template <class T>
-Index Fmm<T>::near_pairs() const { return 0; }
+Cheb<T> make_cheb(int p) {
+  Cheb<T> c{};
+  c.p = p;
+  for (int m = 0; m < p; ++m) {
+    double xm = cheb_node(p, m);
+    double t0 = 1.0, t1 = xm;
+    c.tkm[m][0] = T(1);
+    if (p > 1) c.tkm[m][1] = static_cast<T>(xm);
+    for (int k = 2; k < p; ++k) {
+      double t2 = 2 * xm * t1 - t0;
+      c.tkm[m][k] = static_cast<T>(t2);
+      t0 = t1;
+      t1 = t2;
+    }
+  }
+  for (int a = 0; a < p; ++a)
+    for (int b = 0; b < p; ++b) {
+      double xb = cheb_node(p, b);
+      c.wlo[a][b] = static_cast<T>(cheb_s_host(p, a, -0.5 + 0.5 * xb));
+      c.whi[a][b] = static_cast<T>(cheb_s_host(p, a, 0.5 + 0.5 * xb));
+    }
+  return c;
+}
+
+template <int P, class T>
+__device__ __forceinline__ void cheb_basis(const Cheb<T>& c, T x, T* s) {
+  T t[P];
+  t[0] = T(1);
+  if (P > 1) t[1] = x;
+#pragma unroll
+  for (int k = 2; k < P; ++k) t[k] = T(2) * x * t[k - 1] - t[k - 2];
+#pragma unroll
+  for (int m = 0; m < P; ++m) {
+    T v = T(0);
+#pragma unroll
+    for (int k = 1; k < P; ++k) v += c.tkm[m][k] * t[k];
+    s[m] = (T(1) + T(2) * v) / T(P);
+  }
+}
+
+// ---- Morton keys --------------------------------------------------------------------------
+__host__ __device__ __forceinline__ uint64_t spread3(uint64_t x) {
+  x &= 0x1fffffULL;
+  x = (x | (x << 32)) & 0x1f00000000ffffULL;
+  x = (x | (x << 16)) & 0x1f0000ff0000ffULL;
+  x = (x | (x << 8)) & 0x100f00f00f00f00fULL;
+  x = (x | (x << 4)) & 0x10c30c30c30c30c3ULL;
+  x = (x | (x << 2)) & 0x1249249249249249ULL;
+  return x;
+}
+
+__host__ __device__ __forceinline__ uint64_t compact3(uint64_t x) {
+  x &= 0x1249249249249249ULL;
+  x = (x ^ (x >> 2)) & 0x10c30c30c30c30c3ULL;
+  x = (x ^ (x >> 4)) & 0x100f00f00f00f00fULL;
+  x = (x ^ (x >> 8)) & 0x1f0000ff0000ffULL;
+  x = (x ^ (x >> 16)) & 0x1f00000000ffffULL;
+  x = (x ^ (x >> 32)) & 0x1fffffULL;
+  return x;
+}
+
+__host__ __device__ __forceinline__ uint64_t morton(uint64_t x, uint64_t y, uint64_t z) {
+  return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2);
+}
+
+__device__ __forceinline__ void unmorton(uint64_t k, int& x, int& y, int& z) {
+  x = static_cast<int>(compact3(k));
+  y = static_cast<int>(compact3(k >> 1));
+  z = static_cast<int>(compact3(k >> 2));
+}
+
+struct Box {
+  double min[3];
+  double width;
+};
+
+template <class T>
+__global__ void keys_kernel(const P4<T>* __restrict__ pos, Index n, Box box, int lf,
+                            uint64_t* __restrict__ keys, Index* __restrict__ idx) {
+  Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double cells = static_cast<double>(1 << lf);
+  const double inv = cells / box.width;
+  P4<T> p = pos[i];
+  int c[3];
+  double v[3] = {static_cast<double>(p.x), static_cast<double>(p.y), static_cast<double>(p.z)};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    double f = floor((v[k] - box.min[k]) * inv);
+    f = fmin(fmax(f, 0.0), cells - 1.0);
+    c[k] = static_cast<int>(f);
+  }
+  keys[i] = morton(c[0], c[1], c[2]);
+  idx[i] = i;
+}
+
+template <class T>
+__global__ void gather_pos_kernel(const P4<T>* __restrict__ pos, const Index* __restrict__ perm,
+                                  Index n, P4<T>* __restrict__ out) {
+  Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = pos[perm[i]];
+}
+
+template <class T>
+__global__ void gather_w_kernel(const T* __restrict__ w, const Index* __restrict__ perm, Index n,
+                                T* __restrict__ out) {
+  Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = w[perm[i]];
+}
+
+__global__ void rle_flags_kernel(const uint64_t* __restrict__ keys, Index n, int shift,
+                                 Index* __restrict__ flags) {
+  Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  flags[i] = (i == 0 || (keys[i] >> shift) != (keys[i - 1] >> shift)) ? 1 : 0;
+}
+
+__global__ void rle_scatter_kernel(const uint64_t* __restrict__ keys, Index n, int shift,
+                                   const Index* __restrict__ scan, uint64_t* __restrict__ ukeys,
+                                   Index* __restrict__ start, Index* __restrict__ parent) {
+  Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Index u = scan[i] - 1;
+  if (parent) parent[i] = u;
+  if (i == 0 || (keys[i] >> shift) != (keys[i - 1] >> shift)) {
+    ukeys[u] = keys[i] >> shift;
+    start[u] = i;
+  }
+}
+
+__device__ __forceinline__ Index find_key(const uint64_t* __restrict__ keys, Index n, uint64_t k) {
+  Index lo = 0, hi = n;
+  while (lo < hi) {
+    Index mid = (lo + hi) >> 1;
+    if (keys[mid] < k) lo = mid + 1;
+    else hi = mid;
+  }
+  return (lo < n && keys[lo] == k) ? lo : -1;
+}
+
+// M2L interaction table: children of the parent's neighbours that are not adjacent.
+__global__ void m2l_table_kernel(const uint64_t* __restrict__ tkeys, Index nt,
+                                 const uint64_t* __restrict__ skeys, Index ns, int level,
+                                 int* __restrict__ table, Index* __restrict__ count) {
+  Index t = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  int cx, cy, cz;
+  unmorton(tkeys[t], cx, cy, cz);
+  const int px = cx >> 1, py = cy >> 1, pz = cz >> 1;
+  const int n = 1 << level;
+  int* row = table + t * kNOff;
+  Index cnt = 0;
+  for (int dx = -1; dx <= 1; ++dx)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dz = -1; dz <= 1; ++dz)
+        for (int e = 0; e < 8; ++e) {
+          int qx = 2 * (px + dx) + (e & 1), qy = 2 * (py + dy) + ((e >> 1) & 1),
+              qz = 2 * (pz + dz) + ((e >> 2) & 1);
+          if (qx < 0 || qy < 0 || qz < 0 || qx >= n || qy >= n || qz >= n) continue;
+          int ox = qx - cx, oy = qy - cy, oz = qz - cz;
+          if (abs(ox) <= 1 && abs(oy) <= 1 && abs(oz) <= 1) continue;
+          Index s = find_key(skeys, ns, morton(qx, qy, qz));
+          if (s < 0) continue;
+          row[(ox + 3) * 49 + (oy + 3) * 7 + (oz + 3)] = static_cast<int>(s);
+          ++cnt;
+        }
+  count[t] = cnt;
+}
+
+__global__ void p2p_table_kernel(const uint64_t* __restrict__ tkeys, Index nt,
+                                 const uint64_t* __restrict__ skeys, Index ns, int level,
+                                 int* __restrict__ table) {
+  Index t = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  int cx, cy, cz;
+  unmorton(tkeys[t], cx, cy, cz);
+  const int n = 1 << level;
+  int j = 0;
+  for (int dx = -1; dx <= 1; ++dx)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dz = -1; dz <= 1; ++dz) {
+        int qx = cx + dx, qy = cy + dy, qz = cz + dz;
+        int s = -1;
+        if (qx >= 0 && qy >= 0 && qz >= 0 && qx < n && qy < n && qz < n)
+          s = static_cast<int>(find_key(skeys, ns, morton(qx, qy, qz)));
+        table[t * 27 + j++] = s;
+      }
+}
+
+template <int KIND, class T>
+__global__ void m2l_matrix_kernel(KParams<T> kp, int p, double r, const double* __restrict__ nodes,
+                                  T* __restrict__ K) {
+  const Index p3 = static_cast<Index>(p) * p * p;
+  const Index total = kNOff * p3 * p3;
+  for (Index e = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x; e < total;
+       e += static_cast<Index>(gridDim.x) * blockDim.x) {
+    const Index o = e / (p3 * p3);
+    const Index ab = e % (p3 * p3);
+    const int a = static_cast<int>(ab / p3), b = static_cast<int>(ab % p3);
+    const int ox = static_cast<int>(o / 49) - 3, oy = static_cast<int>((o / 7) % 7) - 3,
+              oz = static_cast<int>(o % 7) - 3;
+    const int ax = a / (p * p), ay = (a / p) % p, az = a % p;
+    const int bx = b / (p * p), by = (b / p) % p, bz = b % p;
+    double dx = r * (nodes[ax] - nodes[bx]) - 2.0 * r * ox;
+    double dy = r * (nodes[ay] - nodes[by]) - 2.0 * r * oy;
+    double dz = r * (nodes[az] - nodes[bz]) - 2.0 * r * oz;
+    KParams<double> kd{static_cast<double>(kp.p0), static_cast<double>(kp.p1)};
+    K[e] = static_cast<T>(rbf_value<KIND>(dx * dx + dy * dy + dz * dz, kd));
+  }
+}
+
+// ---- passes ------------------------------------------------------------------------------
+
+template <int P, class T>
+__global__ void __launch_bounds__(256)
+    p2m_kernel(Cheb<T> ch, const P4<T>* __restrict__ spos, const T* __restrict__ sw,
+               const Index* __restrict__ leaf_start, const uint64_t* __restrict__ leaf_keys,
+               Box box, int lf, T* __restrict__ M) {
+  constexpr int P3 = P * P * P;
+  const Index leaf = blockIdx.x;
+  __shared__ T s_b[32][3][P];
+  __shared__ T s_w[32];
+  int cx, cy, cz;
+  unmorton(leaf_keys[leaf], cx, cy, cz);
+  const double wk = box.width / static_cast<double>(1 << lf);
+  const T ctr[3] = {static_cast<T>(box.min[0] + (cx + 0.5) * wk),
+                    static_cast<T>(box.min[1] + (cy + 0.5) * wk),
+                    static_cast<T>(box.min[2] + (cz + 0.5) * wk)};
+  const T inv_r = static_cast<T>(2.0 / wk);
+  const Index beg = leaf_start[leaf], end = leaf_start[leaf + 1];
+  T acc[(P3 + 255) / 256];
+#pragma unroll
+  for (int q = 0; q < (P3 + 255) / 256; ++q) acc[q] = T(0);
+  for (Index base = beg; base < end; base += 32) {
+    const int cnt = static_cast<int>(min(static_cast<Index>(32), end - base));
+    __syncthreads();
+    if (threadIdx.x < 3 * cnt) {
+      const int j = threadIdx.x / 3, d = threadIdx.x % 3;
+      P4<T> pt = spos[base + j];
+      T x = (d == 0 ? pt.x : (d == 1 ? pt.y : pt.z));
+      cheb_basis<P>(ch, (x - ctr[d]) * inv_r, s_b[j][d]);
+    }
+    if (threadIdx.x < cnt) s_w[threadIdx.x] = sw[base + threadIdx.x];
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < (P3 + 255) / 256; ++q) {
+      const int a = threadIdx.x + 256 * q;
+      if (a < P3) {
+        const int ax = a / (P * P), ay = (a / P) % P, az = a % P;
+        T s = T(0);
+        for (int j = 0; j < cnt; ++j) s += s_w[j] * s_b[j][0][ax] * s_b[j][1][ay] * s_b[j][2][az];
+        acc[q] += s;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < (P3 + 255) / 256; ++q) {
+    const int a = threadIdx.x + 256 * q;
+    if (a < P3) M[leaf * P3 + a] = acc[q];
+  }
+}
+
+// Separable transfer of one p^3 tensor: out[a] = sum_b Wx[ax][bx] Wy[ay][by] Wz[az][bz] in[b]
+// (transpose = false) or the transposed map (transpose = true). Uses two scratch tensors.
+template <int P, class T>
+__device__ __forceinline__ T sep_transfer(const T (*wx)[kMaxP], const T (*wy)[kMaxP],
+                                          const T (*wz)[kMaxP], bool transpose, T* in, T* t1,
+                                          T* t2) {
+  constexpr int P3 = P * P * P;
+  const int a = threadIdx.x;
+  const int ax = a / (P * P), ay = (a / P) % P, az = a % P;
+  // pass z
+  if (a < P3) {
+    T s = T(0);
+#pragma unroll
+    for (int b = 0; b < P; ++b) s += (transpose ? wz[b][az] : wz[az][b]) * in[(ax * P + ay) * P + b];
+    t1[a] = s;
+  }
+  __syncthreads();
+  if (a < P3) {
+    T s = T(0);
+#pragma unroll
+    for (int b = 0; b < P; ++b) s += (transpose ? wy[b][ay] : wy[ay][b]) * t1[(ax * P + b) * P + az];
+    t2[a] = s;
+  }
+  __syncthreads();
+  T s = T(0);
+  if (a < P3) {
+#pragma unroll
+    for (int b = 0; b < P; ++b) s += (transpose ? wx[b][ax] : wx[ax][b]) * t2[(b * P + ay) * P + az];
+  }
+  __syncthreads();
+  return s;
+}
+
+template <int P, class T>
+__global__ void m2m_kernel(Cheb<T> ch, const Index* __restrict__ child_start,
+                           const uint64_t* __restrict__ child_keys, const T* __restrict__ Mc,
+                           T* __restrict__ Mp) {
+  constexpr int P3 = P * P * P;
+  __shared__ T s_in[P3], s_t1[P3], s_t2[P3];
+  const Index parent = blockIdx.x;
+  const Index c0 = child_start[parent], c1 = child_start[parent + 1];
+  T acc = T(0);
+  for (Index c = c0; c < c1; ++c) {
+    const uint64_t k = child_keys[c];
+    for (int e = threadIdx.x; e < P3; e += blockDim.x) s_in[e] = Mc[c * P3 + e];
+    __syncthreads();
+    const T(*wx)[kMaxP] = (k & 1) ? ch.whi : ch.wlo;
+    const T(*wy)[kMaxP] = (k & 2) ? ch.whi : ch.wlo;
+    const T(*wz)[kMaxP] = (k & 4) ? ch.whi : ch.wlo;
+    acc += sep_transfer<P>(wx, wy, wz, false, s_in, s_t1, s_t2);
+  }
+  if (threadIdx.x < P3) Mp[parent * P3 + threadIdx.x] = acc;
+}
+
+template <int P, class T>
+__global__ void l2l_kernel(Cheb<T> ch, const Index* __restrict__ parent_of,
+                           const uint64_t* __restrict__ child_keys, const T* __restrict__ Lp,
+                           T* __restrict__ Lc) {
+  constexpr int P3 = P * P * P;
+  __shared__ T s_in[P3], s_t1[P3], s_t2[P3];
+  const Index c = blockIdx.x;
+  const Index parent = parent_of[c];
+  const uint64_t k = child_keys[c];
+  for (int e = threadIdx.x; e < P3; e += blockDim.x) s_in[e] = Lp[parent * P3 + e];
+  __syncthreads();
+  const T(*wx)[kMaxP] = (k & 1) ? ch.whi : ch.wlo;
+  const T(*wy)[kMaxP] = (k & 2) ? ch.whi : ch.wlo;
+  const T(*wz)[kMaxP] = (k & 4) ? ch.whi : ch.wlo;
+  T v = sep_transfer<P>(wx, wy, wz, true, s_in, s_t1, s_t2);
+  if (threadIdx.x < P3) Lc[c * P3 + threadIdx.x] += v;
+}
+
+// M2L over a tile of kTT target cells: every non-adjacent offset o with at least one source in
+// the tile is applied as a dense (p^3 x p^3) x (p^3 x kTT) product with K_o streamed in 8-row
+// chunks through shared memory; the local expansions stay in registers across all offsets.
+template <int P, class T>
+__global__ void __launch_bounds__(256)
+    m2l_kernel(const T* __restrict__ K, const int* __restrict__ table, Index nt,
+               const T* __restrict__ Ms, T* __restrict__ L) {
+  constexpr int P3 = P * P * P;
+  constexpr int NC = P3 / 8;  // row chunks
+  extern __shared__ unsigned char smem_raw[];
+  T* s_m = reinterpret_cast<T*>(smem_raw);  // [P3][kTT + 1]
+  T* s_k = s_m + P3 * (kTT + 1);            // [8][P3]
+  __shared__ int s_src[kTT];
+  const Index t0 = static_cast<Index>(blockIdx.x) * kTT;
+  const int r = threadIdx.x >> 5;  // row within chunk
+  const int t = threadIdx.x & 31;  // target within tile
+  T acc[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) acc[c] = T(0);
+
+  for (int o = 0; o < kNOff; ++o) {
+    const int ox = o / 49 - 3, oy = (o / 7) % 7 - 3, oz = o % 7 - 3;
+    if (abs(ox) <= 1 && abs(oy) <= 1 && abs(oz) <= 1) continue;
+    __syncthreads();
+    if (threadIdx.x < kTT) {
+      const Index tt = t0 + threadIdx.x;
+      s_src[threadIdx.x] = tt < nt ? table[tt * kNOff + o] : -1;
+    }
+    __syncthreads();
+    const bool any = __syncthreads_or(threadIdx.x < kTT && s_src[threadIdx.x] >= 0);
+    if (!any) continue;
+    for (int e = threadIdx.x; e < P3 * kTT; e += blockDim.x) {
+      const int tt = e / P3, b = e % P3;
+      const int s = s_src[tt];
+      s_m[b * (kTT + 1) + tt] = s >= 0 ? Ms[static_cast<Index>(s) * P3 + b] : T(0);
+    }
+    const T* ko = K + static_cast<Index>(o) * P3 * P3;
+#pragma unroll 1
+    for (int c = 0; c < NC; ++c) {
+      __syncthreads();
+      for (int e = threadIdx.x; e < 8 * P3; e += blockDim.x) s_k[e] = ko[static_cast<Index>(c) * 8 * P3 + e];
+      __syncthreads();
+      T s = T(0);
+      const T* krow = s_k + r * P3;
+#pragma unroll 8
+      for (int b = 0; b < P3; ++b) s += krow[b] * s_m[b * (kTT + 1) + t];
+      // acc[c] with a runtime c: select through a switch-free unrolled update
+#pragma unroll
+      for (int cc = 0; cc < NC; ++cc)
+        if (cc == c) acc[cc] += s;
+    }
+  }
+  const Index tt = t0 + t;
+  if (tt < nt) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) L[tt * P3 + c * 8 + r] += acc[c];
+  }
+}
+
+template <int P, class T>
+__global__ void __launch_bounds__(128)
+    l2p_kernel(Cheb<T> ch, const P4<T>* __restrict__ tpos, const Index* __restrict__ perm,
+               const Index* __restrict__ leaf_start, const uint64_t* __restrict__ leaf_keys,
+               Box box, int lf, const T* __restrict__ L, double* __restrict__ out) {
+  constexpr int P3 = P * P * P;
+  __shared__ T s_l[P3];
+  const Index leaf = blockIdx.x;
+  for (int e = threadIdx.x; e < P3; e += blockDim.x) s_l[e] = L[leaf * P3 + e];
+  __syncthreads();
+  int cx, cy, cz;
+  unmorton(leaf_keys[leaf], cx, cy, cz);
+  const double wk = box.width / static_cast<double>(1 << lf);
+  const T ctr[3] = {static_cast<T>(box.min[0] + (cx + 0.5) * wk),
+                    static_cast<T>(box.min[1] + (cy + 0.5) * wk),
+                    static_cast<T>(box.min[2] + (cz + 0.5) * wk)};
+  const T inv_r = static_cast<T>(2.0 / wk);
+  const Index beg = leaf_start[leaf], end = leaf_start[leaf + 1];
+  for (Index i = beg + threadIdx.x; i < end; i += blockDim.x) {
+    P4<T> pt = tpos[i];
+    T sx[P], sy[P], sz[P];
+    cheb_basis<P>(ch, (pt.x - ctr[0]) * inv_r, sx);
+    cheb_basis<P>(ch, (pt.y - ctr[1]) * inv_r, sy);
+    cheb_basis<P>(ch, (pt.z - ctr[2]) * inv_r, sz);
+    T v = T(0);
+#pragma unroll
+    for (int ax = 0; ax < P; ++ax) {
+      T vy = T(0);
+#pragma unroll
+      for (int ay = 0; ay < P; ++ay) {
+        T vz = T(0);
+#pragma unroll
+        for (int az = 0; az < P; ++az) vz += s_l[(ax * P + ay) * P + az] * sz[az];
+        vy += vz * sy[ay];
+      }
+      v += vy * sx[ax];
+    }
+    out[perm[i]] += static_cast<double>(v);
+  }
+}
+
+// Near field: one block per target leaf, each thread one target, source tiles in shared memory.
+template <int KIND, class T>
+__global__ void __launch_bounds__(128)
+    p2p_kernel(KParams<T> kp, const P4<T>* __restrict__ tpos, const Index* __restrict__ tperm,
+               const Index* __restrict__ tleaf_start, const int* __restrict__ table,
+               const P4<T>* __restrict__ spos, const T* __restrict__ sw,
+               const Index* __restrict__ sleaf_start, double* __restrict__ out) {
+  __shared__ P4<T> s_p[128];
+  __shared__ int s_nb[27];
+  const Index leaf = blockIdx.x;
+  if (threadIdx.x < 27) s_nb[threadIdx.x] = table[leaf * 27 + threadIdx.x];
+  __syncthreads();
+  const Index tb = tleaf_start[leaf], te = tleaf_start[leaf + 1];
+  for (Index i0 = tb; i0 < te; i0 += blockDim.x) {
+    const Index i = i0 + threadIdx.x;
+    const bool active = i < te;
+    const P4<T> t = active ? tpos[i] : P4<T>{T(0), T(0), T(0), T(0)};
+    double tot = 0;
+    for (int nb = 0; nb < 27; ++nb) {
+      const int s = s_nb[nb];
+      if (s < 0) continue;
+      const Index sb = sleaf_start[s], se = sleaf_start[s + 1];
+      for (Index base = sb; base < se; base += 128) {
+        const int cnt = static_cast<int>(min(static_cast<Index>(128), se - base));
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+          P4<T> p = spos[base + threadIdx.x];
+          p.w = sw[base + threadIdx.x];
+          s_p[threadIdx.x] = p;
+        }
+        __syncthreads();
+        T acc = T(0);
+#pragma unroll 4
+        for (int j = 0; j < cnt; ++j) {
+          const P4<T> s4 = s_p[j];
+          const T dx = t.x - s4.x, dy = t.y - s4.y, dz = t.z - s4.z;
+          acc += rbf_value<KIND>(dx * dx + dy * dy + dz * dz, kp) * s4.w;
+        }
+        tot += static_cast<double>(acc);
+      }
+    }
+    if (active) out[tperm[i]] += tot;
+  }
+}
+
+template <class T>
+__global__ void count_pairs_kernel(const Index* __restrict__ tleaf_start, Index ntl,
+                                   const int* __restrict__ table,
+                                   const Index* __restrict__ sleaf_start,
+                                   unsigned long long* __restrict__ total) {
+  Index t = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= ntl) return;
+  unsigned long long nt = tleaf_start[t + 1] - tleaf_start[t];
+  unsigned long long ns = 0;
+  for (int j = 0; j < 27; ++j) {
+    int s = table[t * 27 + j];
+    if (s >= 0) ns += sleaf_start[s + 1] - sleaf_start[s];
+  }
+  atomicAdd(total, nt * ns);
+}
+
+// ---- host-side structures ------------------------------------------------------------------
+
+template <class T>
+struct Tree {
+  Index n = 0;
+  int lf = 0;
+  DevBuf<Index> perm;
+  DevBuf<P4<T>> pos;  // sorted
+  // per level k = 0..lf
+  std::vector<DevBuf<uint64_t>> keys;
+  std::vector<Index> ncell;
+  std::vector<DevBuf<Index>> start;   // level lf: point ranges (n_leaf + 1); k < lf: child ranges
+  std::vector<DevBuf<Index>> parent;  // level k: parent index (k >= 1)
+};
+
+template <class T>
+void build_tree(Tree<T>& tr, const P4<T>* pos, Index n, const Box& box, int lf) {
+  cudaStream_t st = stream();
+  tr.n = n;
+  tr.lf = lf;
+  tr.keys.clear();
+  tr.keys.resize(lf + 1);
+  tr.ncell.assign(lf + 1, 0);
+  tr.start.clear();
+  tr.start.resize(lf + 1);
+  tr.parent.clear();
+  tr.parent.resize(lf + 1);
+  tr.perm.resize(n);
+  tr.pos.resize(n);
+  if (n == 0) return;
+  DevBuf<uint64_t> k_in(n), k_out(n);
+  DevBuf<Index> i_in(n);
+  keys_kernel<T><<<blocks_for(n, 256), 256, 0, st>>>(pos, n, box, lf, k_in.data(), i_in.data());
+  PGPU_LAUNCH_CHECK();
+  size_t tmp_bytes = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, k_in.data(), k_out.data(), i_in.data(),
+                                  tr.perm.data(), n, 0, std::max(1, 3 * lf), st);
+  DevBuf<unsigned char> tmp(tmp_bytes);
+  PGPU_CUDA(cub::DeviceRadixSort::SortPairs(tmp.data(), tmp_bytes, k_in.data(), k_out.data(),
+                                            i_in.data(), tr.perm.data(), n, 0, std::max(1, 3 * lf),
+                                            st));
+  gather_pos_kernel<T><<<blocks_for(n, 256), 256, 0, st>>>(pos, tr.perm.data(), n, tr.pos.data());
+  PGPU_LAUNCH_CHECK();
+
+  // Run-length encode level by level: level lf from the sorted point keys, then parents.
+  DevBuf<Index> flags(n), scan(n);
+  const uint64_t* src_keys = k_out.data();
+  Index src_n = n;
+  for (int k = lf; k >= 0; --k) {
+    const int shift = (k == lf) ? 0 : 3;
+    rle_flags_kernel<<<blocks_for(src_n, 256), 256, 0, st>>>(src_keys, src_n, shift, flags.data());
+    PGPU_LAUNCH_CHECK();
+    size_t sb = 0;
+    cub::DeviceScan::InclusiveSum(nullptr, sb, flags.data(), scan.data(), src_n, st);
+    DevBuf<unsigned char> stmp(sb);
+    PGPU_CUDA(cub::DeviceScan::InclusiveSum(stmp.data(), sb, flags.data(), scan.data(), src_n, st));
+    Index nu = 0;
+    PGPU_CUDA(cudaMemcpyAsync(&nu, scan.data() + src_n - 1, sizeof(Index), cudaMemcpyDeviceToHost, st));
+    sync();
+    tr.ncell[k] = nu;
+    tr.keys[k].resize(nu);
+    tr.start[k].resize(nu + 1);
+    if (k < lf) tr.parent[k + 1].resize(src_n);
+    rle_scatter_kernel<<<blocks_for(src_n, 256), 256, 0, st>>>(
+        src_keys, src_n, shift, scan.data(), tr.keys[k].data(), tr.start[k].data(),
+        k < lf ? tr.parent[k + 1].data() : nullptr);
+    PGPU_LAUNCH_CHECK();
+    PGPU_CUDA(cudaMemcpyAsync(tr.start[k].data() + nu, &src_n, sizeof(Index), cudaMemcpyHostToDevice, st));
+    sync();
+    src_keys = tr.keys[k].data();
+    src_n = nu;
+  }
+}
+
+// Process-wide cache of M2L operator matrices keyed by (kind, params, cell radius, order, type).
+struct KKey {
+  int kind;
+  double p0, p1, r;
+  int p;
+  int tsize;
+  bool operator<(const KKey& o) const {
+    return std::tie(kind, p0, p1, r, p, tsize) < std::tie(o.kind, o.p0, o.p1, o.r, o.p, o.tsize);
+  }
+};
+
+std::mutex g_kcache_mu;
+std::map<KKey, std::shared_ptr<void>> g_kcache;
+
+template <class T>
+std::shared_ptr<DevBuf<T>> m2l_matrices(int kind, const KParams<T>& kp, double r, int p) {
+  KKey key{kind, static_cast<double>(kp.p0), static_cast<double>(kp.p1), r, p,
+           static_cast<int>(sizeof(T))};
+  {
+    std::lock_guard<std::mutex> lk(g_kcache_mu);
+    auto it = g_kcache.find(key);
+    if (it != g_kcache.end()) return std::static_pointer_cast<DevBuf<T>>(it->second);
+  }
+  const Index p3 = static_cast<Index>(p) * p * p;
+  auto buf = std::make_shared<DevBuf<T>>(static_cast<size_t>(kNOff) * p3 * p3);
+  std::vector<double> nodes(p);
+  for (int m = 0; m < p; ++m) nodes[m] = cheb_node(p, m);
+  DevBuf<double> dn;
+  dn.upload(nodes);
+  dispatch_kind(kind, [&]<int K>() {
+    m2l_matrix_kernel<K, T><<<4 * num_sms(), 256, 0, stream()>>>(kp, p, r, dn.data(), buf->data());
+    return 0;
+  });
+  PGPU_LAUNCH_CHECK();
+  sync();
+  std::lock_guard<std::mutex> lk(g_kcache_mu);
+  g_kcache[key] = buf;
+  return buf;
+}
+
+int order_for_accuracy(double accuracy) {
+  // accuracy = inf: the reference's default order 6 (fmm_accuracy_estimator.hpp:77-79);
+  // accuracy = 0 (the fit operator): the highest order kept here.
+  if (std::isinf(accuracy)) return 6;
+  if (accuracy <= 0.0) return 8;
+  if (accuracy >= 1e-4) return 6;
+  return 8;
+}
+
+}  // namespace
+
+template <class T>
+struct Fmm<T>::Impl {
+  int kind;
+  KParams<T> kp;
+  Mat3 a;
+  Box box;
+  double accuracy;
+  FarFieldConfig cfg;
+  bool cfg_set = false;
+  int p = 6;
+  Tree<T> src, trg;
+  bool symmetric = false;
+  const P4<T>* spos_in = nullptr;
+  const P4<T>* tpos_in = nullptr;
+  Index ns = 0, nt = 0;
+  int lf = 2;
+  bool built = false;
+  // M2L tables per level (target cells x 343) and P2P table (target leaves x 27).
+  std::vector<DevBuf<int>> m2l_table;
+  DevBuf<int> p2p_table;
+  std::vector<std::shared_ptr<DevBuf<T>>> kmats;
+  std::vector<DevBuf<T>> M, L;
+  DevBuf<T> sw;
+  Index near_pairs = 0;
+  Cheb<T> ch;
+
+  Tree<T>& ttree() { return symmetric ? src : trg; }
+
+  int choose_leaf_level() const {
+    if (cfg_set && cfg.leaf_level >= 0) return cfg.leaf_level;
+    // Sources per leaf around 64 (FP32) / 32 (FP64) for uniform data; at least two levels of
+    // far field.
+    const double per_leaf = sizeof(T) == 4 ? 64.0 : 32.0;
+    const Index n = std::max(ns, std::min(nt, ns * 4));
+    int lf = static_cast<int>(std::lround(std::log(std::max(1.0, n / per_leaf)) / std::log(8.0)));
+    return std::min(std::max(lf, 2), 10);
+  }
+
+  void build() {
+    lf = choose_leaf_level();
+    p = cfg_set && cfg.order > 0 ? cfg.order : order_for_accuracy(accuracy);
+    if (p != 4 && p != 6 && p != 8) p = 6;
+    ch = make_cheb<T>(p);
+    build_tree(src, spos_in, ns, box, lf);
+    if (!symmetric) build_tree(trg, tpos_in, nt, box, lf);
+    Tree<T>& tt = ttree();
+    cudaStream_t st = stream();
+    // Interaction tables.
+    m2l_table.clear();
+    m2l_table.resize(lf + 1);
+    kmats.assign(lf + 1, nullptr);
+    for (int k = 2; k <= lf; ++k) {
+      const Index n_t = tt.ncell[k];
+      m2l_table[k].resize(std::max<Index>(n_t, 1) * kNOff);
+      PGPU_CUDA(cudaMemsetAsync(m2l_table[k].data(), 0xff, m2l_table[k].size() * sizeof(int), st));
+      DevBuf<Index> cnt(std::max<Index>(n_t, 1));
+      if (n_t > 0) {
+        m2l_table_kernel<<<blocks_for(n_t, 128), 128, 0, st>>>(tt.keys[k].data(), n_t,
+                                                               src.keys[k].data(), src.ncell[k], k,
+                                                               m2l_table[k].data(), cnt.data());
+        PGPU_LAUNCH_CHECK();
+      }
+      const double r = box.width / static_cast<double>(1 << k) / 2.0;
+      kmats[k] = m2l_matrices<T>(kind, kp, r, p);
+    }
+    const Index ntl = tt.ncell[lf];
+    p2p_table.resize(std::max<Index>(ntl, 1) * 27);
+    if (ntl > 0) {
+      p2p_table_kernel<<<blocks_for(ntl, 128), 128, 0, st>>>(tt.keys[lf].data(), ntl,
+                                                             src.keys[lf].data(), src.ncell[lf], lf,
+                                                             p2p_table.data());
+      PGPU_LAUNCH_CHECK();
+      DevBuf<unsigned long long> tot(1);
+      PGPU_CUDA(cudaMemsetAsync(tot.data(), 0, sizeof(unsigned long long), st));
+      count_pairs_kernel<T><<<blocks_for(ntl, 128), 128, 0, st>>>(
+          tt.start[lf].data(), ntl, p2p_table.data(), src.start[lf].data(), tot.data());
+      PGPU_LAUNCH_CHECK();
+      unsigned long long h = 0;
+      PGPU_CUDA(cudaMemcpyAsync(&h, tot.data(), sizeof(h), cudaMemcpyDeviceToHost, st));
+      sync();
+      near_pairs = static_cast<Index>(h);
+    }
+    const Index p3 = static_cast<Index>(p) * p * p;
+    M.clear();
+    L.clear();
+    M.resize(lf + 1);
+    L.resize(lf + 1);
+    for (int k = 2; k <= lf; ++k) {
+      M[k].resize(std::max<Index>(src.ncell[k], 1) * p3);
+      L[k].resize(std::max<Index>(tt.ncell[k], 1) * p3);
+    }
+    sw.resize(std::max<Index>(ns, 1));
+    built = true;
+  }
+
+  template <int P>
+  void run_far(cudaStream_t st, double* out) {
+    constexpr int P3 = P * P * P;
+    Tree<T>& tt = ttree();
+    // Upward pass.
+    if (src.ncell[lf] > 0) {
+      p2m_kernel<P, T><<<static_cast<unsigned>(src.ncell[lf]), 256, 0, st>>>(
+          ch, src.pos.data(), sw.data(), src.start[lf].data(), src.keys[lf].data(), box, lf,
+          M[lf].data());
+      PGPU_LAUNCH_CHECK();
+    }
+    for (int k = lf - 1; k >= 2; --k) {
+      if (src.ncell[k] == 0) continue;
+      m2m_kernel<P, T><<<static_cast<unsigned>(src.ncell[k]), ((P3 + 31) / 32) * 32, 0, st>>>(
+          ch, src.start[k].data(), src.keys[k + 1].data(), M[k + 1].data(), M[k].data());
+      PGPU_LAUNCH_CHECK();
+    }
+    // Transfer + downward pass.
+    const size_t smem = (static_cast<size_t>(P3) * (kTT + 1) + 8 * P3) * sizeof(T);
+    for (int k = 2; k <= lf; ++k) {
+      const Index n_t = tt.ncell[k];
+      if (n_t == 0) continue;
+      PGPU_CUDA(cudaMemsetAsync(L[k].data(), 0, n_t * P3 * sizeof(T), st));
+      if (k > 2) {
+        l2l_kernel<P, T><<<static_cast<unsigned>(n_t), ((P3 + 31) / 32) * 32, 0, st>>>(
+            ch, tt.parent[k].data(), tt.keys[k].data(), L[k - 1].data(), L[k].data());
+        PGPU_LAUNCH_CHECK();
+      }
+      if (src.ncell[k] > 0) {
+        auto kern = m2l_kernel<P, T>;
+        PGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem)));
+        kern<<<static_cast<unsigned>((n_t + kTT - 1) / kTT), 256, smem, st>>>(
+            kmats[k]->data(), m2l_table[k].data(), n_t, M[k].data(), L[k].data());
+        PGPU_LAUNCH_CHECK();
+      }
+    }
+    if (tt.ncell[lf] > 0) {
+      l2p_kernel<P, T><<<static_cast<unsigned>(tt.ncell[lf]), 128, 0, st>>>(
+          ch, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), tt.keys[lf].data(), box, lf,
+          L[lf].data(), out);
+      PGPU_LAUNCH_CHECK();
+    }
+  }
+
+  void evaluate(const T* vw, double* out) {
+    if (!built) build();
+    cudaStream_t st = stream();
+    Tree<T>& tt = ttree();
+    if (ns == 0 || (symmetric ? ns : nt) == 0) return;
+    gather_w_kernel<T><<<blocks_for(ns, 256), 256, 0, st>>>(vw, src.perm.data(), ns, sw.data());
+    PGPU_LAUNCH_CHECK();
+    if (lf >= 2) {
+      switch (p) {
+        case 4: run_far<4>(st, out); break;
+        case 8: run_far<8>(st, out); break;
+        default: run_far<6>(st, out); break;
+      }
+    }
+    const Index ntl = tt.ncell[lf];
+    if (ntl > 0) {
+      dispatch_kind(kind, [&]<int K>() {
+        p2p_kernel<K, T><<<static_cast<unsigned>(ntl), 128, 0, st>>>(
+            kp, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), p2p_table.data(),
+            src.pos.data(), sw.data(), src.start[lf].data(), out);
+        return 0;
+      });
+      PGPU_LAUNCH_CHECK();
+    }
+  }
+};
+
+template <class T>
+bool Fmm<T>::supported(int kind) {
+  // Compactly supported and piecewise kernels are not smooth enough for interpolation; the
+  // reference splits the spheroidal family (src/fmm/spheroidal_evaluator.hpp); those stay on the
+  // exact direct backend here.
+  switch (kind) {
+    case PGPU_RBF_CUB:
+    case PGPU_RBF_SPH:
+    case PGPU_RBF_SP3:
+    case PGPU_RBF_SP5:
+    case PGPU_RBF_SP7:
+    case PGPU_RBF_SP9:
+      return false;
+    default:
+      return true;
+  }
+}
+
+template <class T>
+Fmm<T>::Fmm(int kind, const KParams<T>& kp, const Mat3& a, const double box_min[3],
+            double box_width, double accuracy)
+    : impl_(new Impl) {
+  impl_->kind = kind;
+  impl_->kp = kp;
+  impl_->a = a;
+  for (int k = 0; k < 3; ++k) impl_->box.min[k] = box_min[k];
+  impl_->box.width = box_width;
+  impl_->accuracy = accuracy;
+}
+
+template <class T>
+Fmm<T>::~Fmm() {
+  delete impl_;
+}
+
+template <class T>
+void Fmm<T>::set_config(const FarFieldConfig& c) {
+  impl_->cfg = c;
+  impl_->cfg_set = true;
+  impl_->built = false;
+}
+
+template <class T>
+void Fmm<T>::set_points(const P4<T>* pos, Index n, const P4<T>*, Index) {
+  impl_->symmetric = true;
+  impl_->spos_in = impl_->tpos_in = pos;
+  impl_->ns = impl_->nt = n;
+  impl_->built = false;
+}
+
+template <class T>
+void Fmm<T>::set_sources(const P4<T>* pos, Index n, const P4<T>*, Index) {
+  impl_->symmetric = false;
+  impl_->spos_in = pos;
+  impl_->ns = n;
+  impl_->built = false;
+}
+
+template <class T>
+void Fmm<T>::set_targets(const P4<T>* pos, Index n, const P4<T>*, Index) {
+  impl_->symmetric = false;
+  impl_->tpos_in = pos;
+  impl_->nt = n;
+  impl_->built = false;
+}
+
+template <class T>
+void Fmm<T>::evaluate(const T* vw, const T*, double* out_v, double*) {
+  impl_->evaluate(vw, out_v);
+}
+
+template <class T>
+Index Fmm<T>::near_pairs() const {
+  return impl_->near_pairs;
+}
 
 template class Fmm<double>;
 template class Fmm<float>;

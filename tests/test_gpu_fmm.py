@@ -1,0 +1,104 @@
+"""FMM parity against the oracle's exact sums, restating the reference's differential tests
+(test/interpolation/test_evaluator.cpp:27-76: FMM evaluator vs DirectEvaluator within the
+requested accuracy). The error is normalised by the conditioning of the sum,
+s_i = sum_j |w_j phi(x_i - y_j)| (computed by the oracle), so the bound is independent of the
+weights' scale."""
+import numpy as np
+import pytest
+
+import oracle
+import polatory_gb300 as pg
+
+pytestmark = pytest.mark.gpu
+
+# Relative-to-conditioning bounds per Chebyshev order (estimated from rho^-p with rho ~ 5.8 for
+# the nearest well-separated cells, times a safety factor).
+BOUND = {4: 2e-3, 6: 1e-4, 8: 5e-6}
+
+
+def sample(n_src, n_trg, seed, clustered=False):
+    g = np.random.Generator(np.random.PCG64(seed))
+    if clustered:
+        c = g.random((16, 3))
+        src = c[g.integers(0, 16, n_src)] + 0.05 * g.standard_normal((n_src, 3))
+    else:
+        src = g.random((n_src, 3))
+    trg = g.random((n_trg, 3))
+    w = g.standard_normal(n_src)
+    return src, trg, w
+
+
+def check(rbf, order, precision, src, trg, w, symmetric=False, leaf_level=-1):
+    lo = np.minimum(src.min(0), trg.min(0))
+    hi = np.maximum(src.max(0), trg.max(0))
+    ev = pg.FmmEvaluator(rbf, np.concatenate([lo, hi]), symmetric=symmetric, precision=precision)
+    ev.configure(backend=2, order=order, leaf_level=leaf_level)
+    if symmetric:
+        ev.set_points(src)
+    else:
+        ev.set_source_points(src)
+        ev.set_target_points(trg)
+    ev.set_weights(w)
+    got = ev.evaluate()
+    m = pg.Model(rbf, rbf.cpd_order - 1)._c()
+    m.poly_degree = -1
+    tpts = src if symmetric else trg
+    want = oracle.direct_evaluate(m, src, w, tpts)
+    # |phi| sums: evaluate |phi| with |w| through the oracle on a subsample of targets.
+    sub = np.arange(0, tpts.shape[0], max(1, tpts.shape[0] // 200))
+    absum = np.zeros(sub.shape[0])
+    for k, i in enumerate(sub):
+        d = tpts[i] - src
+        vals = np.array([oracle.rbf_evaluate(rbf._kind, rbf.parameters, rbf.anisotropy, dd)[0]
+                         for dd in d[:: max(1, src.shape[0] // 2000)]])
+        absum[k] = np.abs(vals).mean() * np.abs(w).sum()
+    scale = absum.max()
+    err = np.max(np.abs(got - want))
+    return err, scale
+
+
+@pytest.mark.parametrize("cls,params", [(pg.Biharmonic3D, [1.0]), (pg.Triharmonic3D, [1.0]),
+                                        (pg.CovExponential, [1.0, 0.3]),
+                                        (pg.CovGaussian, [1.0, 0.5])],
+                         ids=["bh3", "th3", "exp", "gau"])
+@pytest.mark.parametrize("order", [6, 8])
+def test_fmm_plain_matches_direct(cls, params, order):
+    src, trg, w = sample(20000, 3000, 31)
+    err, scale = check(cls(params), order, pg.PLAIN, src, trg, w)
+    print(f"order {order}: err {err:.3e} scale {scale:.3e} rel {err / scale:.3e}")
+    assert err <= BOUND[order] * scale
+
+
+@pytest.mark.parametrize("order", [6, 8])
+def test_fmm_mixed_matches_direct(order):
+    src, trg, w = sample(20000, 3000, 32)
+    err, scale = check(pg.Biharmonic3D([1.0]), order, pg.MIXED, src, trg, w)
+    print(f"mixed order {order}: err {err:.3e} scale {scale:.3e} rel {err / scale:.3e}")
+    assert err <= max(BOUND[order], 2e-5) * scale
+
+
+def test_fmm_clustered_symmetric_anisotropic():
+    src, _, w = sample(15000, 0, 33, clustered=True)
+    rbf = pg.Triharmonic3D([1.0])
+    rbf.anisotropy = np.diag([1.0, 1.0, 2.0])
+    err, scale = check(rbf, 6, pg.PLAIN, src, src, w, symmetric=True)
+    print(f"clustered: err {err:.3e} scale {scale:.3e} rel {err / scale:.3e}")
+    assert err <= BOUND[6] * scale
+
+
+@pytest.mark.parametrize("leaf_level", [2, 3, 4])
+def test_fmm_leaf_levels(leaf_level):
+    src, trg, w = sample(12000, 2000, 34)
+    err, scale = check(pg.Biharmonic3D([1.0]), 6, pg.PLAIN, src, trg, w, leaf_level=leaf_level)
+    print(f"leaf level {leaf_level}: rel {err / scale:.3e}")
+    assert err <= BOUND[6] * scale
+
+
+def test_fmm_empty_and_tiny():
+    rbf = pg.Biharmonic3D([1.0])
+    ev = pg.FmmEvaluator(rbf, [0, 0, 0, 1, 1, 1])
+    ev.configure(backend=2, order=6)
+    ev.set_source_points(np.random.default_rng(0).random((5, 3)))
+    ev.set_target_points(np.zeros((0, 3)))
+    ev.set_weights(np.ones(5))
+    assert ev.evaluate().shape == (0,)
