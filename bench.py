@@ -1,0 +1,304 @@
+"""Benchmark: RBF fit + evaluate throughput, mixed precision vs plain FP64, on one GB300.
+
+Workload (default): the surface-style fit — 1M points on the ellipsoid (1, 0.7, 0.5) plus 2M
+points offset by +/-0.01 along the normals (SDF values 0, +/-0.01), biharmonic3d with a degree-1
+polynomial, absolute tolerance 1e-4, evaluated at 2M uniform points in the bounding box. One step
+is one fit of the 3M points followed by the evaluation at the 2M query points. Inputs are seeded
+synthetic data (numpy PCG64); no dataset is involved.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--scale S]
+
+With --gpus N > 1 (torchrun, one rank per GPU) every rank fits its own replica of the workload
+(replicas only: the path has no cross-GPU exchange) and value is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "fit+eval points/s (mixed precision, 1e-4 abs err vs plain FP64)"
+UNIT = "points/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--scale", type=float, default=1.0, help="fraction of the default sizes")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    return ap.parse_args()
+
+
+def workload(scale: float):
+    from polatory_gb300 import workloads
+
+    ns = max(1000, int(1_000_000 * scale))
+    pts, vals, q = workloads.c2(n_surface=ns, n_eval=max(1000, int(2_000_000 * scale)))
+    cfg = {
+        "workload": f"surface SDF fit: {pts.shape[0]} points (ellipsoid 1/0.7/0.5, +/-0.01 "
+                    f"offsets), biharmonic3d degree 1, tol 1e-4, {q.shape[0]} uniform queries",
+        "n_fit": int(pts.shape[0]), "n_eval": int(q.shape[0]), "rbf": "bh3 (-r)",
+        "poly_degree": 1, "tolerance": 1e-4, "precision": "mixed (FP32 near/far field, "
+        "FP64 Krylov + residual)",
+        "l2_policy": "inputs and working set larger than L2 (no flush needed)",
+    }
+    return pts, vals, q, cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.device),
+                                      f"--query-gpu={self.Q}", "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for k, name in enumerate(names):
+                if len(s) > 5 + k and s[5 + k].strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.samples)}
+
+
+def cpu_baseline(pts, vals, q, budget_n_fit=3000, n_eval=2000):
+    """The oracle (FP64 C restatement: exact dense fit + direct sums) on the host cores, on a
+    bounded subsample of the same workload."""
+    import oracle
+    import polatory_gb300 as pg
+
+    g = np.random.Generator(np.random.PCG64(77))
+    idx = np.sort(g.choice(pts.shape[0], size=min(budget_n_fit, pts.shape[0]), replace=False))
+    sp, sv = pts[idx], vals[idx]
+    sq = q[g.choice(q.shape[0], size=min(n_eval, q.shape[0]), replace=False)]
+    model = pg.Model(pg.Biharmonic3D([1.0]), 1)
+    t0 = time.perf_counter()
+    w = oracle.fit_exact(model, sp, sv)
+    oracle.direct_evaluate(model, sp, w, sq)
+    dt = time.perf_counter() - t0
+    return {"value": (sp.shape[0] + sq.shape[0]) / dt, "unit": UNIT, "cores": oracle.num_threads(),
+            "kind": "port",
+            "sample": f"exact dense FP64 fit of {sp.shape[0]} sampled data points + direct "
+                      f"evaluation at {sq.shape[0]} sampled queries ({dt:.2f} s)"}
+
+
+def dist_setup(args):
+    if args.gpus <= 1 or "RANK" not in os.environ:
+        return 0, 1, 0, None
+    import torch.distributed as dist
+
+    rank = int(os.environ["RANK"])
+    world = int(os.environ["WORLD_SIZE"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    import torch
+
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return rank, world, local, dist
+
+
+def run_reference(args):
+    """The reference arm: the reference's CPU path as restated by the oracle (the reference
+    itself cannot be built here), timed on the host cores on a bounded sample per step."""
+    rank, world, local, dist = dist_setup(args)
+    if rank != 0:
+        return
+    pts, vals, q, cfg = workload(args.scale)
+    for _ in range(args.warmup):
+        cpu_baseline(pts, vals, q, budget_n_fit=1000, n_eval=500)
+    vals_s = []
+    base = None
+    for _ in range(args.steps):
+        base = cpu_baseline(pts, vals, q)
+        vals_s.append(base["value"])
+    v = float(np.mean(vals_s))
+    base["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": cfg, "cpu_baseline": base,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference not buildable here (Eigen/ScalFMM3 absent); oracle FP64 port timed"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    rank, world, local, dist = dist_setup(args)
+    import polatory_gb300 as pg
+
+    pg._lib.check(pg._lib.lib.pgpu_set_device(local))
+    torch.cuda.set_device(local)
+    pts, vals, q, cfg = workload(args.scale)
+    n_units = pts.shape[0] + q.shape[0]
+    dev = torch.device("cuda", local)
+    pts_d = torch.from_numpy(pts).to(dev)
+    vals_d = torch.from_numpy(vals).to(dev)
+    q_d = torch.from_numpy(q).to(dev)
+    out_d = torch.empty(q.shape[0], dtype=torch.float64, device=dev)
+    model = pg.Model(pg.Biharmonic3D([1.0]), 1)
+    stream = torch.cuda.ExternalStream(pg.stream_handle(), device=dev)
+
+    def step(interp):
+        interp.fit_device(pts_d, vals_d, 1e-4)
+        interp.evaluate_device(q_d, out_d)
+
+    interp = pg.Interpolant(model, pg.MIXED)
+    for _ in range(args.warmup):
+        step(interp)
+    pg.synchronize()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    pg.profile_reset()
+    pg.profile_enable(True)
+    launches0 = pg.launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    iters = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step(interp)
+            iters.append(interp.fit_stats["iterations"])
+        ev1.record(stream)
+        pg.synchronize()
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    launches = pg.launch_count() - launches0
+    report = pg.profile_report()
+    pg.profile_enable(False)
+    t_max = ms
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+        dist.barrier()
+    value = world * n_units * args.steps / (t_max * 1e-3)
+    mixed_out = out_d.cpu().numpy()
+    stats = interp.fit_stats
+
+    # End to end through the C ABI with host buffers (copies inside the timed region).
+    e2e_interp = pg.Interpolant(model, pg.MIXED)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(max(1, min(args.steps, 2))):
+        e2e_interp.fit(pts, vals, 1e-4)
+        host_out = e2e_interp.evaluate(q)
+    e2e_s = (time.perf_counter() - t0) / max(1, min(args.steps, 2))
+    e2e = {"value": world * n_units / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(pts.nbytes + vals.nbytes + q.nbytes),
+           "d2h_bytes_per_step": int(host_out.nbytes)}
+
+    plain = None
+    if not args.no_plain:
+        pi = pg.Interpolant(model, pg.PLAIN)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step(pi)
+        pg.synchronize()
+        dt = time.perf_counter() - t0
+        plain_out = out_d.cpu().numpy()
+        err = float(np.max(np.abs(mixed_out - plain_out)))
+        plain = {"value": n_units / dt, "unit": UNIT, "seconds": dt,
+                 "iterations": pi.fit_stats["iterations"],
+                 "mixed_vs_plain_max_abs_err": err, "speedup_mixed_over_plain": value / world / (n_units / dt)}
+
+    if rank != 0:
+        return
+    # Roofline of the dominant kernel (device time per region from the live CUDA events).
+    dom_name, dom = max(report.items(), key=lambda kv: kv[1]["ms"])
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    clk_max = peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = sms * 128 * 2 * clk_max * 1e6 / 1e12  # TFLOP/s, CUDA-core FP32 FMA
+    fp64_peak = sms * 2 * 2 * clk_max * 1e6 / 1e12
+    if dom["bytes"] > 0 and dom["flops"] / max(dom["bytes"], 1) < 4:
+        achieved = dom["bytes"] / (dom["ms"] * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs", 6800.0),
+                "unit": "GB/s", "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    else:
+        achieved = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
+        f32 = dom_name.endswith("f32")
+        roof = {"bound": "fp32-cuda-core" if f32 else "fp64-cuda-core", "achieved": achieved,
+                "peak": fp32_peak if f32 else fp64_peak, "unit": "TFLOP/s",
+                "peak_source": f"nominal {'FP32' if f32 else 'FP64'} CUDA-core FMA rate: {sms} SMs x "
+                               f"{128 if f32 else 2} x 2 flops x {clk_max:.0f} MHz"}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["kernel"] = dom_name
+    roof["traffic"] = None
+    roof["launches"] = dom["calls"]
+    roof["ms_total"] = dom["ms"]
+    roof["share_of_step"] = dom["ms"] / ms
+    cpu = None if args.no_cpu else cpu_baseline(pts, vals, q)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": cfg, "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
+        "cpu_baseline": cpu, "clocks": clk.summary(), "plain_fp64": plain,
+        "fit": {"iterations": iters, "levels": stats["levels"], "residual": stats["residual"],
+                "setup_s": stats["setup_seconds"], "solve_s": stats["solve_seconds"],
+                "n_domains": stats["n_domains"]},
+        "profile_ms": {k: round(v["ms"], 3) for k, v in sorted(report.items(), key=lambda kv: -kv[1]["ms"])},
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -101,6 +101,17 @@ int pgpu_version(void);
 int pgpu_set_device(int device);
 /* Releases cached device memory held by the library's pool. */
 int pgpu_release_cached_memory(void);
+/* Phase profiler (no reference counterpart): CUDA events around every instrumented region of
+ * the library stream. report writes a JSON object {region: {calls, ms, flops, bytes}} into buf
+ * (truncated to size) and synchronizes the stream. launch_count counts kernel launches. */
+int pgpu_profile_enable(int on);
+int pgpu_profile_reset(void);
+int pgpu_profile_report(char* buf, int64_t size);
+int pgpu_launch_count(int64_t* out);
+/* Synchronizes the library stream of this thread. */
+int pgpu_synchronize(void);
+/* The library's CUDA stream of this thread (a cudaStream_t), for event timing by callers. */
+int pgpu_stream(void** out);
 
 /* ---- RBF pointwise evaluation (rbf/rbf_base.hpp:40-53) -------------------------------- */
 /* Evaluates the anisotropic kernel at n difference vectors (host buffers). Any of values

@@ -236,6 +236,19 @@ class Interpolant:
             float(accuracy), float(grad_accuracy), ptr(out)))
         return out
 
+    def fit_device(self, points, values, tolerance, max_iter=100, accuracy=INF):
+        """fit() with device-resident inputs (torch CUDA float64 tensors, (n, 3) and (n,))."""
+        n = int(points.shape[0])
+        check(lib.pgpu_interpolant_fit(self._h, ptr(points), n, None, 0, ptr(values),
+                                       float(tolerance), INF, int(max_iter), float(accuracy), INF,
+                                       None))
+
+    def evaluate_device(self, points, out, accuracy=INF):
+        """evaluate() from device-resident points into a device-resident output tensor."""
+        m = int(points.shape[0])
+        check(lib.pgpu_interpolant_evaluate(self._h, ptr(points), m, None, 0, float(accuracy),
+                                            INF, ptr(out)))
+
     def evaluate_impl(self, points, grad_points=None):
         pts = as_points(points)
         gpts = as_points(np.zeros((0, 3)) if grad_points is None else grad_points)
@@ -272,6 +285,39 @@ class Interpolant:
         s = _lib.PgpuFitStats()
         check(lib.pgpu_interpolant_fit_stats(self._h, C.byref(s)))
         return {k: getattr(s, k) for k, _ in s._fields_}
+
+
+def profile_enable(on: bool = True) -> None:
+    check(lib.pgpu_profile_enable(int(on)))
+
+
+def profile_reset() -> None:
+    check(lib.pgpu_profile_reset())
+
+
+def profile_report() -> dict:
+    import json
+
+    buf = C.create_string_buffer(1 << 16)
+    check(lib.pgpu_profile_report(buf, len(buf)))
+    return json.loads(buf.value.decode())
+
+
+def launch_count() -> int:
+    out = C.c_int64()
+    check(lib.pgpu_launch_count(C.byref(out)))
+    return out.value
+
+
+def synchronize() -> None:
+    check(lib.pgpu_synchronize())
+
+
+def stream_handle() -> int:
+    """The library's cudaStream_t of this thread, as an integer handle."""
+    out = C.c_void_p()
+    check(lib.pgpu_stream(C.byref(out)))
+    return int(out.value or 0)
 
 
 class FmmEvaluator:

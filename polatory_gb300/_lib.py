@@ -69,6 +69,12 @@ def _load():
         "pgpu_version": ([], C.c_int),
         "pgpu_set_device": ([C.c_int], C.c_int),
         "pgpu_release_cached_memory": ([], C.c_int),
+        "pgpu_profile_enable": ([C.c_int], C.c_int),
+        "pgpu_profile_reset": ([], C.c_int),
+        "pgpu_profile_report": ([C.c_char_p, I64], C.c_int),
+        "pgpu_launch_count": ([C.POINTER(I64)], C.c_int),
+        "pgpu_synchronize": ([], C.c_int),
+        "pgpu_stream": ([C.POINTER(C.c_void_p)], C.c_int),
         "pgpu_rbf_evaluate": ([C.POINTER(PgpuRbf), P, I64, P, P, P], C.c_int),
         "pgpu_rbf_cpd_order": ([C.POINTER(PgpuRbf), C.POINTER(C.c_int)], C.c_int),
         "pgpu_rbf_support_radius_isotropic": ([C.POINTER(PgpuRbf), D], C.c_int),

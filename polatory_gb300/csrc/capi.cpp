@@ -8,6 +8,7 @@
 #include "common.hpp"
 #include "evaluator.hpp"
 #include "model.hpp"
+#include "profile.hpp"
 #include "rbf.cuh"
 #include "solver.hpp"
 
@@ -92,6 +93,43 @@ int pgpu_set_device(int device) {
 
 int pgpu_release_cached_memory(void) {
   return guarded([&] { release_cached_memory(); });
+}
+
+int pgpu_profile_enable(int on) {
+  return guarded([&] { profile_enable(on != 0); });
+}
+
+int pgpu_profile_reset(void) {
+  return guarded([&] { profile_reset(); });
+}
+
+int pgpu_profile_report(char* buf, int64_t size) {
+  return guarded([&] {
+    check_ptr(buf, "buf");
+    if (size <= 0) throw_invalid("size must be positive");
+    std::string r = profile_report();
+    size_t n = std::min<size_t>(r.size(), static_cast<size_t>(size - 1));
+    std::memcpy(buf, r.data(), n);
+    buf[n] = '\0';
+  });
+}
+
+int pgpu_launch_count(int64_t* out) {
+  return guarded([&] {
+    check_ptr(out, "out");
+    *out = launch_count();
+  });
+}
+
+int pgpu_synchronize(void) {
+  return guarded([&] { pgpu::sync(); });
+}
+
+int pgpu_stream(void** out) {
+  return guarded([&] {
+    check_ptr(out, "out");
+    *out = reinterpret_cast<void*>(stream());
+  });
 }
 
 int pgpu_rbf_evaluate(const pgpu_rbf* rbf, const double* diffs, int64_t n, double* values,
@@ -515,15 +553,12 @@ int pgpu_interpolant_evaluate(pgpu_interpolant* it, const double* points, int64_
     throw_if_not_fitted(it);
     if (!(accuracy > 0.0)) throw_invalid("accuracy must be positive");
     if (!(grad_accuracy > 0.0)) throw_invalid("grad_accuracy must be positive");
-    Bbox3 b;
-    if (m > 0) {
-      auto hp = host_copy(points, 3 * m);
-      b = Bbox3::from_host_points(hp.data(), m);
-    }
-    if (mg > 0) {
-      auto hg = host_copy(grad_points, 3 * mg);
-      b = b.hull(Bbox3::from_host_points(hg.data(), mg));
-    }
+    auto bbox_of = [](const double* p, int64_t n) {
+      if (n == 0) return Bbox3{};
+      if (is_device_pointer(p)) return bbox_of_device_points(p, n);
+      return Bbox3::from_host_points(p, n);
+    };
+    Bbox3 b = bbox_of(points, m).hull(bbox_of(grad_points, mg));
     it->eval_bbox = b.hull(it->bbox);
     it->eval_accuracy = accuracy;
     it->eval_grad_accuracy = grad_accuracy;

@@ -40,7 +40,11 @@ struct Error : std::runtime_error {
     }                                                                                      \
   } while (0)
 
-#define PGPU_LAUNCH_CHECK() PGPU_CUDA(cudaGetLastError())
+#define PGPU_LAUNCH_CHECK()      \
+  do {                           \
+    ::pgpu::count_launch();      \
+    PGPU_CUDA(cudaGetLastError()); \
+  } while (0)
 
 // Library stream (one per host thread; the reference's evaluators are single-thread-affine).
 cudaStream_t stream();
@@ -128,5 +132,12 @@ int num_sms();
 
 // Monotonic host clock in seconds.
 double wall_seconds();
+
+// PGPU_VERBOSE set in the environment: progress and phase timings on stdout.
+bool verbose();
+
+// Counts kernel launches (every launch site is followed by PGPU_LAUNCH_CHECK).
+void count_launch();
+int64_t launch_count();
 
 }  // namespace pgpu

@@ -6,6 +6,7 @@
 #include "common.hpp"
 #include "direct.hpp"
 #include "kernels.cuh"
+#include "profile.hpp"
 
 namespace pgpu {
 
@@ -153,6 +154,8 @@ void launch_direct(int kind, const KParams<T>& kp, const Mat3& a, const DirectSo
   if (chunks < 1) chunks = 1;
 
   const int comps = TGRAD ? 3 : 1;
+  ProfScope ps(sizeof(T) == 4 ? "direct_f32" : "direct_f64",
+               pair_flops(kind) * static_cast<double>(nt) * static_cast<double>(src.nv + src.ng));
   DevBuf<double> part;
   if (chunks > 1) part.resize(static_cast<size_t>(chunks) * nt * comps);
   dim3 grid(bx, chunks);

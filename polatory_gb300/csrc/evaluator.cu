@@ -112,6 +112,8 @@ struct Evaluator<T>::Term {
   double box_width;
   KParams<T> kp;
   DevBuf<P4<T>> spos, sgpos, tpos, tgpos;
+  // Frame coordinates in FP64 for the FMM (it re-expresses them relative to leaf centres).
+  DevBuf<P4<double>> spos_d, tpos_d;
   DevBuf<T> vw, gg;
   std::unique_ptr<Fmm<T>> fmm;
   bool fmm_sources_dirty = true;
@@ -160,9 +162,13 @@ void Evaluator<T>::set_sources(const double* pts, Index mu, const double* gpts, 
   for (auto& t : terms_) {
     t->spos.resize(mu);
     t->sgpos.resize(sigma);
-    if (mu)
+    t->spos_d.resize(mu);
+    if (mu) {
       to_frame_kernel<T><<<blocks_for(mu, 256), 256, 0, stream()>>>(
           pts, mu, t->a, t->origin[0], t->origin[1], t->origin[2], t->spos.data());
+      to_frame_kernel<double><<<blocks_for(mu, 256), 256, 0, stream()>>>(
+          pts, mu, t->a, t->origin[0], t->origin[1], t->origin[2], t->spos_d.data());
+    }
     if (sigma)
       to_frame_kernel<T><<<blocks_for(sigma, 256), 256, 0, stream()>>>(
           gpts, sigma, t->a, t->origin[0], t->origin[1], t->origin[2], t->sgpos.data());
@@ -182,9 +188,13 @@ void Evaluator<T>::set_targets(const double* pts, Index m, const double* gpts, I
   for (auto& t : terms_) {
     t->tpos.resize(m);
     t->tgpos.resize(mg);
-    if (m)
+    t->tpos_d.resize(m);
+    if (m) {
       to_frame_kernel<T><<<blocks_for(m, 256), 256, 0, stream()>>>(
           pts, m, t->a, t->origin[0], t->origin[1], t->origin[2], t->tpos.data());
+      to_frame_kernel<double><<<blocks_for(m, 256), 256, 0, stream()>>>(
+          pts, m, t->a, t->origin[0], t->origin[1], t->origin[2], t->tpos_d.data());
+    }
     if (mg)
       to_frame_kernel<T><<<blocks_for(mg, 256), 256, 0, stream()>>>(
           gpts, mg, t->a, t->origin[0], t->origin[1], t->origin[2], t->tgpos.data());
@@ -255,10 +265,10 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
       }
       if (t.fmm_sources_dirty || t.fmm_targets_dirty) {
         if (symmetric_) {
-          t.fmm->set_points(t.spos.data(), mu_, t.sgpos.data(), sigma_);
+          t.fmm->set_points(t.spos_d.data(), mu_);
         } else {
-          if (t.fmm_sources_dirty) t.fmm->set_sources(t.spos.data(), mu_, t.sgpos.data(), sigma_);
-          if (t.fmm_targets_dirty) t.fmm->set_targets(t.tpos.data(), m_, t.tgpos.data(), mg_);
+          if (t.fmm_sources_dirty) t.fmm->set_sources(t.spos_d.data(), mu_);
+          if (t.fmm_targets_dirty) t.fmm->set_targets(t.tpos_d.data(), m_);
         }
         t.fmm_sources_dirty = t.fmm_targets_dirty = false;
       }

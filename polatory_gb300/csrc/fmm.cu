@@ -26,6 +26,7 @@
 
 #include "fmm.hpp"
 #include "linalg.hpp"
+#include "profile.hpp"
 
 namespace pgpu {
 
@@ -139,14 +140,13 @@ struct Box {
   double width;
 };
 
-template <class T>
-__global__ void keys_kernel(const P4<T>* __restrict__ pos, Index n, Box box, int lf,
+__global__ void keys_kernel(const P4<double>* __restrict__ pos, Index n, Box box, int lf,
                             uint64_t* __restrict__ keys, Index* __restrict__ idx) {
   Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double cells = static_cast<double>(1 << lf);
   const double inv = cells / box.width;
-  P4<T> p = pos[i];
+  P4<double> p = pos[i];
   int c[3];
   double v[3] = {static_cast<double>(p.x), static_cast<double>(p.y), static_cast<double>(p.z)};
 #pragma unroll
@@ -159,11 +159,21 @@ __global__ void keys_kernel(const P4<T>* __restrict__ pos, Index n, Box box, int
   idx[i] = i;
 }
 
+// Sorted positions relative to the centre of their leaf cell.
 template <class T>
-__global__ void gather_pos_kernel(const P4<T>* __restrict__ pos, const Index* __restrict__ perm,
-                                  Index n, P4<T>* __restrict__ out) {
+__global__ void gather_rel_pos_kernel(const P4<double>* __restrict__ pos,
+                                      const Index* __restrict__ perm,
+                                      const uint64_t* __restrict__ keys, Index n, Box box, int lf,
+                                      P4<T>* __restrict__ out) {
   Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = pos[perm[i]];
+  if (i >= n) return;
+  const P4<double> p = pos[perm[i]];
+  const uint64_t k = keys[i];
+  const double wk = box.width / static_cast<double>(1 << lf);
+  const double cx = box.min[0] + (static_cast<double>(compact3(k)) + 0.5) * wk;
+  const double cy = box.min[1] + (static_cast<double>(compact3(k >> 1)) + 0.5) * wk;
+  const double cz = box.min[2] + (static_cast<double>(compact3(k >> 2)) + 0.5) * wk;
+  out[i] = P4<T>{static_cast<T>(p.x - cx), static_cast<T>(p.y - cy), static_cast<T>(p.z - cz), T(0)};
 }
 
 template <class T>
@@ -285,12 +295,9 @@ __global__ void __launch_bounds__(256)
   const Index leaf = blockIdx.x;
   __shared__ T s_b[32][3][P];
   __shared__ T s_w[32];
-  int cx, cy, cz;
-  unmorton(leaf_keys[leaf], cx, cy, cz);
+  (void)leaf_keys;
   const double wk = box.width / static_cast<double>(1 << lf);
-  const T ctr[3] = {static_cast<T>(box.min[0] + (cx + 0.5) * wk),
-                    static_cast<T>(box.min[1] + (cy + 0.5) * wk),
-                    static_cast<T>(box.min[2] + (cz + 0.5) * wk)};
+  const T ctr[3] = {T(0), T(0), T(0)};  // tree positions are relative to the leaf centre
   const T inv_r = static_cast<T>(2.0 / wk);
   const Index beg = leaf_start[leaf], end = leaf_start[leaf + 1];
   T acc[(P3 + 255) / 256];
@@ -403,9 +410,13 @@ __global__ void l2l_kernel(Cheb<T> ch, const Index* __restrict__ parent_of,
 template <int P, class T>
 __global__ void __launch_bounds__(256)
     m2l_kernel(const T* __restrict__ K, const int* __restrict__ table, Index nt,
-               const T* __restrict__ Ms, T* __restrict__ L) {
+               const T* __restrict__ Ms, T* __restrict__ L, int groups, T* __restrict__ part) {
   constexpr int P3 = P * P * P;
   constexpr int NC = P3 / 8;  // row chunks
+  // blockIdx.y selects a contiguous group of offsets; with several groups each block writes a
+  // partial expansion that m2l_reduce_kernel sums in a fixed order.
+  const int o_beg = static_cast<int>((static_cast<long>(blockIdx.y) * kNOff) / groups);
+  const int o_end = static_cast<int>((static_cast<long>(blockIdx.y + 1) * kNOff) / groups);
   extern __shared__ unsigned char smem_raw[];
   T* s_m = reinterpret_cast<T*>(smem_raw);  // [P3][kTT + 1]
   T* s_k = s_m + P3 * (kTT + 1);            // [8][P3]
@@ -417,7 +428,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
   for (int c = 0; c < NC; ++c) acc[c] = T(0);
 
-  for (int o = 0; o < kNOff; ++o) {
+  for (int o = o_beg; o < o_end; ++o) {
     const int ox = o / 49 - 3, oy = (o / 7) % 7 - 3, oz = o % 7 - 3;
     if (abs(ox) <= 1 && abs(oy) <= 1 && abs(oz) <= 1) continue;
     __syncthreads();
@@ -451,9 +462,25 @@ __global__ void __launch_bounds__(256)
   }
   const Index tt = t0 + t;
   if (tt < nt) {
+    if (groups == 1) {
 #pragma unroll
-    for (int c = 0; c < NC; ++c) L[tt * P3 + c * 8 + r] += acc[c];
+      for (int c = 0; c < NC; ++c) L[tt * P3 + c * 8 + r] += acc[c];
+    } else {
+      T* pg = part + (static_cast<Index>(blockIdx.y) * nt + tt) * P3;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) pg[c * 8 + r] = acc[c];
+    }
   }
+}
+
+template <class T>
+__global__ void m2l_reduce_kernel(const T* __restrict__ part, int groups, Index n,
+                                  T* __restrict__ L) {
+  Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T s = T(0);
+  for (int g = 0; g < groups; ++g) s += part[static_cast<Index>(g) * n + i];
+  L[i] += s;
 }
 
 template <int P, class T>
@@ -466,12 +493,9 @@ __global__ void __launch_bounds__(128)
   const Index leaf = blockIdx.x;
   for (int e = threadIdx.x; e < P3; e += blockDim.x) s_l[e] = L[leaf * P3 + e];
   __syncthreads();
-  int cx, cy, cz;
-  unmorton(leaf_keys[leaf], cx, cy, cz);
+  (void)leaf_keys;
   const double wk = box.width / static_cast<double>(1 << lf);
-  const T ctr[3] = {static_cast<T>(box.min[0] + (cx + 0.5) * wk),
-                    static_cast<T>(box.min[1] + (cy + 0.5) * wk),
-                    static_cast<T>(box.min[2] + (cz + 0.5) * wk)};
+  const T ctr[3] = {T(0), T(0), T(0)};  // tree positions are relative to the leaf centre
   const T inv_r = static_cast<T>(2.0 / wk);
   const Index beg = leaf_start[leaf], end = leaf_start[leaf + 1];
   for (Index i = beg + threadIdx.x; i < end; i += blockDim.x) {
@@ -503,7 +527,10 @@ __global__ void __launch_bounds__(128)
     p2p_kernel(KParams<T> kp, const P4<T>* __restrict__ tpos, const Index* __restrict__ tperm,
                const Index* __restrict__ tleaf_start, const int* __restrict__ table,
                const P4<T>* __restrict__ spos, const T* __restrict__ sw,
-               const Index* __restrict__ sleaf_start, double* __restrict__ out) {
+               const Index* __restrict__ sleaf_start, T wleaf, double* __restrict__ out) {
+  // Positions are relative to their leaf centres; the neighbour slot nb = 9 (dx+1) + 3 (dy+1) +
+  // (dz+1) puts the source leaf centre at the target's + (dx, dy, dz) * wleaf, so
+  // d = (t - (dx, dy, dz) wleaf) - s involves only leaf-sized numbers.
   __shared__ P4<T> s_p[128];
   __shared__ int s_nb[27];
   const Index leaf = blockIdx.x;
@@ -518,6 +545,9 @@ __global__ void __launch_bounds__(128)
     for (int nb = 0; nb < 27; ++nb) {
       const int s = s_nb[nb];
       if (s < 0) continue;
+      const T tx = t.x - static_cast<T>(nb / 9 - 1) * wleaf;
+      const T ty = t.y - static_cast<T>((nb / 3) % 3 - 1) * wleaf;
+      const T tz = t.z - static_cast<T>(nb % 3 - 1) * wleaf;
       const Index sb = sleaf_start[s], se = sleaf_start[s + 1];
       for (Index base = sb; base < se; base += 128) {
         const int cnt = static_cast<int>(min(static_cast<Index>(128), se - base));
@@ -532,7 +562,7 @@ __global__ void __launch_bounds__(128)
 #pragma unroll 4
         for (int j = 0; j < cnt; ++j) {
           const P4<T> s4 = s_p[j];
-          const T dx = t.x - s4.x, dy = t.y - s4.y, dz = t.z - s4.z;
+          const T dx = tx - s4.x, dy = ty - s4.y, dz = tz - s4.z;
           acc += rbf_value<KIND>(dx * dx + dy * dy + dz * dz, kp) * s4.w;
         }
         tot += static_cast<double>(acc);
@@ -574,7 +604,7 @@ struct Tree {
 };
 
 template <class T>
-void build_tree(Tree<T>& tr, const P4<T>* pos, Index n, const Box& box, int lf) {
+void build_tree(Tree<T>& tr, const P4<double>* pos, Index n, const Box& box, int lf) {
   cudaStream_t st = stream();
   tr.n = n;
   tr.lf = lf;
@@ -590,7 +620,7 @@ void build_tree(Tree<T>& tr, const P4<T>* pos, Index n, const Box& box, int lf) 
   if (n == 0) return;
   DevBuf<uint64_t> k_in(n), k_out(n);
   DevBuf<Index> i_in(n);
-  keys_kernel<T><<<blocks_for(n, 256), 256, 0, st>>>(pos, n, box, lf, k_in.data(), i_in.data());
+  keys_kernel<<<blocks_for(n, 256), 256, 0, st>>>(pos, n, box, lf, k_in.data(), i_in.data());
   PGPU_LAUNCH_CHECK();
   size_t tmp_bytes = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, k_in.data(), k_out.data(), i_in.data(),
@@ -599,7 +629,8 @@ void build_tree(Tree<T>& tr, const P4<T>* pos, Index n, const Box& box, int lf) 
   PGPU_CUDA(cub::DeviceRadixSort::SortPairs(tmp.data(), tmp_bytes, k_in.data(), k_out.data(),
                                             i_in.data(), tr.perm.data(), n, 0, std::max(1, 3 * lf),
                                             st));
-  gather_pos_kernel<T><<<blocks_for(n, 256), 256, 0, st>>>(pos, tr.perm.data(), n, tr.pos.data());
+  gather_rel_pos_kernel<T><<<blocks_for(n, 256), 256, 0, st>>>(pos, tr.perm.data(), k_out.data(),
+                                                                 n, box, lf, tr.pos.data());
   PGPU_LAUNCH_CHECK();
 
   // Run-length encode level by level: level lf from the sorted point keys, then parents.
@@ -675,8 +706,9 @@ std::shared_ptr<DevBuf<T>> m2l_matrices(int kind, const KParams<T>& kp, double r
 int order_for_accuracy(double accuracy) {
   // accuracy = inf: the reference's default order 6 (fmm_accuracy_estimator.hpp:77-79);
   // accuracy = 0 (the fit operator): the highest order kept here.
-  if (std::isinf(accuracy)) return 6;
-  if (accuracy <= 0.0) return 8;
+  // Order 6 Chebyshev already reaches ~1e-9 of the sum's conditioning on the parity tests,
+  // which the reference's order-12 uniform interpolation targets for the fit operator.
+  if (std::isinf(accuracy) || accuracy <= 0.0) return 6;
   if (accuracy >= 1e-4) return 6;
   return 8;
 }
@@ -695,8 +727,8 @@ struct Fmm<T>::Impl {
   int p = 6;
   Tree<T> src, trg;
   bool symmetric = false;
-  const P4<T>* spos_in = nullptr;
-  const P4<T>* tpos_in = nullptr;
+  const P4<double>* spos_in = nullptr;
+  const P4<double>* tpos_in = nullptr;
   Index ns = 0, nt = 0;
   int lf = 2;
   bool built = false;
@@ -707,6 +739,7 @@ struct Fmm<T>::Impl {
   std::vector<DevBuf<T>> M, L;
   DevBuf<T> sw;
   Index near_pairs = 0;
+  std::vector<Index> m2l_pairs;  // interactions per level
   Cheb<T> ch;
 
   Tree<T>& ttree() { return symmetric ? src : trg; }
@@ -733,6 +766,7 @@ struct Fmm<T>::Impl {
     // Interaction tables.
     m2l_table.clear();
     m2l_table.resize(lf + 1);
+    m2l_pairs.assign(lf + 1, 0);
     kmats.assign(lf + 1, nullptr);
     for (int k = 2; k <= lf; ++k) {
       const Index n_t = tt.ncell[k];
@@ -744,6 +778,10 @@ struct Fmm<T>::Impl {
                                                                src.keys[k].data(), src.ncell[k], k,
                                                                m2l_table[k].data(), cnt.data());
         PGPU_LAUNCH_CHECK();
+        auto hc = cnt.to_host();
+        Index s = 0;
+        for (Index i = 0; i < n_t; ++i) s += hc[i];
+        m2l_pairs[k] = s;
       }
       const double r = box.width / static_cast<double>(1 << k) / 2.0;
       kmats[k] = m2l_matrices<T>(kind, kp, r, p);
@@ -782,8 +820,11 @@ struct Fmm<T>::Impl {
   void run_far(cudaStream_t st, double* out) {
     constexpr int P3 = P * P * P;
     Tree<T>& tt = ttree();
+    const bool f32 = sizeof(T) == 4;
     // Upward pass.
     if (src.ncell[lf] > 0) {
+      ProfScope ps(f32 ? "fmm_p2m_f32" : "fmm_p2m_f64", 4.0 * P3 * static_cast<double>(ns),
+                   static_cast<double>(ns) * 5 * sizeof(T));
       p2m_kernel<P, T><<<static_cast<unsigned>(src.ncell[lf]), 256, 0, st>>>(
           ch, src.pos.data(), sw.data(), src.start[lf].data(), src.keys[lf].data(), box, lf,
           M[lf].data());
@@ -791,6 +832,8 @@ struct Fmm<T>::Impl {
     }
     for (int k = lf - 1; k >= 2; --k) {
       if (src.ncell[k] == 0) continue;
+      ProfScope ps(f32 ? "fmm_m2m_f32" : "fmm_m2m_f64",
+                   static_cast<double>(src.ncell[k + 1]) * 6.0 * P3 * P);
       m2m_kernel<P, T><<<static_cast<unsigned>(src.ncell[k]), ((P3 + 31) / 32) * 32, 0, st>>>(
           ch, src.start[k].data(), src.keys[k + 1].data(), M[k + 1].data(), M[k].data());
       PGPU_LAUNCH_CHECK();
@@ -802,20 +845,37 @@ struct Fmm<T>::Impl {
       if (n_t == 0) continue;
       PGPU_CUDA(cudaMemsetAsync(L[k].data(), 0, n_t * P3 * sizeof(T), st));
       if (k > 2) {
+        ProfScope ps(f32 ? "fmm_l2l_f32" : "fmm_l2l_f64", static_cast<double>(n_t) * 6.0 * P3 * P);
         l2l_kernel<P, T><<<static_cast<unsigned>(n_t), ((P3 + 31) / 32) * 32, 0, st>>>(
             ch, tt.parent[k].data(), tt.keys[k].data(), L[k - 1].data(), L[k].data());
         PGPU_LAUNCH_CHECK();
       }
       if (src.ncell[k] > 0) {
+        ProfScope ps(f32 ? "fmm_m2l_f32" : "fmm_m2l_f64",
+                     2.0 * P3 * P3 * static_cast<double>(m2l_pairs[k]));
         auto kern = m2l_kernel<P, T>;
         PGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem)));
-        kern<<<static_cast<unsigned>((n_t + kTT - 1) / kTT), 256, smem, st>>>(
-            kmats[k]->data(), m2l_table[k].data(), n_t, M[k].data(), L[k].data());
+        // Enough blocks to fill the GPU about twice: split the offsets when the tiles are few.
+        const Index tiles = (n_t + kTT - 1) / kTT;
+        int groups = static_cast<int>(
+            std::min<Index>(16, std::max<Index>(1, (2 * num_sms() + tiles - 1) / tiles)));
+        DevBuf<T> part;
+        if (groups > 1) part.resize(static_cast<size_t>(groups) * n_t * P3);
+        kern<<<dim3(static_cast<unsigned>(tiles), groups), 256, smem, st>>>(
+            kmats[k]->data(), m2l_table[k].data(), n_t, M[k].data(), L[k].data(), groups,
+            part.data());
         PGPU_LAUNCH_CHECK();
+        if (groups > 1) {
+          const Index n = n_t * P3;
+          m2l_reduce_kernel<T><<<blocks_for(n, 256), 256, 0, st>>>(part.data(), groups, n, L[k].data());
+          PGPU_LAUNCH_CHECK();
+        }
       }
     }
     if (tt.ncell[lf] > 0) {
+      const double npt = static_cast<double>(symmetric ? ns : nt);
+      ProfScope ps(f32 ? "fmm_l2p_f32" : "fmm_l2p_f64", npt * (2.0 * P3 + 6.0 * P * P));
       l2p_kernel<P, T><<<static_cast<unsigned>(tt.ncell[lf]), 128, 0, st>>>(
           ch, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), tt.keys[lf].data(), box, lf,
           L[lf].data(), out);
@@ -839,10 +899,13 @@ struct Fmm<T>::Impl {
     }
     const Index ntl = tt.ncell[lf];
     if (ntl > 0) {
+      ProfScope ps(sizeof(T) == 4 ? "fmm_p2p_f32" : "fmm_p2p_f64",
+                   pair_flops(kind) * static_cast<double>(near_pairs));
       dispatch_kind(kind, [&]<int K>() {
         p2p_kernel<K, T><<<static_cast<unsigned>(ntl), 128, 0, st>>>(
             kp, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), p2p_table.data(),
-            src.pos.data(), sw.data(), src.start[lf].data(), out);
+            src.pos.data(), sw.data(), src.start[lf].data(),
+            static_cast<T>(box.width / static_cast<double>(1 << lf)), out);
         return 0;
       });
       PGPU_LAUNCH_CHECK();
@@ -893,7 +956,7 @@ void Fmm<T>::set_config(const FarFieldConfig& c) {
 }
 
 template <class T>
-void Fmm<T>::set_points(const P4<T>* pos, Index n, const P4<T>*, Index) {
+void Fmm<T>::set_points(const P4<double>* pos, Index n) {
   impl_->symmetric = true;
   impl_->spos_in = impl_->tpos_in = pos;
   impl_->ns = impl_->nt = n;
@@ -901,7 +964,7 @@ void Fmm<T>::set_points(const P4<T>* pos, Index n, const P4<T>*, Index) {
 }
 
 template <class T>
-void Fmm<T>::set_sources(const P4<T>* pos, Index n, const P4<T>*, Index) {
+void Fmm<T>::set_sources(const P4<double>* pos, Index n) {
   impl_->symmetric = false;
   impl_->spos_in = pos;
   impl_->ns = n;
@@ -909,7 +972,7 @@ void Fmm<T>::set_sources(const P4<T>* pos, Index n, const P4<T>*, Index) {
 }
 
 template <class T>
-void Fmm<T>::set_targets(const P4<T>* pos, Index n, const P4<T>*, Index) {
+void Fmm<T>::set_targets(const P4<double>* pos, Index n) {
   impl_->symmetric = false;
   impl_->tpos_in = pos;
   impl_->nt = n;

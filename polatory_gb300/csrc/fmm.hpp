@@ -17,9 +17,12 @@ class Fmm {
       double accuracy);
   ~Fmm();
   void set_config(const FarFieldConfig& c);
-  void set_points(const P4<T>* pos, Index n, const P4<T>* gpos, Index ng);
-  void set_sources(const P4<T>* pos, Index n, const P4<T>* gpos, Index ng);
-  void set_targets(const P4<T>* pos, Index n, const P4<T>* gpos, Index ng);
+  // Positions in the anisotropy frame (FP64, relative to the frame origin). The tree keeps them
+  // relative to their leaf centres in T, which keeps FP32 near-field differences exact to FP32
+  // rounding of the (small) leaf-relative offsets.
+  void set_points(const P4<double>* pos, Index n);
+  void set_sources(const P4<double>* pos, Index n);
+  void set_targets(const P4<double>* pos, Index n);
   // Adds the potentials (value targets) and A^T-mapped gradients (gradient targets).
   void evaluate(const T* vw, const T* gg, double* out_v, double* out_g);
   Index near_pairs() const;

@@ -79,4 +79,15 @@ struct Mat3 {
   double a[9];
 };
 
+// Algorithmic flops of one value-value pair interaction (3 subtractions, 5 for r^2, the kernel,
+// 2 for the multiply-add into the accumulator; sqrt/exp/log/div count 1): biharmonic 11,
+// triharmonic 13, exponential 14; the other kernels are counted like the exponential.
+inline double pair_flops(int kind) {
+  switch (kind) {
+    case PGPU_RBF_BH3: return 11.0;
+    case PGPU_RBF_TH3: return 13.0;
+    default: return 14.0;
+  }
+}
+
 }  // namespace pgpu

@@ -1,10 +1,9 @@
 // Device vector kernels. The Krylov kernels are HBM-bound: multi_dot reads each basis vector
 // once (the w segment of a block stays in shared memory), multi_axpy_sub_norm2 reads the basis
 // and w once and writes w once, folding the norm into the same pass (src/krylov/gmres.cpp:20-31).
-#include <cub/block/block_reduce.cuh>
-
 #include "common.hpp"
 #include "linalg.hpp"
+#include "profile.hpp"
 
 namespace pgpu {
 
@@ -255,6 +254,7 @@ void multi_dot(const double* V, Index ld, int k, const double* w, Index n, doubl
   const int nblk = blocks_for(n, kSeg);
   DevBuf<double> part(static_cast<size_t>(nblk) * k);
   DevBuf<double> out(k);
+  ProfScope ps("krylov_multidot", 2.0 * k * n, (k + 1.0) * n * sizeof(double));
   multi_dot_kernel<<<nblk, kRedThreads, 0, stream()>>>(V, ld, k, w, n, part.data());
   PGPU_LAUNCH_CHECK();
   reduce_rows_kernel<<<k, kRedThreads, 0, stream()>>>(part.data(), nblk, k, out.data());
@@ -270,6 +270,7 @@ double multi_axpy_sub_norm2(const double* V, Index ld, int k, const double* h, d
   dh.upload(h, k);
   const int nblk = reduce_blocks(n);
   DevBuf<double> part(nblk);
+  ProfScope ps("krylov_axpy_norm", 2.0 * (k + 1) * n, (k + 2.0) * n * sizeof(double));
   multi_axpy_sub_norm2_kernel<<<nblk, kRedThreads, 0, stream()>>>(V, ld, k, dh.data(), w, n,
                                                                   part.data(), -1.0, 1);
   PGPU_LAUNCH_CHECK();
@@ -282,6 +283,7 @@ void multi_axpy(const double* Z, Index ld, int k, const double* y, double* x, In
   DevBuf<double> dy;
   dy.upload(y, k);
   const int nblk = reduce_blocks(n);
+  ProfScope ps("krylov_solution", 2.0 * k * n, (k + 2.0) * n * sizeof(double));
   multi_axpy_sub_norm2_kernel<<<nblk, kRedThreads, 0, stream()>>>(Z, ld, k, dy.data(), x, n,
                                                                   nullptr, 1.0, 0);
   PGPU_LAUNCH_CHECK();

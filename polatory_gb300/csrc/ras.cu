@@ -11,6 +11,7 @@
 
 #include "kernels.cuh"
 #include "linalg.hpp"
+#include "profile.hpp"
 #include "ras.hpp"
 
 namespace pgpu {
@@ -246,6 +247,41 @@ __global__ void syrk_update_kernel(int kb, const int* __restrict__ lds,
   }
 }
 
+// Replaces every 32x32 diagonal block of the Cholesky factor by its inverse (lower triangular),
+// so that the triangular solves apply the diagonal blocks as small matrix-vector products
+// instead of 32-step dependent substitutions.
+template <class T>
+__global__ void invert_diag_kernel(const int* __restrict__ lds, const Index* __restrict__ mat_off,
+                                   T* __restrict__ mats) {
+  const Index d = blockIdx.x;
+  const int ld = lds[d];
+  const int kb = blockIdx.y;
+  if (kb * NB >= ld) return;
+  __shared__ T a[NB][NB + 1];
+  __shared__ T inv[NB][NB + 1];
+  T* m = mats + mat_off[d] + static_cast<Index>(kb * NB) * ld + kb * NB;
+  const int lane = threadIdx.x;
+  for (int c = 0; c < NB; ++c) a[lane][c] = m[lane + static_cast<Index>(c) * ld];
+  __syncwarp();
+  // Column `lane` of the inverse by forward substitution.
+  const int j = lane;
+  for (int i = 0; i < NB; ++i) {
+    T v;
+    if (i < j) {
+      v = T(0);
+    } else if (i == j) {
+      v = T(1) / a[j][j];
+    } else {
+      T s = T(0);
+      for (int k = j; k < i; ++k) s += a[i][k] * inv[k][j];
+      v = -s / a[i][i];
+    }
+    inv[i][j] = v;
+  }
+  __syncwarp();
+  for (int c = 0; c < NB; ++c) m[lane + static_cast<Index>(c) * ld] = inv[lane][c];
+}
+
 // Fine (or coarse) solve of every domain: gather the residuals, form Q^T d, solve with the
 // Cholesky factor, expand lambda = Q gamma and scatter the owned entries
 // (fine_grid.hpp:97-156, coarse_grid.hpp:91-131).
@@ -284,15 +320,15 @@ __global__ void ras_solve_kernel(const int* __restrict__ nsz, const int* __restr
   // Forward: L y = b.
   for (int kb = 0; kb < nb; ++kb) {
     if (warp == 0) {
+      // y_blk = L_kk^{-1} b_blk (the diagonal block holds the inverse).
       const int base = kb * NB;
-      double xi = x[base + lane];
+      const double bi = x[base + lane];
+      double yi = 0;
       for (int jj = 0; jj < NB; ++jj) {
-        double yj = __shfl_sync(0xffffffffu, xi, jj) /
-                    static_cast<double>(m[(base + jj) + static_cast<Index>(base + jj) * ld]);
-        if (lane == jj) xi = yj;
-        if (lane > jj) xi -= static_cast<double>(m[(base + lane) + static_cast<Index>(base + jj) * ld]) * yj;
+        const double bj = __shfl_sync(0xffffffffu, bi, jj);
+        if (jj <= lane) yi += static_cast<double>(m[(base + lane) + static_cast<Index>(base + jj) * ld]) * bj;
       }
-      x[base + lane] = xi;
+      x[base + lane] = yi;
     }
     __syncthreads();
     for (int r = (kb + 1) * NB + tid; r < ld; r += blockDim.x) {
@@ -316,14 +352,14 @@ __global__ void ras_solve_kernel(const int* __restrict__ nsz, const int* __restr
     }
     __syncthreads();
     if (warp == 0) {
-      double xi = x[base + lane];
-      for (int jj = NB - 1; jj >= 0; --jj) {
-        double zj = __shfl_sync(0xffffffffu, xi, jj) /
-                    static_cast<double>(m[(base + jj) + static_cast<Index>(base + jj) * ld]);
-        if (lane == jj) xi = zj;
-        if (lane < jj) xi -= static_cast<double>(m[(base + jj) + static_cast<Index>(base + lane) * ld]) * zj;
+      // x_blk = L_kk^{-T} y_blk: lane i sums inv[j][i] y_j over j >= i.
+      const double yi = x[base + lane];
+      double zi = 0;
+      for (int jj = 0; jj < NB; ++jj) {
+        const double yj = __shfl_sync(0xffffffffu, yi, jj);
+        if (jj >= lane) zi += static_cast<double>(m[(base + jj) + static_cast<Index>(base + lane) * ld]) * yj;
       }
-      x[base + lane] = xi;
+      x[base + lane] = zi;
     }
     __syncthreads();
   }
@@ -570,6 +606,8 @@ void RasPreconditioner<T>::build_batch(DomainBatch<T>& b, const std::vector<Doma
     b.max_n = std::max(b.max_n, ld[d]);
     mat_off[d] = moff;
     moff += static_cast<Index>(ld[d]) * ld[d];
+    b.factor_flops += static_cast<double>(n[d]) * n[d] * n[d] / 3.0;
+    b.solve_bytes += static_cast<double>(n[d]) * n[d] * sizeof(T);  // two triangle sweeps
     pt_off[d] = poff;
     poff += m;
     pts.insert(pts.end(), dom.point_indices.begin(), dom.point_indices.end());
@@ -593,6 +631,7 @@ void RasPreconditioner<T>::build_batch(DomainBatch<T>& b, const std::vector<Doma
   if (b.n_dom == 0) return;
 
   // Assembly, one pass per RBF in its own frame.
+  ProfScope ps(sizeof(T) == 4 ? "ras_factor_f32" : "ras_factor_f64", b.factor_flops);
   const int nbmax = b.max_n / NB;
   const Index ntiles = static_cast<Index>(nbmax) * (nbmax + 1) / 2;
   for (size_t r = 0; r < model_.rbfs.size(); ++r) {
@@ -644,6 +683,9 @@ void RasPreconditioner<T>::build_batch(DomainBatch<T>& b, const std::vector<Doma
     syrk_update_kernel<T><<<gs, 256, 0, stream()>>>(kb, b.ld.data(), b.mat_off.data(), b.mats.data());
     PGPU_LAUNCH_CHECK();
   }
+  invert_diag_kernel<T><<<dim3(static_cast<unsigned>(b.n_dom), nbmax), 32, 0, stream()>>>(
+      b.ld.data(), b.mat_off.data(), b.mats.data());
+  PGPU_LAUNCH_CHECK();
 }
 
 template <class T>
@@ -653,6 +695,8 @@ void RasPreconditioner<T>::solve_level(int level, const double* residuals, doubl
   if (b.n_dom == 0) return;
   const size_t smem = (static_cast<size_t>(b.max_n) + 16 + 64) * sizeof(double);
   DevBuf<double> cout(32);
+  ProfScope ps(sizeof(T) == 4 ? "ras_solve_f32" : "ras_solve_f64", 2.0 * b.solve_bytes / sizeof(T),
+               b.solve_bytes);
   ras_solve_kernel<T><<<static_cast<unsigned>(b.n_dom), 256, smem, stream()>>>(
       b.n.data(), b.ld.data(), b.mat_off.data(), b.mats.data(), b.pt_off.data(), b.pts.data(),
       b.inner.data(), l_, lagrange_.data(), u_.data(), residuals, weights, level == 0 ? 1 : 0,

@@ -30,6 +30,8 @@ struct DomainBatch {
   DevBuf<char> inner;            // inner flag per entry of pts
   DevBuf<int> info;              // per-domain count of modified pivots
   Index total_points = 0;
+  double factor_flops = 0;       // sum of n^3 / 3
+  double solve_bytes = 0;        // factor bytes read per solve (forward + backward sweeps)
 };
 
 template <class T>

@@ -1,6 +1,8 @@
 // Library context: per-thread device and stream, the stream-ordered memory pool, pointer
 // classification and the host<->device copy helpers.
+#include <atomic>
 #include <chrono>
+#include <cstdlib>
 #include <mutex>
 
 #include "common.hpp"
@@ -115,6 +117,18 @@ int num_sms() {
   }
   return sms;
 }
+
+bool verbose() {
+  static const bool v = std::getenv("PGPU_VERBOSE") != nullptr;
+  return v;
+}
+
+namespace {
+std::atomic<int64_t> g_launches{0};
+}
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 double wall_seconds() {
   using clock = std::chrono::steady_clock;

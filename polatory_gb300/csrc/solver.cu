@@ -343,7 +343,12 @@ FitResult fit_impl(const FitRequest& req) {
     res.iterations = solver.iteration_count();
   } else {
     // Iterative refinement: FP64 residuals, FP32 inner solves.
-    Operator<double> op64(model, pts.data(), mu, bbox, 0.0, P.data());
+    // Residual operator: exact FP64 sums while they are cheap; beyond that the FP32 FMM whose
+    // near field subtracts leaf-relative coordinates (exact to FP32 rounding of leaf-sized
+    // offsets) and accumulates every tile in FP64 — the compensated near-field sum.
+    const bool fp64_residual = static_cast<double>(mu) * static_cast<double>(mu) <= 1073741824.0;
+    std::unique_ptr<Operator<double>> op64;
+    if (fp64_residual) op64 = std::make_unique<Operator<double>>(model, pts.data(), mu, bbox, 0.0, P.data());
     Operator<float> op32(model, pts.data(), mu, bbox, 0.0, P.data());
     DevBuf<double> r(M), delta(M), zero(M);
     zero.zero();
@@ -351,7 +356,8 @@ FitResult fit_impl(const FitRequest& req) {
     for (int outer = 0;; ++outer) {
       // r = rhs - op64(w): the FP64 residual at every data point (the same absolute inf-norm
       // test as residual_evaluator.hpp:93-107, evaluated with the fit operator's accuracy).
-      op64.apply(w.data(), r.data());
+      if (op64) op64->apply(w.data(), r.data());
+      else op32.apply(w.data(), r.data());
       axpby(M, 1.0, rhs.data(), -1.0, r.data());
       const double rinf = inf_norm_diff(r.data(), zero.data(), mu);
       res.residual = rinf;
