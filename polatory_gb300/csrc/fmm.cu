@@ -163,12 +163,12 @@ __global__ void keys_kernel(const P4<double>* __restrict__ pos, Index n, Box box
 template <class T>
 __global__ void gather_rel_pos_kernel(const P4<double>* __restrict__ pos,
                                       const Index* __restrict__ perm,
-                                      const uint64_t* __restrict__ keys, Index n, Box box, int lf,
-                                      P4<T>* __restrict__ out) {
+                                      const uint64_t* __restrict__ keys, int shift, Index n,
+                                      Box box, int lf, P4<T>* __restrict__ out) {
   Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const P4<double> p = pos[perm[i]];
-  const uint64_t k = keys[i];
+  const uint64_t k = keys[i] >> shift;
   const double wk = box.width / static_cast<double>(1 << lf);
   const double cx = box.min[0] + (static_cast<double>(compact3(k)) + 0.5) * wk;
   const double cy = box.min[1] + (static_cast<double>(compact3(k >> 1)) + 0.5) * wk;
@@ -603,9 +603,77 @@ struct Tree {
   std::vector<DevBuf<Index>> parent;  // level k: parent index (k >= 1)
 };
 
-template <class T>
-void build_tree(Tree<T>& tr, const P4<double>* pos, Index n, const Box& box, int lf) {
+void copy_index(Index* dst, const Index* src, Index n) {
+  PGPU_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(Index), cudaMemcpyDeviceToDevice, stream()));
+}
+
+// Points sorted once by their Morton key at the deepest candidate level; the key of any
+// shallower level is a right shift of it, so the leaf level can be chosen after sorting.
+constexpr int kSortLevel = 10;
+
+struct SortedPoints {
+  Index n = 0;
+  DevBuf<uint64_t> keys;  // level kSortLevel, ascending
+  DevBuf<Index> perm;     // sorted position -> input index
+};
+
+void sort_points(SortedPoints& sp, const P4<double>* pos, Index n, const Box& box) {
   cudaStream_t st = stream();
+  sp.n = n;
+  sp.keys.resize(n);
+  sp.perm.resize(n);
+  if (n == 0) return;
+  DevBuf<uint64_t> k_in(n);
+  DevBuf<Index> i_in(n);
+  keys_kernel<<<blocks_for(n, 256), 256, 0, st>>>(pos, n, box, kSortLevel, k_in.data(), i_in.data());
+  PGPU_LAUNCH_CHECK();
+  size_t tmp_bytes = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, k_in.data(), sp.keys.data(), i_in.data(),
+                                  sp.perm.data(), n, 0, 3 * kSortLevel, st);
+  DevBuf<unsigned char> tmp(tmp_bytes);
+  PGPU_CUDA(cub::DeviceRadixSort::SortPairs(tmp.data(), tmp_bytes, k_in.data(), sp.keys.data(),
+                                            i_in.data(), sp.perm.data(), n, 0, 3 * kSortLevel, st));
+}
+
+// hist[d] = number of i with the first level at which key[i] and key[i-1] differ equal to d.
+__global__ void occupancy_kernel(const uint64_t* __restrict__ keys, Index n,
+                                 unsigned long long* __restrict__ hist) {
+  __shared__ unsigned int h[kSortLevel + 1];
+  if (threadIdx.x <= kSortLevel) h[threadIdx.x] = 0;
+  __syncthreads();
+  for (Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x + 1; i < n;
+       i += static_cast<Index>(gridDim.x) * blockDim.x) {
+    const uint64_t x = keys[i] ^ keys[i - 1];
+    if (x == 0) continue;
+    const int hb = 63 - __clzll(static_cast<long long>(x));
+    atomicAdd(&h[kSortLevel - hb / 3], 1u);
+  }
+  __syncthreads();
+  if (threadIdx.x <= kSortLevel && h[threadIdx.x]) atomicAdd(hist + threadIdx.x, h[threadIdx.x]);
+}
+
+// Occupied cells per level 0..kSortLevel.
+std::vector<Index> occupancy(const SortedPoints& sp) {
+  std::vector<Index> occ(kSortLevel + 1, sp.n > 0 ? 1 : 0);
+  if (sp.n < 2) return occ;
+  DevBuf<unsigned long long> hist(kSortLevel + 1);
+  hist.zero();
+  occupancy_kernel<<<std::min<Index>(blocks_for(sp.n, 256), 4 * num_sms()), 256, 0, stream()>>>(
+      sp.keys.data(), sp.n, hist.data());
+  PGPU_LAUNCH_CHECK();
+  auto h = hist.to_host();
+  Index run = 1;
+  for (int k = 0; k <= kSortLevel; ++k) {
+    run += static_cast<Index>(h[k]);
+    occ[k] = run;
+  }
+  return occ;
+}
+
+template <class T>
+void build_tree(Tree<T>& tr, const SortedPoints& sp, const P4<double>* pos, const Box& box, int lf) {
+  cudaStream_t st = stream();
+  const Index n = sp.n;
   tr.n = n;
   tr.lf = lf;
   tr.keys.clear();
@@ -618,27 +686,19 @@ void build_tree(Tree<T>& tr, const P4<double>* pos, Index n, const Box& box, int
   tr.perm.resize(n);
   tr.pos.resize(n);
   if (n == 0) return;
-  DevBuf<uint64_t> k_in(n), k_out(n);
-  DevBuf<Index> i_in(n);
-  keys_kernel<<<blocks_for(n, 256), 256, 0, st>>>(pos, n, box, lf, k_in.data(), i_in.data());
-  PGPU_LAUNCH_CHECK();
-  size_t tmp_bytes = 0;
-  cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, k_in.data(), k_out.data(), i_in.data(),
-                                  tr.perm.data(), n, 0, std::max(1, 3 * lf), st);
-  DevBuf<unsigned char> tmp(tmp_bytes);
-  PGPU_CUDA(cub::DeviceRadixSort::SortPairs(tmp.data(), tmp_bytes, k_in.data(), k_out.data(),
-                                            i_in.data(), tr.perm.data(), n, 0, std::max(1, 3 * lf),
-                                            st));
-  gather_rel_pos_kernel<T><<<blocks_for(n, 256), 256, 0, st>>>(pos, tr.perm.data(), k_out.data(),
-                                                                 n, box, lf, tr.pos.data());
+  copy_index(tr.perm.data(), sp.perm.data(), n);
+  const int leaf_shift = 3 * (kSortLevel - lf);
+  gather_rel_pos_kernel<T><<<blocks_for(n, 256), 256, 0, st>>>(pos, tr.perm.data(), sp.keys.data(),
+                                                                 leaf_shift, n, box, lf,
+                                                                 tr.pos.data());
   PGPU_LAUNCH_CHECK();
 
   // Run-length encode level by level: level lf from the sorted point keys, then parents.
   DevBuf<Index> flags(n), scan(n);
-  const uint64_t* src_keys = k_out.data();
+  const uint64_t* src_keys = sp.keys.data();
   Index src_n = n;
   for (int k = lf; k >= 0; --k) {
-    const int shift = (k == lf) ? 0 : 3;
+    const int shift = (k == lf) ? leaf_shift : 3;
     rle_flags_kernel<<<blocks_for(src_n, 256), 256, 0, st>>>(src_keys, src_n, shift, flags.data());
     PGPU_LAUNCH_CHECK();
     size_t sb = 0;
@@ -744,23 +804,35 @@ struct Fmm<T>::Impl {
 
   Tree<T>& ttree() { return symmetric ? src : trg; }
 
-  int choose_leaf_level() const {
-    if (cfg_set && cfg.leaf_level >= 0) return cfg.leaf_level;
-    // Sources per leaf around 64 (FP32) / 32 (FP64) for uniform data; at least two levels of
-    // far field.
-    const double per_leaf = sizeof(T) == 4 ? 64.0 : 32.0;
-    const Index n = std::max(ns, std::min(nt, ns * 4));
-    int lf = static_cast<int>(std::lround(std::log(std::max(1.0, n / per_leaf)) / std::log(8.0)));
-    return std::min(std::max(lf, 2), 10);
+  // Leaf level from the measured occupancy: the level whose average number of sources per
+  // occupied leaf is closest (in ratio) to the target — surface data fills far fewer cells than
+  // uniform data, so a level chosen from the point count alone would overfill the leaves.
+  int choose_leaf_level(const std::vector<Index>& occ) const {
+    if (cfg_set && cfg.leaf_level >= 0) return std::min(cfg.leaf_level, kSortLevel);
+    const double target = sizeof(T) == 4 ? 96.0 : 40.0;
+    int best = 2;
+    double best_d = INFINITY;
+    for (int k = 2; k <= kSortLevel; ++k) {
+      const double avg = static_cast<double>(ns) / std::max<Index>(occ[k], 1);
+      const double d = std::fabs(std::log(std::max(avg, 1e-9) / target));
+      if (d < best_d) {
+        best_d = d;
+        best = k;
+      }
+    }
+    return best;
   }
 
   void build() {
-    lf = choose_leaf_level();
+    SortedPoints ss, ts;
+    sort_points(ss, spos_in, ns, box);
+    if (!symmetric) sort_points(ts, tpos_in, nt, box);
+    lf = choose_leaf_level(occupancy(ss));
     p = cfg_set && cfg.order > 0 ? cfg.order : order_for_accuracy(accuracy);
     if (p != 4 && p != 6 && p != 8) p = 6;
     ch = make_cheb<T>(p);
-    build_tree(src, spos_in, ns, box, lf);
-    if (!symmetric) build_tree(trg, tpos_in, nt, box, lf);
+    build_tree(src, ss, spos_in, box, lf);
+    if (!symmetric) build_tree(trg, ts, tpos_in, box, lf);
     Tree<T>& tt = ttree();
     cudaStream_t st = stream();
     // Interaction tables.

@@ -282,6 +282,145 @@ __global__ void invert_diag_kernel(const int* __restrict__ lds, const Index* __r
   for (int c = 0; c < NB; ++c) m[lane + static_cast<Index>(c) * ld] = inv[lane][c];
 }
 
+// Solves L L^T x = b in place (x in shared memory, ld entries) with the factor whose diagonal
+// blocks hold their inverses. Block-sequential; within a block the diagonal block is a 32x32
+// product (warp 0, loads issued before the shuffles) and the off-diagonal part is spread over
+// the whole thread block.
+template <class T>
+__device__ void chol_solve_inplace(double* x, const T* __restrict__ m, int ld) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int nb = ld / NB;
+  // Forward: L y = b.
+  for (int kb = 0; kb < nb; ++kb) {
+    const int base = kb * NB;
+    if (warp == 0) {
+      double a[NB];
+#pragma unroll
+      for (int jj = 0; jj < NB; ++jj)
+        a[jj] = jj <= lane ? static_cast<double>(m[(base + lane) + static_cast<Index>(base + jj) * ld]) : 0.0;
+      const double bi = x[base + lane];
+      double yi = 0;
+#pragma unroll
+      for (int jj = 0; jj < NB; ++jj) yi += a[jj] * __shfl_sync(0xffffffffu, bi, jj);
+      x[base + lane] = yi;
+    }
+    __syncthreads();
+    for (int r = (kb + 1) * NB + tid; r < ld; r += blockDim.x) {
+      double s = 0;
+#pragma unroll 8
+      for (int c = 0; c < NB; ++c) s += static_cast<double>(m[r + static_cast<Index>(base + c) * ld]) * x[base + c];
+      x[r] -= s;
+    }
+    __syncthreads();
+  }
+  // Backward: L^T x = y.
+  for (int kb = nb - 1; kb >= 0; --kb) {
+    const int base = kb * NB;
+    for (int c = warp; c < NB; c += nw) {
+      const int col = base + c;
+      double s = 0;
+      for (int r = (kb + 1) * NB + lane; r < ld; r += 32)
+        s += static_cast<double>(m[r + static_cast<Index>(col) * ld]) * x[r];
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) x[col] -= s;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      // x_blk = L_kk^{-T} y_blk: lane i sums inv[j][i] y_j over j >= i (column i of the block).
+      double a[NB];
+#pragma unroll
+      for (int jj = 0; jj < NB; ++jj)
+        a[jj] = jj >= lane ? static_cast<double>(m[(base + jj) + static_cast<Index>(base + lane) * ld]) : 0.0;
+      const double yi = x[base + lane];
+      double zi = 0;
+#pragma unroll
+      for (int jj = 0; jj < NB; ++jj) zi += a[jj] * __shfl_sync(0xffffffffu, yi, jj);
+      x[base + lane] = zi;
+    }
+    __syncthreads();
+  }
+}
+
+// Column j of (L L^T)^{-1} for every j (grid = ld blocks): the coarse grid keeps the explicit
+// inverse so that each coarse solve is one matrix-vector product spread over the GPU.
+template <class T>
+__global__ void chol_inverse_kernel(const T* __restrict__ m, int ld, int n, double* __restrict__ inv) {
+  extern __shared__ double sh[];
+  double* x = sh;
+  const int j = blockIdx.x;
+  for (int i = threadIdx.x; i < ld; i += blockDim.x) x[i] = (i == j) ? 1.0 : 0.0;
+  __syncthreads();
+  chol_solve_inplace(x, m, ld);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) inv[static_cast<Index>(j) * n + i] = x[i];
+}
+
+// Coarse right-hand side: x_i = d_{l+i} - sum_k L_ik d_k (Q^T d), d_k the polynomial points.
+__global__ void coarse_rhs_kernel(const Index* __restrict__ dp, int n, int l,
+                                  const double* __restrict__ lag, const double* __restrict__ resid,
+                                  double* __restrict__ x, double* __restrict__ dh_out) {
+  __shared__ double dh[16];
+  if (threadIdx.x < l) dh[threadIdx.x] = resid[dp[threadIdx.x]];
+  __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x < l) dh_out[threadIdx.x] = dh[threadIdx.x];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Index g = dp[l + i];
+  double s = resid[g];
+  for (int k = 0; k < l; ++k) s -= lag[g * l + k] * dh[k];
+  x[i] = s;
+}
+
+// y = S x for a symmetric n x n matrix (column j contiguous): one warp per output entry.
+__global__ void symv_kernel(const double* __restrict__ s, int n, const double* __restrict__ x,
+                            double* __restrict__ y) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const double* col = s + static_cast<Index>(warp) * n;
+  double acc = 0;
+  for (int j = lane; j < n; j += 32) acc += col[j] * x[j];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) y[warp] = acc;
+}
+
+// lambda = Q gamma scattered to every coarse point; out[k] = lambda_head_k, out[16+k] = sum_i
+// u_ik gamma_i (for the polynomial solve on the host).
+__global__ void coarse_finish_kernel(const Index* __restrict__ dp, int n, int l,
+                                     const double* __restrict__ lag, const double* __restrict__ u,
+                                     const double* __restrict__ gamma, double* __restrict__ weights,
+                                     double* __restrict__ out) {
+  __shared__ double red[2][32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  for (int i = tid; i < n; i += blockDim.x) weights[dp[l + i]] = gamma[i];
+  for (int k = 0; k < l; ++k) {
+    double s1 = 0, s2 = 0;
+    for (int i = tid; i < n; i += blockDim.x) {
+      const Index g = dp[l + i];
+      s1 += lag[g * l + k] * gamma[i];
+      s2 += u[g * l + k] * gamma[i];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    __syncthreads();
+    if (lane == 0) {
+      red[0][warp] = s1;
+      red[1][warp] = s2;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double a = 0, b = 0;
+      for (int w = 0; w < nw; ++w) {
+        a += red[0][w];
+        b += red[1][w];
+      }
+      out[k] = -a;
+      out[16 + k] = b;
+      weights[dp[k]] = -a;
+    }
+  }
+}
+
 // Fine (or coarse) solve of every domain: gather the residuals, form Q^T d, solve with the
 // Cholesky factor, expand lambda = Q gamma and scatter the owned entries
 // (fine_grid.hpp:97-156, coarse_grid.hpp:91-131).
@@ -316,53 +455,7 @@ __global__ void ras_solve_kernel(const int* __restrict__ nsz, const int* __restr
     x[i] = s;
   }
   __syncthreads();
-  const int nb = ld / NB;
-  // Forward: L y = b.
-  for (int kb = 0; kb < nb; ++kb) {
-    if (warp == 0) {
-      // y_blk = L_kk^{-1} b_blk (the diagonal block holds the inverse).
-      const int base = kb * NB;
-      const double bi = x[base + lane];
-      double yi = 0;
-      for (int jj = 0; jj < NB; ++jj) {
-        const double bj = __shfl_sync(0xffffffffu, bi, jj);
-        if (jj <= lane) yi += static_cast<double>(m[(base + lane) + static_cast<Index>(base + jj) * ld]) * bj;
-      }
-      x[base + lane] = yi;
-    }
-    __syncthreads();
-    for (int r = (kb + 1) * NB + tid; r < ld; r += blockDim.x) {
-      double s = 0;
-#pragma unroll 8
-      for (int c = 0; c < NB; ++c) s += static_cast<double>(m[r + static_cast<Index>(kb * NB + c) * ld]) * x[kb * NB + c];
-      x[r] -= s;
-    }
-    __syncthreads();
-  }
-  // Backward: L^T x = y.
-  for (int kb = nb - 1; kb >= 0; --kb) {
-    const int base = kb * NB;
-    for (int c = warp; c < NB; c += nw) {
-      const int col = base + c;
-      double s = 0;
-      for (int r = (kb + 1) * NB + lane; r < ld; r += 32)
-        s += static_cast<double>(m[r + static_cast<Index>(col) * ld]) * x[r];
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) x[col] -= s;
-    }
-    __syncthreads();
-    if (warp == 0) {
-      // x_blk = L_kk^{-T} y_blk: lane i sums inv[j][i] y_j over j >= i.
-      const double yi = x[base + lane];
-      double zi = 0;
-      for (int jj = 0; jj < NB; ++jj) {
-        const double yj = __shfl_sync(0xffffffffu, yi, jj);
-        if (jj >= lane) zi += static_cast<double>(m[(base + jj) + static_cast<Index>(base + lane) * ld]) * yj;
-      }
-      x[base + lane] = zi;
-    }
-    __syncthreads();
-  }
+  chol_solve_inplace(x, m, ld);
   // lambda_head_k = -sum_i L_ik gamma_i ; for the coarse grid also s_k = sum_i u_ik gamma_i.
   for (int k = 0; k < l; ++k) {
     double s1 = 0, s2 = 0;
@@ -531,6 +624,19 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
     cd.inner_point.assign(cd.point_indices.size(), 1);
     std::vector<Domain> v{cd};
     build_batch(coarse_, v);
+    coarse_n_ = std::max(static_cast<int>(cd.point_indices.size()) - l_, 0);
+    const int cld = std::max(NB, ((coarse_n_ + NB - 1) / NB) * NB);
+    coarse_inv_.resize(std::max<Index>(static_cast<Index>(coarse_n_) * coarse_n_, 1));
+    if (coarse_n_ > 0) {
+      chol_inverse_kernel<double><<<coarse_n_, 256, cld * sizeof(double), stream()>>>(
+          coarse_.mats.data(), cld, coarse_n_, coarse_inv_.data());
+      PGPU_LAUNCH_CHECK();
+    }
+    coarse_x_.resize(std::max(coarse_n_, 1));
+    coarse_g_.resize(std::max(coarse_n_, 1));
+    coarse_out_.resize(48);
+    coarse_out_.zero();
+    coarse_.mats.release();  // the explicit inverse replaces the factor
   }
 
   // Level point sets on the device (for the residual-update evaluators).
@@ -589,7 +695,8 @@ Index RasPreconditioner<T>::n_domains() const {
 }
 
 template <class T>
-void RasPreconditioner<T>::build_batch(DomainBatch<T>& b, const std::vector<Domain>& domains) {
+template <class U>
+void RasPreconditioner<T>::build_batch(DomainBatch<U>& b, const std::vector<Domain>& domains) {
   const int l = l_;
   b.n_dom = static_cast<Index>(domains.size());
   std::vector<int> n(b.n_dom), ld(b.n_dom);
@@ -607,7 +714,7 @@ void RasPreconditioner<T>::build_batch(DomainBatch<T>& b, const std::vector<Doma
     mat_off[d] = moff;
     moff += static_cast<Index>(ld[d]) * ld[d];
     b.factor_flops += static_cast<double>(n[d]) * n[d] * n[d] / 3.0;
-    b.solve_bytes += static_cast<double>(n[d]) * n[d] * sizeof(T);  // two triangle sweeps
+    b.solve_bytes += static_cast<double>(n[d]) * n[d] * sizeof(U);  // two triangle sweeps
     pt_off[d] = poff;
     poff += m;
     pts.insert(pts.end(), dom.point_indices.begin(), dom.point_indices.end());
@@ -631,7 +738,7 @@ void RasPreconditioner<T>::build_batch(DomainBatch<T>& b, const std::vector<Doma
   if (b.n_dom == 0) return;
 
   // Assembly, one pass per RBF in its own frame.
-  ProfScope ps(sizeof(T) == 4 ? "ras_factor_f32" : "ras_factor_f64", b.factor_flops);
+  ProfScope ps(sizeof(U) == 4 ? "ras_factor_f32" : "ras_factor_f64", b.factor_flops);
   const int nbmax = b.max_n / NB;
   const Index ntiles = static_cast<Index>(nbmax) * (nbmax + 1) / 2;
   for (size_t r = 0; r < model_.rbfs.size(); ++r) {
@@ -650,16 +757,16 @@ void RasPreconditioner<T>::build_batch(DomainBatch<T>& b, const std::vector<Doma
     }
     double o[3];
     for (int q = 0; q < 3; ++q) o[q] = bbox_.empty() ? 0.0 : 0.5 * (tmin[q] + tmax[q]);
-    DevBuf<P4<T>> frame(mu_);
-    frame_kernel<T><<<blocks_for(mu_, 256), 256, 0, stream()>>>(points_dev_, mu_, a, o[0], o[1], o[2],
+    DevBuf<P4<U>> frame(mu_);
+    frame_kernel<U><<<blocks_for(mu_, 256), 256, 0, stream()>>>(points_dev_, mu_, a, o[0], o[1], o[2],
                                                                 frame.data());
     PGPU_LAUNCH_CHECK();
-    KParams<T> kp{static_cast<T>(rb.p[0]), static_cast<T>(rb.p[1])};
+    KParams<U> kp{static_cast<U>(rb.p[0]), static_cast<U>(rb.p[1])};
     const int first = r == 0, last = r + 1 == model_.rbfs.size();
     if (ntiles > 65535) throw_runtime("domain too large for the batched assembly");
     dim3 grid(static_cast<unsigned>(b.n_dom), static_cast<unsigned>(ntiles));
     dispatch_kind(rb.kind, [&]<int K>() {
-      assemble_kernel<T, K><<<grid, 256, 0, stream()>>>(
+      assemble_kernel<U, K><<<grid, 256, 0, stream()>>>(
           kp, frame.data(), b.n.data(), b.ld.data(), b.mat_off.data(), b.mats.data(),
           b.pt_off.data(), b.pts.data(), l, first, last, model_.nugget, lagrange_.data(),
           u_.data(), v_.data());
@@ -670,20 +777,20 @@ void RasPreconditioner<T>::build_batch(DomainBatch<T>& b, const std::vector<Doma
 
   // Blocked Cholesky over all domains.
   for (int kb = 0; kb < nbmax; ++kb) {
-    potrf_diag_kernel<T><<<static_cast<unsigned>(b.n_dom), 32, 0, stream()>>>(
+    potrf_diag_kernel<U><<<static_cast<unsigned>(b.n_dom), 32, 0, stream()>>>(
         kb, b.ld.data(), b.mat_off.data(), b.mats.data(), b.info.data());
     PGPU_LAUNCH_CHECK();
     const int rows_below = b.max_n - (kb + 1) * NB;
     if (rows_below <= 0) continue;
     dim3 gp(static_cast<unsigned>(b.n_dom), static_cast<unsigned>((rows_below + 127) / 128));
-    trsm_panel_kernel<T><<<gp, 128, 0, stream()>>>(kb, b.ld.data(), b.mat_off.data(), b.mats.data());
+    trsm_panel_kernel<U><<<gp, 128, 0, stream()>>>(kb, b.ld.data(), b.mat_off.data(), b.mats.data());
     PGPU_LAUNCH_CHECK();
     const int rem = nbmax - kb - 1;
     dim3 gs(static_cast<unsigned>(b.n_dom), static_cast<unsigned>(static_cast<Index>(rem) * (rem + 1) / 2));
-    syrk_update_kernel<T><<<gs, 256, 0, stream()>>>(kb, b.ld.data(), b.mat_off.data(), b.mats.data());
+    syrk_update_kernel<U><<<gs, 256, 0, stream()>>>(kb, b.ld.data(), b.mat_off.data(), b.mats.data());
     PGPU_LAUNCH_CHECK();
   }
-  invert_diag_kernel<T><<<dim3(static_cast<unsigned>(b.n_dom), nbmax), 32, 0, stream()>>>(
+  invert_diag_kernel<U><<<dim3(static_cast<unsigned>(b.n_dom), nbmax), 32, 0, stream()>>>(
       b.ld.data(), b.mat_off.data(), b.mats.data());
   PGPU_LAUNCH_CHECK();
 }
@@ -691,34 +798,45 @@ void RasPreconditioner<T>::build_batch(DomainBatch<T>& b, const std::vector<Doma
 template <class T>
 void RasPreconditioner<T>::solve_level(int level, const double* residuals, double* weights) {
   fill(weights, mu_ + l_, 0.0);
-  DomainBatch<T>& b = level == 0 ? coarse_ : *fine_[level];
-  if (b.n_dom == 0) return;
-  const size_t smem = (static_cast<size_t>(b.max_n) + 16 + 64) * sizeof(double);
-  DevBuf<double> cout(32);
-  ProfScope ps(sizeof(T) == 4 ? "ras_solve_f32" : "ras_solve_f64", 2.0 * b.solve_bytes / sizeof(T),
-               b.solve_bytes);
-  ras_solve_kernel<T><<<static_cast<unsigned>(b.n_dom), 256, smem, stream()>>>(
-      b.n.data(), b.ld.data(), b.mat_off.data(), b.mats.data(), b.pt_off.data(), b.pts.data(),
-      b.inner.data(), l_, lagrange_.data(), u_.data(), residuals, weights, level == 0 ? 1 : 0,
-      cout.data());
+  if (level > 0) {
+    DomainBatch<T>& b = *fine_[level];
+    if (b.n_dom == 0) return;
+    const size_t smem = (static_cast<size_t>(b.max_n) + 16 + 64) * sizeof(double);
+    ProfScope ps(sizeof(T) == 4 ? "ras_solve_f32" : "ras_solve_f64",
+                 2.0 * b.solve_bytes / sizeof(T), b.solve_bytes);
+    ras_solve_kernel<T><<<static_cast<unsigned>(b.n_dom), 256, smem, stream()>>>(
+        b.n.data(), b.ld.data(), b.mat_off.data(), b.mats.data(), b.pt_off.data(), b.pts.data(),
+        b.inner.data(), l_, lagrange_.data(), u_.data(), residuals, weights, 0, nullptr);
+    PGPU_LAUNCH_CHECK();
+    return;
+  }
+  // Coarse grid (coarse_grid.hpp:91-131): gamma = (Q^T A Q)^{-1} Q^T d with the explicit FP64
+  // inverse, lambda = Q gamma on every coarse point, then the polynomial coefficients.
+  const int n = coarse_n_, l = l_;
+  const Index* dp = coarse_.pts.data();
+  ProfScope ps("ras_coarse_f64", 2.0 * n * static_cast<double>(n), 8.0 * n * static_cast<double>(n));
+  coarse_rhs_kernel<<<blocks_for(std::max(n, 1), 256), 256, 0, stream()>>>(
+      dp, n, l, lagrange_.data(), residuals, coarse_x_.data(), coarse_out_.data() + 32);
   PGPU_LAUNCH_CHECK();
-  if (level == 0 && l_ > 0) {
+  if (n > 0) {
+    symv_kernel<<<blocks_for(static_cast<Index>(n) * 32, 256), 256, 0, stream()>>>(
+        coarse_inv_.data(), n, coarse_x_.data(), coarse_g_.data());
+    PGPU_LAUNCH_CHECK();
+  }
+  coarse_finish_kernel<<<1, 256, 0, stream()>>>(dp, n, l, lagrange_.data(), u_.data(),
+                                                coarse_g_.data(), weights, coarse_out_.data());
+  PGPU_LAUNCH_CHECK();
+  if (l > 0) {
     // Polynomial part: solve P_top c = d_head - A_top lambda (coarse_grid.hpp:124-127).
-    auto h = cout.to_host();
-    const int l = l_;
-    std::vector<double> dh(l);
-    std::vector<Index> pidx(point_idcs_[0].begin(), point_idcs_[0].begin() + l);
-    DevBuf<Index> dpi;
-    dpi.upload(pidx);
-    DevBuf<double> dd(l);
-    gather(residuals, dpi.data(), l, dd.data());
-    dd.download(dh.data(), l);
+    double h[48];
+    PGPU_CUDA(cudaMemcpyAsync(h, coarse_out_.data(), 48 * sizeof(double), cudaMemcpyDeviceToHost,
+                              stream()));
     sync();
     std::vector<double> rhs(l);
     for (int k = 0; k < l; ++k) {
       double a_lambda = h[16 + k];
       for (int j = 0; j < l; ++j) a_lambda += a11_[k * l + j] * h[j];
-      rhs[k] = dh[k] - a_lambda;
+      rhs[k] = h[32 + k] - a_lambda;
     }
     // c = P_top^{-1} rhs; lagrange_coeffs_ holds P_top^{-1} (row-major).
     std::vector<double> c(l, 0.0);

@@ -53,7 +53,8 @@ class RasPreconditioner {
   void solve_level(int level, const double* residuals, double* weights);
   void update_residuals(int src_level, int trg_level, const double* weights, double* residuals);
   void orthogonalize(double* weights, double* residuals);
-  void build_batch(DomainBatch<T>& b, const std::vector<Domain>& domains);
+  template <class U>
+  void build_batch(DomainBatch<U>& b, const std::vector<Domain>& domains);
   Evaluator<T>& evaluator(int src_level, int trg_level);
 
   ModelDesc model_;
@@ -72,7 +73,11 @@ class RasPreconditioner {
   DevBuf<double> u_;         // mu x l: sum_r K_r(p_k, x_i)
   DevBuf<double> v_;         // mu x l: A11 L_i
   std::vector<std::unique_ptr<DomainBatch<T>>> fine_;  // per level (index 0 unused)
-  DomainBatch<T> coarse_;
+  // The coarse grid is always factorised in FP64 and kept as an explicit inverse.
+  DomainBatch<double> coarse_;
+  DevBuf<double> coarse_inv_;  // n x n
+  int coarse_n_ = 0;
+  DevBuf<double> coarse_x_, coarse_g_, coarse_out_;
   DevBuf<double> p_;   // mu x l orthonormalised monomials (column-major)
   DevBuf<double> ap_;  // mu x l
   std::map<std::pair<int, int>, std::unique_ptr<Evaluator<T>>> evaluators_;
