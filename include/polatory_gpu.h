@@ -149,6 +149,18 @@ int pgpu_evaluator_set_weights(pgpu_evaluator* ev, const double* weights, int64_
 /* out: kn * n_targets values in the caller's target order. */
 int pgpu_evaluator_evaluate(pgpu_evaluator* ev, double* out, int64_t n);
 
+/* Allocation-free direct sums (no counterpart in the reference). For callers whose device
+ * memory is owned and budgeted by their own allocator, so that the library may not allocate:
+ * out[i] = sum_j weights[j] * phi(A (trg_i - src_j)), exact FP64 sums, on the caller's stream
+ * (NULL = legacy default stream). All pointers must be device pointers; nothing is allocated or
+ * copied. Partial sums live in a fixed 16 MiB device array compiled into the library (held by
+ * every GPU that loads it until exit), which limits a call to 2,097,152 targets; larger calls
+ * return PGPU_INVALID_ARGUMENT. The first call on a device looks the array up on that device.
+ * Calls share the array: calls that may overlap on the GPU race and must be serialised. */
+int pgpu_direct_evaluate_noalloc(const pgpu_rbf* rbf, const double* src_points, int64_t n_src,
+                                 const double* weights, const double* trg_points, int64_t n_trg,
+                                 double* out, void* stream);
+
 /* ---- Interpolant (interpolant.hpp:54-218) --------------------------------------------- */
 typedef struct pgpu_interpolant pgpu_interpolant;
 

@@ -90,6 +90,7 @@ def _load():
         "pgpu_evaluator_set_weights": ([P, P, I64], C.c_int),
         "pgpu_evaluator_configure": ([P, C.c_int, C.c_int, C.c_int], C.c_int),
         "pgpu_evaluator_evaluate": ([P, P, I64], C.c_int),
+        "pgpu_direct_evaluate_noalloc": ([C.POINTER(PgpuRbf), P, I64, P, P, I64, P, P], C.c_int),
         "pgpu_interpolant_create": ([C.POINTER(PgpuModel), C.POINTER(P)], C.c_int),
         "pgpu_interpolant_destroy": ([P], C.c_int),
         "pgpu_interpolant_set_precision": ([P, C.c_int], C.c_int),

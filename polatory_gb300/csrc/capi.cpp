@@ -15,6 +15,9 @@
 namespace pgpu {
 void set_device(int device);
 void release_cached_memory();
+int direct_evaluate_noalloc(const pgpu_rbf* rbf, const double* src, int64_t ns,
+                            const double* weights, const double* trg, int64_t nt, double* out,
+                            cudaStream_t st, const char** msg);
 }  // namespace pgpu
 
 using namespace pgpu;
@@ -360,6 +363,19 @@ int pgpu_evaluator_evaluate(pgpu_evaluator* ev, double* out, int64_t n) {
     }
     copy_out(out, ev->out.data(), n);
   });
+}
+
+int pgpu_direct_evaluate_noalloc(const pgpu_rbf* rbf, const double* src_points, int64_t n_src,
+                                 const double* weights, const double* trg_points, int64_t n_trg,
+                                 double* out, void* stream) {
+  // No device allocation on any path (see noalloc.cu); the message string is only written when
+  // the call fails.
+  const char* msg = nullptr;
+  int rc = direct_evaluate_noalloc(rbf, src_points, n_src, weights, trg_points, n_trg, out,
+                                   static_cast<cudaStream_t>(stream), &msg);
+  if (rc != PGPU_OK) g_last_error = msg ? msg : "allocation-free evaluation failed";
+  else g_last_error.clear();
+  return rc;
 }
 
 // ---- interpolant ----------------------------------------------------------------------
