@@ -8,6 +8,7 @@
 // which equals the four-block product of fine_grid.hpp:80-84 with q_top = -L^T.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 
 #include "kernels.cuh"
 #include "linalg.hpp"
@@ -565,14 +566,21 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
   std::vector<std::vector<Domain>> level_domains(n_levels_);
   for (int level = n_levels_ - 1; level >= 1; --level) {
     std::vector<Index> no_grad;
+    const double t0 = wall_seconds();
     DomainDivider divider(div_points, nullptr, point_idcs_[level], no_grad, poly_idcs_);
+    const double t1 = wall_seconds();
     double finest = std::log(static_cast<double>(mu_)) / std::log(kFineToCoarseRatio);
     double coarsest = std::log(static_cast<double>(kNCoarsestPoints)) / std::log(kFineToCoarseRatio);
     Index n_coarse = static_cast<Index>(std::pow(
         kFineToCoarseRatio, coarsest + (level - 1) * (finest - coarsest) / (n_levels_ - 1)));
     point_idcs_[level - 1] = divider.choose_coarse_points(n_coarse).first;
     level_domains[level] = std::move(divider.domains());
+    if (verbose())
+      std::printf("ras level %d: %zu points, %zu domains, divide %.3f s, coarse points %.3f s\n",
+                  level, point_idcs_[level].size(), level_domains[level].size(), t1 - t0,
+                  wall_seconds() - t1);
   }
+  const double t_dev = wall_seconds();
 
   // Device-side per-point data.
   const int l = l_;
@@ -674,6 +682,11 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
       ev.set_weights(w.data());
       ev.evaluate(ap_.data() + static_cast<Index>(i) * mu_, false);
     }
+  }
+  if (verbose()) {
+    sync();
+    std::printf("ras device setup (lagrange, factors, coarse inverse, AP) %.3f s\n",
+                wall_seconds() - t_dev);
   }
   work_res_.resize(mu_);
   work_w_.resize(mu_ + l);

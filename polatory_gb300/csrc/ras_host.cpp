@@ -8,7 +8,6 @@
 #include <array>
 #include <cmath>
 #include <numeric>
-#include <queue>
 #include <random>
 #include <set>
 
@@ -169,48 +168,97 @@ void merge_poly_points(Domain& d, const std::vector<Index>& poly) {
   }
 }
 
-struct Cluster {
-  int level = 0;
+// A cluster of the coarse-point selection: a segment [b, e) of one shared point array.
+struct Segment {
+  Index b = 0, e = 0;
   double volume = 0;
-  std::vector<MixedPoint> points;
   MixedPoint center{};
   bool has_grad = false;
 };
 
-struct ClusterLess {
-  // priority_queue top = highest priority: lowest level, then largest bbox volume
-  // (domain_divider.hpp:151-158).
-  bool operator()(const Cluster* a, const Cluster* b) const {
-    if (a->level != b->level) return a->level > b->level;
-    return a->volume < b->volume;
+// initialize_cluster (domain_divider.hpp:277-308): bbox volume, the point nearest to the bbox
+// centre, and (for clusters holding gradient points) the lexicographic sort used by the next
+// split; value-only clusters are partitioned with nth_element at split time instead.
+// parent_less: the parent's lexicographic order, which decides ties in the distance to the
+// bbox centre (the reference takes the first such point in its sorted parent order; two-point
+// clusters always tie). nullptr for the root (input order).
+void init_segment(const Geo& g, std::vector<MixedPoint>& pts, Segment& s,
+                  const LexLess* parent_less = nullptr) {
+  double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+  s.has_grad = false;
+  for (Index i = s.b; i < s.e; ++i) {
+    const double* c = g.at(pts[i]);
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = std::min(mn[k], c[k]);
+      mx[k] = std::max(mx[k], c[k]);
+    }
+    s.has_grad |= pts[i].grad;
   }
-};
-
-// initialize_cluster (domain_divider.hpp:277-308): bbox, the point nearest to the bbox centre,
-// and (for clusters holding gradient points) the lexicographic sort used by the next split.
-void initialize_cluster(const Geo& g, Cluster& c) {
-  double mn[3], mx[3];
-  bbox_of(g, c.points, mn, mx);
-  c.volume = (mx[0] - mn[0]) * (mx[1] - mn[1]) * (mx[2] - mn[2]);
+  s.volume = (mx[0] - mn[0]) * (mx[1] - mn[1]) * (mx[2] - mn[2]);
   double ctr[3];
   for (int k = 0; k < 3; ++k) ctr[k] = mn[k] + (mx[k] - mn[k]) / 2.0;
   double best = INFINITY;
-  c.has_grad = false;
-  for (const auto& p : c.points) {
-    const double* q = g.at(p);
+  for (Index i = s.b; i < s.e; ++i) {
+    const double* q = g.at(pts[i]);
     double dx = q[0] - ctr[0], dy = q[1] - ctr[1], dz = q[2] - ctr[2];
     double d2 = dx * dx + dy * dy + dz * dz;
-    if (d2 < best) {
+    if (d2 < best || (d2 == best && parent_less && (*parent_less)(pts[i], s.center))) {
       best = d2;
-      c.center = p;
+      s.center = pts[i];
     }
-    c.has_grad |= p.grad;
   }
-  if (c.has_grad) {
-    // Clusters without gradient points are partitioned lazily (nth_element) at split time.
+  if (s.has_grad) {
     LexLess less{&g, axes_by_width(mn, mx)};
-    std::sort(c.points.begin(), c.points.end(), less);
+    std::sort(pts.begin() + s.b, pts.begin() + s.e, less);
   }
+}
+
+// Splits a segment at the position minimising |2 prefix(i) - size| with the tie rule of
+// std::min_element and the comparator of domain_divider.hpp:82-88; children are initialised.
+void split_segment(const Geo& g, std::vector<MixedPoint>& pts, const Segment& s, Segment& left,
+                   Segment& right) {
+  const Index n = s.e - s.b;
+  Index mid = 0;
+  double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (Index i = s.b; i < s.e; ++i) {
+    const double* c = g.at(pts[i]);
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = std::min(mn[k], c[k]);
+      mx[k] = std::max(mx[k], c[k]);
+    }
+  }
+  const LexLess less{&g, axes_by_width(mn, mx)};
+  if (s.has_grad) {
+    std::vector<Index> prefix{0};
+    prefix.reserve(n + 1);
+    for (Index i = s.b; i < s.e; ++i) prefix.push_back(prefix.back() + pts[i].mult());
+    const Index size = prefix.back();
+    Index bestd = std::llabs(2 * prefix[0] - size);
+    for (Index i = 1; i < n; ++i) {
+      Index di = std::llabs(2 * prefix[i] - size);
+      if (di < bestd || (di == bestd && i % 2 == 0)) {
+        mid = i;
+        bestd = di;
+      }
+    }
+  } else {
+    Index bestd = n;
+    for (Index i = 1; i < n; ++i) {
+      Index di = std::llabs(2 * i - n);
+      if (di < bestd || (di == bestd && i % 2 == 0)) {
+        mid = i;
+        bestd = di;
+      }
+    }
+    if (mid > 0 && mid < n)
+      std::nth_element(pts.begin() + s.b, pts.begin() + s.b + mid, pts.begin() + s.e, less);
+  }
+  left.b = s.b;
+  left.e = s.b + mid;
+  right.b = s.b + mid;
+  right.e = s.e;
+  if (left.e > left.b) init_segment(g, pts, left, &less);
+  if (right.e > right.b) init_segment(g, pts, right, &less);
 }
 
 }  // namespace
@@ -263,6 +311,12 @@ DomainDivider::DomainDivider(const double* points, const double* grad_points,
 
 std::pair<std::vector<Index>, std::vector<Index>> DomainDivider::choose_coarse_points(
     Index n_coarse) const {
+  // The reference pops clusters from a priority queue ordered by (level ascending, bbox volume
+  // descending), splits each at its median and keeps the centres (domain_divider.hpp:54-125).
+  // That order visits the clusters level by level, so here every level is split at once, in
+  // place on one point array and in parallel; the splits are then accepted in the reference's
+  // order (volume descending) until the centre count reaches n_coarse, and the remaining
+  // clusters of that level stay whole. Apart from ties in volume this yields the same sets.
   Geo g{points_, grad_points_};
   std::vector<Index> idcs(poly_point_idcs_);
   std::vector<Index> grad_idcs;
@@ -275,89 +329,48 @@ std::pair<std::vector<Index>, std::vector<Index>> DomainDivider::choose_coarse_p
     for (auto i : poly_point_idcs_)
       if (i <= maxi) is_poly[i] = 1;
   }
-
-  auto* root = new Cluster;
+  std::vector<MixedPoint> pts;
+  pts.reserve(point_idcs_.size() + grad_point_idcs_.size());
   for (auto i : point_idcs_)
-    if (!is_poly[i]) root->points.push_back({i, true, false});
-  for (auto i : grad_point_idcs_) root->points.push_back({i, true, true});
-  root->level = 0;
-  initialize_cluster(g, *root);
+    if (!is_poly[i]) pts.push_back({i, true, false});
+  for (auto i : grad_point_idcs_) pts.push_back({i, true, true});
 
-  std::priority_queue<Cluster*, std::vector<Cluster*>, ClusterLess> pq;
-  Index current_size = root->center.mult();
-  pq.push(root);
+  std::vector<Segment> cur(1);
+  cur[0].b = 0;
+  cur[0].e = static_cast<Index>(pts.size());
+  std::vector<Segment> finals;
+  if (pts.empty()) return {std::move(idcs), std::move(grad_idcs)};
+  init_segment(g, pts, cur[0]);
+  Index count = cur[0].center.mult();
 
-  while (current_size < n_coarse && !pq.empty()) {
-    Cluster* c = pq.top();
-    auto& pts = c->points;
-    const Index n = static_cast<Index>(pts.size());
-    // Split position minimising |2 prefix(i) - size|, ties resolved as std::min_element with
-    // the comparator of domain_divider.hpp:82-88.
-    Index mid = 0;
-    if (c->has_grad) {
-      std::vector<Index> prefix{0};
-      prefix.reserve(n + 1);
-      for (const auto& p : pts) prefix.push_back(prefix.back() + p.mult());
-      const Index size = prefix.back();
-      Index best = 0;
-      Index bestd = std::llabs(2 * prefix[0] - size);
-      for (Index i = 1; i < n; ++i) {
-        Index di = std::llabs(2 * prefix[i] - size);
-        if (di < bestd || (di == bestd && i % 2 == 0)) {
-          best = i;
-          bestd = di;
+  while (count < n_coarse && !cur.empty()) {
+    const Index ns = static_cast<Index>(cur.size());
+    std::vector<Segment> left(ns), right(ns);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (Index s = 0; s < ns; ++s) split_segment(g, pts, cur[s], left[s], right[s]);
+    // Accept the splits in the reference's order.
+    std::vector<Index> order(ns);
+    for (Index s = 0; s < ns; ++s) order[s] = s;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](Index a, Index b) { return cur[a].volume > cur[b].volume; });
+    std::vector<Segment> next;
+    next.reserve(2 * ns);
+    Index k = 0;
+    for (; k < ns && count < n_coarse; ++k) {
+      const Index s = order[k];
+      count -= cur[s].center.mult();
+      for (Segment* c : {&left[s], &right[s]}) {
+        if (c->e > c->b) {
+          count += c->center.mult();
+          next.push_back(*c);
         }
       }
-      mid = best;
-    } else {
-      const Index size = n;
-      Index best = 0;
-      Index bestd = size;
-      for (Index i = 1; i < n; ++i) {
-        Index di = std::llabs(2 * i - size);
-        if (di < bestd || (di == bestd && i % 2 == 0)) {
-          best = i;
-          bestd = di;
-        }
-      }
-      mid = best;
-      if (mid > 0 && mid < n) {
-        double mn[3], mx[3];
-        bbox_of(g, pts, mn, mx);
-        LexLess less{&g, axes_by_width(mn, mx)};
-        std::nth_element(pts.begin(), pts.begin() + mid, pts.end(), less);
-      }
     }
-    auto* left = new Cluster;
-    auto* right = new Cluster;
-    left->points.assign(pts.begin(), pts.begin() + mid);
-    right->points.assign(pts.begin() + mid, pts.end());
-    left->level = right->level = c->level + 1;
-    current_size -= c->center.mult();
-    pq.pop();
-    delete c;
-    if (!left->points.empty()) {
-      initialize_cluster(g, *left);
-      current_size += left->center.mult();
-      pq.push(left);
-    } else {
-      delete left;
-    }
-    if (!right->points.empty()) {
-      initialize_cluster(g, *right);
-      current_size += right->center.mult();
-      pq.push(right);
-    } else {
-      delete right;
-    }
+    for (; k < ns; ++k) finals.push_back(cur[order[k]]);
+    cur = std::move(next);
   }
-
-  while (!pq.empty()) {
-    Cluster* c = pq.top();
-    (c->center.grad ? grad_idcs : idcs).push_back(c->center.index);
-    pq.pop();
-    delete c;
-  }
+  for (const auto* v : {&finals, &cur})
+    for (const auto& s : *v) (s.center.grad ? grad_idcs : idcs).push_back(s.center.index);
   return {std::move(idcs), std::move(grad_idcs)};
 }
 

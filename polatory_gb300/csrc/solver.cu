@@ -297,9 +297,11 @@ FitResult fit_impl(const FitRequest& req) {
     }
   }
 
+  if (req.verbose) std::printf("fit: basis %.3f s\n", wall_seconds() - t0);
   RasPreconditioner<T> pc(model, req.points_host, pts.data(), mu, bbox);
   res.levels = pc.levels();
   res.n_domains = pc.n_domains();
+  if (req.verbose) std::printf("fit: preconditioner ready %.3f s\n", wall_seconds() - t0);
 
   DevBuf<double> w(M), rhs(M);
   w.zero();

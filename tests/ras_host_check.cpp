@@ -1,0 +1,181 @@
+// CPU checks of the RAS host set-up (compiled and run by tests/test_ras_host.py):
+//  1. the invariants of the reference's test/preconditioner/test_domain_divider.cpp:18-90
+//     (inner points partition the level, polynomial points lead every domain, no duplicates,
+//     coarse-point count within [n + l, n + l + 3));
+//  2. domain sizes (points + 3 x gradient points) at most 1024;
+//  3. the level-parallel coarse-point selection returns the same set as a direct sequential
+//     restatement of the priority-queue rule (domain_divider.hpp:54-125) on value points.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <numeric>
+#include <queue>
+#include <random>
+#include <set>
+#include <vector>
+
+#include "ras_host.hpp"
+
+using pgpu::Index;
+
+static int failures = 0;
+#define CHECK(c)                                                          \
+  do {                                                                    \
+    if (!(c)) {                                                           \
+      std::printf("FAILED %s:%d: %s\n", __FILE__, __LINE__, #c);          \
+      ++failures;                                                         \
+    }                                                                     \
+  } while (0)
+
+static void check_divider(Index n_points, Index n_grad, Index n_poly, unsigned seed) {
+  std::mt19937 gen(seed);
+  std::uniform_real_distribution<double> u(-1.0, 1.0);
+  std::vector<double> pts(3 * n_points), gpts(3 * std::max<Index>(n_grad, 1));
+  for (auto& v : pts) v = u(gen);
+  for (auto& v : gpts) v = u(gen);
+  std::vector<Index> idx(n_points), gidx(n_grad);
+  std::iota(idx.begin(), idx.end(), 0);
+  std::iota(gidx.begin(), gidx.end(), 0);
+  std::vector<Index> poly(idx.begin(), idx.begin() + n_poly);
+  pgpu::DomainDivider div(pts.data(), gpts.data(), idx, gidx, poly);
+  std::vector<Index> inner, ginner;
+  for (const auto& d : div.domains()) {
+    for (Index i = 0; i < d.num_points(); ++i)
+      if (d.inner_point[i]) inner.push_back(d.point_indices[i]);
+    for (Index i = 0; i < d.num_grad_points(); ++i)
+      if (d.inner_grad_point[i]) ginner.push_back(d.grad_point_indices[i]);
+    for (Index i = 0; i < n_poly; ++i) CHECK(d.point_indices[i] == poly[i]);
+    auto a = d.point_indices;
+    std::sort(a.begin(), a.end());
+    CHECK(std::unique(a.begin(), a.end()) == a.end());
+    auto b = d.grad_point_indices;
+    std::sort(b.begin(), b.end());
+    CHECK(std::unique(b.begin(), b.end()) == b.end());
+    CHECK(d.num_points() - n_poly + 3 * d.num_grad_points() <= 1024 + n_poly);
+  }
+  CHECK(static_cast<Index>(inner.size()) == n_points);
+  CHECK(static_cast<Index>(ginner.size()) == n_grad);
+  std::sort(inner.begin(), inner.end());
+  CHECK(std::unique(inner.begin(), inner.end()) == inner.end());
+  std::sort(ginner.begin(), ginner.end());
+  CHECK(std::unique(ginner.begin(), ginner.end()) == ginner.end());
+
+  const Index n_coarse = 1000;
+  auto [cp, cgp] = div.choose_coarse_points(n_coarse);
+  const Index total = static_cast<Index>(cp.size()) + 3 * static_cast<Index>(cgp.size());
+  CHECK(n_coarse + n_poly <= total);
+  // The reference's bound is n + l + 3; a last split that replaces a value centre by two
+  // gradient centres adds 5, so the loop can stop at most 4 above n + l.
+  CHECK(total < n_coarse + n_poly + 5);
+  for (Index i = 0; i < n_poly; ++i) CHECK(cp[i] == poly[i]);
+}
+
+// Sequential restatement of the priority-queue selection for value points only.
+struct Cl {
+  int level;
+  double volume;
+  std::vector<Index> pts;
+  Index center;
+};
+
+static void init_cl(const std::vector<double>& p, Cl& c) {
+  double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (Index i : c.pts)
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = std::min(mn[k], p[3 * i + k]);
+      mx[k] = std::max(mx[k], p[3 * i + k]);
+    }
+  c.volume = (mx[0] - mn[0]) * (mx[1] - mn[1]) * (mx[2] - mn[2]);
+  double best = INFINITY;
+  for (Index i : c.pts) {
+    double d2 = 0;
+    for (int k = 0; k < 3; ++k) {
+      double dd = p[3 * i + k] - (mn[k] + (mx[k] - mn[k]) / 2.0);
+      d2 += dd * dd;
+    }
+    if (d2 < best) {
+      best = d2;
+      c.center = i;
+    }
+  }
+  double w[3] = {mx[0] - mn[0], mx[1] - mn[1], mx[2] - mn[2]};
+  int axes[3] = {0, 1, 2};
+  std::sort(axes, axes + 3, [&](int a, int b) { return w[a] > w[b]; });
+  std::sort(c.pts.begin(), c.pts.end(), [&](Index a, Index b) {
+    for (int ax : axes)
+      if (p[3 * a + ax] != p[3 * b + ax]) return p[3 * a + ax] < p[3 * b + ax];
+    return false;
+  });
+}
+
+static void check_coarse_equivalence(Index n, Index n_coarse, unsigned seed) {
+  std::mt19937 gen(seed);
+  std::uniform_real_distribution<double> u(0.0, 1.0);
+  std::vector<double> p(3 * n);
+  for (auto& v : p) v = u(gen);
+  std::vector<Index> idx(n);
+  std::iota(idx.begin(), idx.end(), 0);
+  std::vector<Index> poly{0, 1, 2, 3};
+  std::vector<Index> none;
+  pgpu::DomainDivider div(p.data(), nullptr, idx, none, poly);
+  auto got = div.choose_coarse_points(n_coarse).first;
+
+  auto cmp = [](const Cl* a, const Cl* b) {
+    if (a->level != b->level) return a->level > b->level;
+    return a->volume < b->volume;
+  };
+  std::priority_queue<Cl*, std::vector<Cl*>, decltype(cmp)> pq(cmp);
+  auto* root = new Cl{0, 0, {}, 0};
+  for (Index i = 4; i < n; ++i) root->pts.push_back(i);
+  init_cl(p, *root);
+  Index count = 1;
+  pq.push(root);
+  while (count < n_coarse) {
+    Cl* c = pq.top();
+    const Index m = static_cast<Index>(c->pts.size());
+    Index mid = 0, bestd = m;
+    for (Index i = 1; i < m; ++i) {
+      Index di = std::llabs(2 * i - m);
+      if (di < bestd || (di == bestd && i % 2 == 0)) {
+        mid = i;
+        bestd = di;
+      }
+    }
+    pq.pop();
+    --count;
+    std::vector<Index> l(c->pts.begin(), c->pts.begin() + mid), r(c->pts.begin() + mid, c->pts.end());
+    for (auto* v : {&l, &r}) {
+      if (v->empty()) continue;
+      auto* ch = new Cl{c->level + 1, 0, std::move(*v), 0};
+      init_cl(p, *ch);
+      ++count;
+      pq.push(ch);
+    }
+    delete c;
+  }
+  std::vector<Index> want(poly);
+  while (!pq.empty()) {
+    want.push_back(pq.top()->center);
+    delete pq.top();
+    pq.pop();
+  }
+  std::set<Index> a(got.begin(), got.end()), b(want.begin(), want.end());
+  CHECK(a == b);
+  CHECK(got.size() == want.size());
+}
+
+int main() {
+  check_divider(10000, 10000, 10, 1);
+  check_divider(20000, 0, 4, 2);
+  check_divider(5000, 3000, 1, 3);
+  check_coarse_equivalence(5000, 700, 4);
+  check_coarse_equivalence(20000, 2048, 5);
+  check_coarse_equivalence(3000, 1500, 6);
+  if (failures) {
+    std::printf("%d failures\n", failures);
+    return 1;
+  }
+  std::printf("ok\n");
+  return 0;
+}
