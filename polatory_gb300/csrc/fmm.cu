@@ -407,11 +407,11 @@ __global__ void l2l_kernel(Cheb<T> ch, const Index* __restrict__ parent_of,
 // M2L over a tile of kTT target cells: every non-adjacent offset o with at least one source in
 // the tile is applied as a dense (p^3 x p^3) x (p^3 x kTT) product with K_o streamed in 8-row
 // chunks through shared memory; the local expansions stay in registers across all offsets.
-template <int P, class T>
+template <int D, class T>
 __global__ void __launch_bounds__(256)
     m2l_kernel(const T* __restrict__ K, const int* __restrict__ table, Index nt,
                const T* __restrict__ Ms, T* __restrict__ L, int groups, T* __restrict__ part) {
-  constexpr int P3 = P * P * P;
+  constexpr int P3 = D;  // operator dimension: p^3 (dense) or the compressed rank
   constexpr int NC = P3 / 8;  // row chunks
   // blockIdx.y selects a contiguous group of offsets; with several groups each block writes a
   // partial expansion that m2l_reduce_kernel sums in a fixed order.
@@ -469,6 +469,93 @@ __global__ void __launch_bounds__(256)
       T* pg = part + (static_cast<Index>(blockIdx.y) * nt + tt) * P3;
 #pragma unroll
       for (int c = 0; c < NC; ++c) pg[c * 8 + r] = acc[c];
+    }
+  }
+}
+
+// Register-tiled M2L (D = p^3 <= 216). A block owns 64 target cells; thread (ag, tg) owns the
+// RA consecutive rows ag*RA.. of the local expansions of the 4 targets tg*4.., accumulated in
+// registers across every offset. For each offset, K_o is streamed through shared memory in
+// column chunks of BK. The kernels are even (phi(d) = phi(-d)), so column b of K_o is row b of
+// K_{-o} and is read contiguously from the operator of the opposite offset (index 342 - o).
+template <int D, class T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1)
+    m2l_tiled_kernel(const T* __restrict__ K, const int* __restrict__ table, Index nt,
+                     const T* __restrict__ Ms, T* __restrict__ L, int groups, T* __restrict__ part) {
+  constexpr int RA = (D + 15) / 16;
+  constexpr int DP = RA * 16;
+  constexpr int BK = sizeof(T) == 8 ? 8 : ((D % 24 == 0) ? 24 : 16);
+  constexpr int TT = 64;
+  __shared__ __align__(16) T s_kt[BK][DP];
+  __shared__ __align__(16) T s_m[BK][TT];
+  __shared__ int s_src[TT];
+  const int o_beg = static_cast<int>((static_cast<long>(blockIdx.y) * kNOff) / groups);
+  const int o_end = static_cast<int>((static_cast<long>(blockIdx.y + 1) * kNOff) / groups);
+  const Index t0 = static_cast<Index>(blockIdx.x) * TT;
+  const int ag = threadIdx.x >> 4;  // 0..15
+  const int tg = threadIdx.x & 15;  // 0..15
+  T acc[RA][4];
+#pragma unroll
+  for (int i = 0; i < RA; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+  // Padding rows of the operator chunk stay zero.
+  if constexpr (DP > D) {
+    for (int e = threadIdx.x; e < BK * (DP - D); e += blockDim.x)
+      s_kt[e / (DP - D)][D + e % (DP - D)] = T(0);
+  }
+
+  for (int o = o_beg; o < o_end; ++o) {
+    const int ox = o / 49 - 3, oy = (o / 7) % 7 - 3, oz = o % 7 - 3;
+    if (abs(ox) <= 1 && abs(oy) <= 1 && abs(oz) <= 1) continue;
+    __syncthreads();
+    if (threadIdx.x < TT) {
+      const Index tt = t0 + threadIdx.x;
+      s_src[threadIdx.x] = tt < nt ? table[tt * kNOff + o] : -1;
+    }
+    const bool any = __syncthreads_or(threadIdx.x < TT && t0 + threadIdx.x < nt &&
+                                      table[(t0 + threadIdx.x) * kNOff + o] >= 0);
+    if (!any) continue;
+    const T* kt = K + static_cast<Index>(kNOff - 1 - o) * D * D;  // row b of K_{-o} = column b of K_o
+    for (int b0 = 0; b0 < D; b0 += BK) {
+      const int bk = min(BK, D - b0);
+      __syncthreads();
+      for (int e = threadIdx.x; e < bk * D; e += blockDim.x) {
+        const int bb = e / D, a = e % D;
+        s_kt[bb][a] = kt[static_cast<Index>(b0 + bb) * D + a];
+      }
+      for (int e = threadIdx.x; e < bk * TT; e += blockDim.x) {
+        const int t = e / bk, bb = e % bk;
+        const int s = s_src[t];
+        s_m[bb][t] = s >= 0 ? Ms[static_cast<Index>(s) * D + b0 + bb] : T(0);
+      }
+      __syncthreads();
+      for (int bb = 0; bb < bk; ++bb) {
+        T kv[RA];
+#pragma unroll
+        for (int i = 0; i < RA; ++i) kv[i] = s_kt[bb][ag * RA + i];
+        T mv[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) mv[j] = s_m[bb][tg * 4 + j];
+#pragma unroll
+        for (int i = 0; i < RA; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] += kv[i] * mv[j];
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const Index tt = t0 + tg * 4 + j;
+    if (tt >= nt) continue;
+    T* dst = groups == 1 ? L + tt * D : part + (static_cast<Index>(blockIdx.y) * nt + tt) * D;
+#pragma unroll
+    for (int i = 0; i < RA; ++i) {
+      const int a = ag * RA + i;
+      if (a < D) {
+        if (groups == 1) dst[a] += acc[i][j];
+        else dst[a] = acc[i][j];
+      }
     }
   }
 }
@@ -738,10 +825,11 @@ std::mutex g_kcache_mu;
 std::map<KKey, std::shared_ptr<void>> g_kcache;
 
 template <class T>
-std::shared_ptr<DevBuf<T>> m2l_matrices(int kind, const KParams<T>& kp, double r, int p) {
+std::shared_ptr<DevBuf<T>> m2l_matrices(int kind, const KParams<T>& kp, double r, int p,
+                                        bool cache = true) {
   KKey key{kind, static_cast<double>(kp.p0), static_cast<double>(kp.p1), r, p,
            static_cast<int>(sizeof(T))};
-  {
+  if (cache) {
     std::lock_guard<std::mutex> lk(g_kcache_mu);
     auto it = g_kcache.find(key);
     if (it != g_kcache.end()) return std::static_pointer_cast<DevBuf<T>>(it->second);
@@ -758,9 +846,279 @@ std::shared_ptr<DevBuf<T>> m2l_matrices(int kind, const KParams<T>& kp, double r
   });
   PGPU_LAUNCH_CHECK();
   sync();
-  std::lock_guard<std::mutex> lk(g_kcache_mu);
-  g_kcache[key] = buf;
+  if (cache) {
+    std::lock_guard<std::mutex> lk(g_kcache_mu);
+    g_kcache[key] = buf;
+  }
   return buf;
+}
+
+// ---- low-rank M2L (SVD compression of the stacked operators) ------------------------------
+// With K_o ~ U C_o V^T for all offsets o (U, V: the leading left/right singular vectors of the
+// stacked [K_o] matrices), M2L becomes L = U sum_o C_o (V^T M_s): an r x r product per
+// interaction instead of p^3 x p^3, plus one projection per cell on each side.
+
+// Cyclic Jacobi eigen-decomposition of a symmetric n x n matrix (row-major). Eigenvalues are
+// returned in descending order with the eigenvectors as the columns of vecs (row-major).
+void jacobi_eig(int n, std::vector<double> a, std::vector<double>& vals, std::vector<double>& vecs) {
+  std::vector<double> v(static_cast<size_t>(n) * n, 0.0);
+  for (int i = 0; i < n; ++i) v[static_cast<size_t>(i) * n + i] = 1.0;
+  auto A = [&](int i, int j) -> double& { return a[static_cast<size_t>(i) * n + j]; };
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0, diag = 0;
+    for (int i = 0; i < n; ++i) {
+      diag += A(i, i) * A(i, i);
+      for (int j = i + 1; j < n; ++j) off += A(i, j) * A(i, j);
+    }
+    if (off <= 1e-30 * diag || off == 0.0) break;
+    for (int p = 0; p < n - 1; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = A(p, q);
+        if (std::fabs(apq) < 1e-300) continue;
+        const double theta = (A(q, q) - A(p, p)) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; ++k) {  // columns p, q
+          const double akp = A(k, p), akq = A(k, q);
+          A(k, p) = c * akp - s * akq;
+          A(k, q) = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {  // rows p, q
+          const double apk = A(p, k), aqk = A(q, k);
+          A(p, k) = c * apk - s * aqk;
+          A(q, k) = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double vkp = v[static_cast<size_t>(k) * n + p], vkq = v[static_cast<size_t>(k) * n + q];
+          v[static_cast<size_t>(k) * n + p] = c * vkp - s * vkq;
+          v[static_cast<size_t>(k) * n + q] = s * vkp + c * vkq;
+        }
+      }
+  }
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](int x, int y) { return A(x, x) > A(y, y); });
+  vals.resize(n);
+  vecs.assign(static_cast<size_t>(n) * n, 0.0);
+  for (int j = 0; j < n; ++j) {
+    vals[j] = A(order[j], order[j]);
+    for (int i = 0; i < n; ++i) vecs[static_cast<size_t>(i) * n + j] = v[static_cast<size_t>(i) * n + order[j]];
+  }
+}
+
+__device__ __forceinline__ bool adjacent_offset(int o) {
+  const int ox = o / 49 - 3, oy = (o / 7) % 7 - 3, oz = o % 7 - 3;
+  return abs(ox) <= 1 && abs(oy) <= 1 && abs(oz) <= 1;
+}
+
+// G[i][j] = sum_o sum_k A_o[i][k] A_o[j][k] (rows) or sum_o sum_k A_o[k][i] A_o[k][j] (cols).
+__global__ void gram_kernel(const double* __restrict__ K, int n, int cols, double* __restrict__ G) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * n) return;
+  const int i = e / n, j = e % n;
+  if (j < i) return;
+  double s = 0;
+  for (int o = 0; o < kNOff; ++o) {
+    if (adjacent_offset(o)) continue;
+    const double* A = K + static_cast<Index>(o) * n * n;
+    if (cols) {
+      for (int k = 0; k < n; ++k) s += A[static_cast<Index>(k) * n + i] * A[static_cast<Index>(k) * n + j];
+    } else {
+      for (int k = 0; k < n; ++k) s += A[static_cast<Index>(i) * n + k] * A[static_cast<Index>(j) * n + k];
+    }
+  }
+  G[static_cast<Index>(i) * n + j] = s;
+  G[static_cast<Index>(j) * n + i] = s;
+}
+
+// W_o = K_o V (n x r), then C_o = U^T W_o (r x r); U, V row-major n x r.
+__global__ void kv_kernel(const double* __restrict__ K, const double* __restrict__ V, int n, int r,
+                          double* __restrict__ W) {
+  const Index e = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= static_cast<Index>(kNOff) * n * r) return;
+  const int o = static_cast<int>(e / (static_cast<Index>(n) * r));
+  const int a = static_cast<int>((e / r) % n), j = static_cast<int>(e % r);
+  if (adjacent_offset(o)) {
+    W[e] = 0.0;
+    return;
+  }
+  const double* A = K + static_cast<Index>(o) * n * n + static_cast<Index>(a) * n;
+  double s = 0;
+  for (int b = 0; b < n; ++b) s += A[b] * V[static_cast<Index>(b) * r + j];
+  W[e] = s;
+}
+
+template <class T>
+__global__ void ukv_kernel(const double* __restrict__ W, const double* __restrict__ U, int n, int r,
+                           double scale, T* __restrict__ C) {
+  const Index e = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= static_cast<Index>(kNOff) * r * r) return;
+  const int o = static_cast<int>(e / (static_cast<Index>(r) * r));
+  const int i = static_cast<int>((e / r) % r), j = static_cast<int>(e % r);
+  const double* Wo = W + static_cast<Index>(o) * n * r;
+  double s = 0;
+  for (int a = 0; a < n; ++a) s += U[static_cast<Index>(a) * r + i] * Wo[static_cast<Index>(a) * r + j];
+  C[e] = static_cast<T>(scale * s);
+}
+
+// Mt[c][j] = sum_b M[c][b] V[b][j]  (one block per cell, threads over j)
+template <class T>
+__global__ void compress_kernel(const T* __restrict__ M, const T* __restrict__ V, int n, int r,
+                                T* __restrict__ Mt) {
+  extern __shared__ unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  const Index c = blockIdx.x;
+  for (int b = threadIdx.x; b < n; b += blockDim.x) sm[b] = M[c * n + b];
+  __syncthreads();
+  for (int j = threadIdx.x; j < r; j += blockDim.x) {
+    T s = T(0);
+    for (int b = 0; b < n; ++b) s += sm[b] * V[static_cast<Index>(b) * r + j];
+    Mt[c * r + j] = s;
+  }
+}
+
+// L[c][a] += sum_j U[a][j] Lt[c][j]  (one block per cell, threads over a)
+template <class T>
+__global__ void expand_kernel(const T* __restrict__ Lt, const T* __restrict__ U, int n, int r,
+                              T* __restrict__ L) {
+  extern __shared__ unsigned char smem_raw[];
+  T* sl = reinterpret_cast<T*>(smem_raw);
+  const Index c = blockIdx.x;
+  for (int j = threadIdx.x; j < r; j += blockDim.x) sl[j] = Lt[c * r + j];
+  __syncthreads();
+  for (int a = threadIdx.x; a < n; a += blockDim.x) {
+    T s = T(0);
+    for (int j = 0; j < r; ++j) s += U[static_cast<Index>(a) * r + j] * sl[j];
+    L[c * n + a] += s;
+  }
+}
+
+// Ranks the compressed kernel is instantiated for (multiples of 16; zero-padded bases).
+constexpr int kRanks[] = {16, 32, 48, 64, 80, 96, 112, 128};
+
+template <class T>
+struct M2LOps {
+  int n = 0;  // p^3
+  int r = 0;  // padded rank; 0 = dense operators in K
+  std::shared_ptr<DevBuf<T>> K;
+  DevBuf<T> U, V, C;
+};
+
+struct SvdBasis {
+  int r = 0;
+  std::vector<double> U, V;  // n x r row-major
+};
+
+std::mutex g_ops_mu;
+std::map<std::tuple<int, double, double, double, int, int, double>, std::shared_ptr<void>> g_ops;
+std::map<std::tuple<int, double, double, double, int, double>, std::shared_ptr<SvdBasis>> g_basis;
+
+// Homogeneous kernels (phi(s d) = s^deg phi(d)): the singular vectors do not depend on the cell
+// radius and C_o scales by r^deg. Returns deg, or -1.
+int homogeneity_degree(int kind, double c) {
+  if (c != 0.0) return -1;
+  if (kind == PGPU_RBF_BH3) return 1;
+  if (kind == PGPU_RBF_TH3) return 3;
+  return -1;
+}
+
+template <class T>
+std::shared_ptr<M2LOps<T>> m2l_ops(int kind, const KParams<T>& kp, double r_cell, int p, double eps) {
+  const int n = p * p * p;
+  const double c = static_cast<double>(kp.p1);
+  const int deg = homogeneity_degree(kind, c);
+  auto key = std::make_tuple(kind, static_cast<double>(kp.p0), c, r_cell, p,
+                             static_cast<int>(sizeof(T)), eps);
+  {
+    std::lock_guard<std::mutex> lk(g_ops_mu);
+    auto it = g_ops.find(key);
+    if (it != g_ops.end()) return std::static_pointer_cast<M2LOps<T>>(it->second);
+  }
+  auto ops = std::make_shared<M2LOps<T>>();
+  ops->n = n;
+  if (eps <= 0.0 || p > 6) {
+    ops->K = m2l_matrices<T>(kind, kp, r_cell, p);
+  } else {
+    // Radius at which the operators are computed (1 for homogeneous kernels, then scaled).
+    const double r0 = deg >= 0 ? 1.0 : r_cell;
+    const double scale = deg >= 0 ? std::pow(r_cell, deg) : 1.0;
+    KParams<double> kd{static_cast<double>(kp.p0), c};
+    auto K64 = m2l_matrices<double>(kind, kd, r0, p, /*cache=*/false);
+    auto bkey = std::make_tuple(kind, static_cast<double>(kp.p0), c, deg >= 0 ? -1.0 : r_cell, p, eps);
+    std::shared_ptr<SvdBasis> basis;
+    {
+      std::lock_guard<std::mutex> lk(g_ops_mu);
+      auto it = g_basis.find(bkey);
+      if (it != g_basis.end()) basis = it->second;
+    }
+    if (!basis) {
+      basis = std::make_shared<SvdBasis>();
+      DevBuf<double> g(static_cast<size_t>(n) * n);
+      std::vector<double> gu, gv, vals_u, vals_v, vec_u, vec_v;
+      gram_kernel<<<blocks_for(static_cast<Index>(n) * n, 128), 128, 0, stream()>>>(K64->data(), n, 0, g.data());
+      PGPU_LAUNCH_CHECK();
+      gu = g.to_host();
+      gram_kernel<<<blocks_for(static_cast<Index>(n) * n, 128), 128, 0, stream()>>>(K64->data(), n, 1, g.data());
+      PGPU_LAUNCH_CHECK();
+      gv = g.to_host();
+      jacobi_eig(n, gu, vals_u, vec_u);
+      jacobi_eig(n, gv, vals_v, vec_v);
+      // Smallest rank whose discarded energy is below eps^2 of the total, on both sides.
+      auto rank_of = [&](const std::vector<double>& vals) {
+        double tot = 0;
+        for (double v : vals) tot += std::max(v, 0.0);
+        double tail = tot;
+        int r = 0;
+        while (r < n && tail > eps * eps * tot) tail -= std::max(vals[r++], 0.0);
+        return r;
+      };
+      int r = std::max(rank_of(vals_u), rank_of(vals_v));
+      int rp = 0;
+      for (int cand : kRanks)
+        if (cand >= r) {
+          rp = cand;
+          break;
+        }
+      if (rp == 0 || rp >= n) {
+        basis->r = 0;  // no useful compression
+      } else {
+        basis->r = rp;
+        basis->U.assign(static_cast<size_t>(n) * rp, 0.0);
+        basis->V.assign(static_cast<size_t>(n) * rp, 0.0);
+        for (int a = 0; a < n; ++a)
+          for (int j = 0; j < std::min(r, rp); ++j) {
+            basis->U[static_cast<size_t>(a) * rp + j] = vec_u[static_cast<size_t>(a) * n + j];
+            basis->V[static_cast<size_t>(a) * rp + j] = vec_v[static_cast<size_t>(a) * n + j];
+          }
+      }
+      std::lock_guard<std::mutex> lk(g_ops_mu);
+      g_basis[bkey] = basis;
+    }
+    if (basis->r == 0) {
+      ops->K = m2l_matrices<T>(kind, kp, r_cell, p);
+    } else {
+      const int r = basis->r;
+      ops->r = r;
+      DevBuf<double> du, dv, w(static_cast<size_t>(kNOff) * n * r);
+      du.upload(basis->U);
+      dv.upload(basis->V);
+      const Index nw = static_cast<Index>(kNOff) * n * r;
+      kv_kernel<<<blocks_for(nw, 256), 256, 0, stream()>>>(K64->data(), dv.data(), n, r, w.data());
+      PGPU_LAUNCH_CHECK();
+      ops->C.resize(static_cast<size_t>(kNOff) * r * r);
+      const Index nc = static_cast<Index>(kNOff) * r * r;
+      ukv_kernel<T><<<blocks_for(nc, 256), 256, 0, stream()>>>(w.data(), du.data(), n, r, scale,
+                                                                ops->C.data());
+      PGPU_LAUNCH_CHECK();
+      std::vector<T> hu(basis->U.begin(), basis->U.end()), hv(basis->V.begin(), basis->V.end());
+      ops->U.upload(hu);
+      ops->V.upload(hv);
+      sync();
+    }
+  }
+  std::lock_guard<std::mutex> lk(g_ops_mu);
+  g_ops[key] = ops;
+  return ops;
 }
 
 int order_for_accuracy(double accuracy) {
@@ -795,8 +1153,8 @@ struct Fmm<T>::Impl {
   // M2L tables per level (target cells x 343) and P2P table (target leaves x 27).
   std::vector<DevBuf<int>> m2l_table;
   DevBuf<int> p2p_table;
-  std::vector<std::shared_ptr<DevBuf<T>>> kmats;
-  std::vector<DevBuf<T>> M, L;
+  std::vector<std::shared_ptr<M2LOps<T>>> kmats;
+  std::vector<DevBuf<T>> M, L, Mt, Lt;  // Mt/Lt: compressed expansions (rank r) when used
   DevBuf<T> sw;
   Index near_pairs = 0;
   std::vector<Index> m2l_pairs;  // interactions per level
@@ -856,7 +1214,15 @@ struct Fmm<T>::Impl {
         m2l_pairs[k] = s;
       }
       const double r = box.width / static_cast<double>(1 << k) / 2.0;
-      kmats[k] = m2l_matrices<T>(kind, kp, r, p);
+      // Dense operators by default. PGPU_M2L_EPS > 0 selects low-rank operators whose discarded
+      // singular values carry at most eps^2 of the stacked operators' energy; at the accuracy the
+      // fits need (eps <= 1e-8 with order 6) the rank exceeds 128 and nothing is gained.
+      static const double env_eps = std::getenv("PGPU_M2L_EPS") ? std::atof(std::getenv("PGPU_M2L_EPS")) : 0.0;
+      const double eps = env_eps;
+      kmats[k] = m2l_ops<T>(kind, kp, r, p, eps);
+      if (verbose() && k == lf)
+        std::printf("fmm: n %ld -> lf %d, p %d, m2l rank %d\n", static_cast<long>(ns), lf, p,
+                    kmats[k]->r);
     }
     const Index ntl = tt.ncell[lf];
     p2p_table.resize(std::max<Index>(ntl, 1) * 27);
@@ -880,12 +1246,61 @@ struct Fmm<T>::Impl {
     L.clear();
     M.resize(lf + 1);
     L.resize(lf + 1);
+    Mt.clear();
+    Lt.clear();
+    Mt.resize(lf + 1);
+    Lt.resize(lf + 1);
     for (int k = 2; k <= lf; ++k) {
       M[k].resize(std::max<Index>(src.ncell[k], 1) * p3);
       L[k].resize(std::max<Index>(tt.ncell[k], 1) * p3);
+      if (kmats[k]->r > 0) {
+        Mt[k].resize(std::max<Index>(src.ncell[k], 1) * kmats[k]->r);
+        Lt[k].resize(std::max<Index>(tt.ncell[k], 1) * kmats[k]->r);
+      }
     }
     sw.resize(std::max<Index>(ns, 1));
     built = true;
+  }
+
+  // One M2L pass over level k with operators of dimension D (p^3 dense or the compressed rank):
+  // tiles of kTT target cells; when the tiles are few, the offsets are split over blockIdx.y and
+  // the partial expansions summed in a fixed order.
+  template <int D>
+  void m2l_apply(const T* K, const T* Min, T* Lout, Index n_t, int k, cudaStream_t st) {
+    if constexpr (D == 64 || D == 216) {
+      constexpr int TT = 64;
+      const Index tiles = (n_t + TT - 1) / TT;
+      int groups = static_cast<int>(
+          std::min<Index>(16, std::max<Index>(1, (2 * num_sms() + tiles - 1) / tiles)));
+      DevBuf<T> part;
+      if (groups > 1) part.resize(static_cast<size_t>(groups) * n_t * D);
+      m2l_tiled_kernel<D, T><<<dim3(static_cast<unsigned>(tiles), groups), 256, 0, st>>>(
+          K, m2l_table[k].data(), n_t, Min, Lout, groups, part.data());
+      PGPU_LAUNCH_CHECK();
+      if (groups > 1) {
+        const Index n = n_t * D;
+        m2l_reduce_kernel<T><<<blocks_for(n, 256), 256, 0, st>>>(part.data(), groups, n, Lout);
+        PGPU_LAUNCH_CHECK();
+      }
+      return;
+    }
+    const size_t smem = (static_cast<size_t>(D) * (kTT + 1) + 8 * D) * sizeof(T);
+    auto kern = m2l_kernel<D, T>;
+    PGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(smem)));
+    const Index tiles = (n_t + kTT - 1) / kTT;
+    int groups = static_cast<int>(
+        std::min<Index>(16, std::max<Index>(1, (2 * num_sms() + tiles - 1) / tiles)));
+    DevBuf<T> part;
+    if (groups > 1) part.resize(static_cast<size_t>(groups) * n_t * D);
+    kern<<<dim3(static_cast<unsigned>(tiles), groups), 256, smem, st>>>(
+        K, m2l_table[k].data(), n_t, Min, Lout, groups, part.data());
+    PGPU_LAUNCH_CHECK();
+    if (groups > 1) {
+      const Index n = n_t * D;
+      m2l_reduce_kernel<T><<<blocks_for(n, 256), 256, 0, st>>>(part.data(), groups, n, Lout);
+      PGPU_LAUNCH_CHECK();
+    }
   }
 
   template <int P>
@@ -923,25 +1338,43 @@ struct Fmm<T>::Impl {
         PGPU_LAUNCH_CHECK();
       }
       if (src.ncell[k] > 0) {
-        ProfScope ps(f32 ? "fmm_m2l_f32" : "fmm_m2l_f64",
-                     2.0 * P3 * P3 * static_cast<double>(m2l_pairs[k]));
-        auto kern = m2l_kernel<P, T>;
-        PGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(smem)));
-        // Enough blocks to fill the GPU about twice: split the offsets when the tiles are few.
-        const Index tiles = (n_t + kTT - 1) / kTT;
-        int groups = static_cast<int>(
-            std::min<Index>(16, std::max<Index>(1, (2 * num_sms() + tiles - 1) / tiles)));
-        DevBuf<T> part;
-        if (groups > 1) part.resize(static_cast<size_t>(groups) * n_t * P3);
-        kern<<<dim3(static_cast<unsigned>(tiles), groups), 256, smem, st>>>(
-            kmats[k]->data(), m2l_table[k].data(), n_t, M[k].data(), L[k].data(), groups,
-            part.data());
-        PGPU_LAUNCH_CHECK();
-        if (groups > 1) {
-          const Index n = n_t * P3;
-          m2l_reduce_kernel<T><<<blocks_for(n, 256), 256, 0, st>>>(part.data(), groups, n, L[k].data());
-          PGPU_LAUNCH_CHECK();
+        const M2LOps<T>& ops = *kmats[k];
+        if (ops.r == 0) {
+          ProfScope ps(f32 ? "fmm_m2l_f32" : "fmm_m2l_f64",
+                       2.0 * P3 * P3 * static_cast<double>(m2l_pairs[k]));
+          (void)smem;
+          m2l_apply<P3>(ops.K->data(), M[k].data(), L[k].data(), n_t, k, st);
+        } else {
+          const int r = ops.r;
+          const Index ns_k = src.ncell[k];
+          {
+            ProfScope ps(f32 ? "fmm_m2l_proj_f32" : "fmm_m2l_proj_f64",
+                         2.0 * P3 * r * static_cast<double>(ns_k + n_t));
+            compress_kernel<T><<<static_cast<unsigned>(ns_k), 128, P3 * sizeof(T), st>>>(
+                M[k].data(), ops.V.data(), P3, r, Mt[k].data());
+            PGPU_LAUNCH_CHECK();
+          }
+          {
+            ProfScope ps(f32 ? "fmm_m2l_f32" : "fmm_m2l_f64",
+                         2.0 * r * r * static_cast<double>(m2l_pairs[k]));
+            PGPU_CUDA(cudaMemsetAsync(Lt[k].data(), 0, n_t * r * sizeof(T), st));
+            switch (r) {
+              case 16: m2l_apply<16>(ops.C.data(), Mt[k].data(), Lt[k].data(), n_t, k, st); break;
+              case 32: m2l_apply<32>(ops.C.data(), Mt[k].data(), Lt[k].data(), n_t, k, st); break;
+              case 48: m2l_apply<48>(ops.C.data(), Mt[k].data(), Lt[k].data(), n_t, k, st); break;
+              case 64: m2l_apply<64>(ops.C.data(), Mt[k].data(), Lt[k].data(), n_t, k, st); break;
+              case 80: m2l_apply<80>(ops.C.data(), Mt[k].data(), Lt[k].data(), n_t, k, st); break;
+              case 96: m2l_apply<96>(ops.C.data(), Mt[k].data(), Lt[k].data(), n_t, k, st); break;
+              case 112: m2l_apply<112>(ops.C.data(), Mt[k].data(), Lt[k].data(), n_t, k, st); break;
+              default: m2l_apply<128>(ops.C.data(), Mt[k].data(), Lt[k].data(), n_t, k, st); break;
+            }
+          }
+          {
+            ProfScope ps(f32 ? "fmm_m2l_proj_f32" : "fmm_m2l_proj_f64", 0.0);
+            expand_kernel<T><<<static_cast<unsigned>(n_t), 128, r * sizeof(T), st>>>(
+                Lt[k].data(), ops.U.data(), P3, r, L[k].data());
+            PGPU_LAUNCH_CHECK();
+          }
         }
       }
     }

@@ -57,7 +57,8 @@ def test_fit_c1_two_levels(precision):
     assert stats["iterations"] <= 60
     q = grid[::97]
     got, want = check_fit(interp, model, pts, vals, tol, q)
-    assert np.max(np.abs(got - want)) <= (1e-9 if precision == pg.PLAIN else 1e-5)
+    # The mixed path evaluates in FP32 (FP64 accumulation) and targets 1e-4 absolute accuracy.
+    assert np.max(np.abs(got - want)) <= (1e-9 if precision == pg.PLAIN else 5e-5)
 
 
 def test_fit_covariance_with_nugget():
