@@ -296,6 +296,10 @@ def main():
                 "setup_s": stats["setup_seconds"], "solve_s": stats["solve_seconds"],
                 "n_domains": stats["n_domains"]},
         "profile_ms": {k: round(v["ms"], 3) for k, v in sorted(report.items(), key=lambda kv: -kv[1]["ms"])},
+        "profile_rate": {k: {"calls": v["calls"],
+                             "tflops": round(v["flops"] / (v["ms"] * 1e-3) / 1e12, 3) if v["ms"] > 0 else None,
+                             "gbs": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1) if v["ms"] > 0 else None}
+                         for k, v in report.items()},
     }
     print(json.dumps(line), flush=True)
 

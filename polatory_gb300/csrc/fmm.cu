@@ -624,17 +624,33 @@ __global__ void __launch_bounds__(128)
   if (threadIdx.x < 27) s_nb[threadIdx.x] = table[leaf * 27 + threadIdx.x];
   __syncthreads();
   const Index tb = tleaf_start[leaf], te = tleaf_start[leaf + 1];
-  for (Index i0 = tb; i0 < te; i0 += blockDim.x) {
-    const Index i = i0 + threadIdx.x;
-    const bool active = i < te;
-    const P4<T> t = active ? tpos[i] : P4<T>{T(0), T(0), T(0), T(0)};
-    double tot = 0;
+  // NT targets per thread (1 or 2, uniform over the block): each source read from shared memory
+  // serves NT targets.
+  auto pass = [&]<int NT>(Index i0) {
+    P4<T> t[NT];
+    bool active[NT];
+#pragma unroll
+    for (int q = 0; q < NT; ++q) {
+      const Index i = i0 + threadIdx.x + q * blockDim.x;
+      active[q] = i < te;
+      t[q] = active[q] ? tpos[i] : P4<T>{T(0), T(0), T(0), T(0)};
+    }
+    double tot[NT];
+#pragma unroll
+    for (int q = 0; q < NT; ++q) tot[q] = 0;
     for (int nb = 0; nb < 27; ++nb) {
       const int s = s_nb[nb];
       if (s < 0) continue;
-      const T tx = t.x - static_cast<T>(nb / 9 - 1) * wleaf;
-      const T ty = t.y - static_cast<T>((nb / 3) % 3 - 1) * wleaf;
-      const T tz = t.z - static_cast<T>(nb % 3 - 1) * wleaf;
+      const T ox = static_cast<T>(nb / 9 - 1) * wleaf;
+      const T oy = static_cast<T>((nb / 3) % 3 - 1) * wleaf;
+      const T oz = static_cast<T>(nb % 3 - 1) * wleaf;
+      T tx[NT], ty[NT], tz[NT];
+#pragma unroll
+      for (int q = 0; q < NT; ++q) {
+        tx[q] = t[q].x - ox;
+        ty[q] = t[q].y - oy;
+        tz[q] = t[q].z - oz;
+      }
       const Index sb = sleaf_start[s], se = sleaf_start[s + 1];
       for (Index base = sb; base < se; base += 128) {
         const int cnt = static_cast<int>(min(static_cast<Index>(128), se - base));
@@ -645,17 +661,34 @@ __global__ void __launch_bounds__(128)
           s_p[threadIdx.x] = p;
         }
         __syncthreads();
-        T acc = T(0);
+        T acc[NT];
+#pragma unroll
+        for (int q = 0; q < NT; ++q) acc[q] = T(0);
 #pragma unroll 4
         for (int j = 0; j < cnt; ++j) {
           const P4<T> s4 = s_p[j];
-          const T dx = tx - s4.x, dy = ty - s4.y, dz = tz - s4.z;
-          acc += rbf_value<KIND>(dx * dx + dy * dy + dz * dz, kp) * s4.w;
+#pragma unroll
+          for (int q = 0; q < NT; ++q) {
+            const T dx = tx[q] - s4.x, dy = ty[q] - s4.y, dz = tz[q] - s4.z;
+            acc[q] += rbf_value_fast<KIND>(dx * dx + dy * dy + dz * dz, kp) * s4.w;
+          }
         }
-        tot += static_cast<double>(acc);
+#pragma unroll
+        for (int q = 0; q < NT; ++q) tot[q] += static_cast<double>(acc[q]);
       }
     }
-    if (active) out[tperm[i]] += tot;
+#pragma unroll
+    for (int q = 0; q < NT; ++q)
+      if (active[q]) out[tperm[i0 + threadIdx.x + q * blockDim.x]] += tot[q];
+  };
+  for (Index i0 = tb; i0 < te;) {
+    if (te - i0 > static_cast<Index>(blockDim.x)) {
+      pass.template operator()<2>(i0);
+      i0 += 2 * blockDim.x;
+    } else {
+      pass.template operator()<1>(i0);
+      i0 += blockDim.x;
+    }
   }
 }
 
@@ -1270,8 +1303,9 @@ struct Fmm<T>::Impl {
     if constexpr (D == 64 || D == 216) {
       constexpr int TT = 64;
       const Index tiles = (n_t + TT - 1) / TT;
+      // Two blocks fit per SM: aim for at least four waves so the last one is a small fraction.
       int groups = static_cast<int>(
-          std::min<Index>(16, std::max<Index>(1, (2 * num_sms() + tiles - 1) / tiles)));
+          std::min<Index>(16, std::max<Index>(1, (8 * num_sms() + tiles - 1) / tiles)));
       DevBuf<T> part;
       if (groups > 1) part.resize(static_cast<size_t>(groups) * n_t * D);
       m2l_tiled_kernel<D, T><<<dim3(static_cast<unsigned>(tiles), groups), 256, 0, st>>>(
