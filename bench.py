@@ -41,7 +41,89 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the default sizes")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--workload", choices=["c2", "c1", "c3", "c4"], default="c2",
+                    help="c2: surface fit (default, the headline); c1: 10k cube fit + 64^3 grid; "
+                         "c3: 500k kriging fit + 10M queries; c4: 4096 uneven batched fits")
     return ap.parse_args()
+
+
+def run_other(args):
+    """Secondary configurations: one JSON line each, same timing rules (device time on the
+    library stream, inputs resident on the device except for the batched fits, whose API takes
+    host arrays)."""
+    import torch
+
+    import polatory_gb300 as pg
+    from polatory_gb300 import workloads
+
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.ExternalStream(pg.stream_handle(), device=dev)
+    s = args.scale
+    if args.workload == "c4":
+        fits = workloads.c4(n_fits=max(8, int(4096 * s)))
+        model = pg.Model(pg.Triharmonic3D([1.0]), 1)
+        probs = [(p, v, q) for p, v, q in fits]
+        units = sum(p.shape[0] + q.shape[0] for p, v, q in fits)
+        cfg = {"workload": f"{len(fits)} uneven fits, N log-uniform 200..20000 (sum {units}), "
+                           "triharmonic3d degree 1, tol 1e-5, 4096 queries each",
+               "n_fits": len(fits)}
+        prec = pg.MIXED
+
+        def step():
+            return pg.fit_batch(model, probs, 1e-5, precision=prec, return_weights=False)
+    else:
+        if args.workload == "c1":
+            pts, vals, q = workloads.c1()
+            model = pg.Model(pg.Biharmonic3D([1.0]), 1)
+            tol = 1e-5
+            cfg = {"workload": "10000 uniform points, biharmonic3d degree 1, tol 1e-5, 64^3 grid"}
+        else:
+            n = max(10000, int(500_000 * s))
+            pts, vals, q, aniso = workloads.c3(n=n, n_eval=max(10000, int(10_000_000 * s)))
+            rbf = pg.CovExponential([1.0, 0.2])
+            rbf.anisotropy = aniso  # diag(1, 1, 2): range scale 1:1:0.5
+            model = pg.Model(rbf, 0)
+            model.nugget = 1e-3
+            tol = 1e-4
+            cfg = {"workload": f"{n} GMM points, cov_exponential range 0.2 aniso 1:1:0.5, nugget "
+                               f"1e-3, degree 0, tol 1e-4, {q.shape[0]} uniform queries"}
+        units = pts.shape[0] + q.shape[0]
+        pts_d = torch.from_numpy(pts).to(dev)
+        vals_d = torch.from_numpy(vals).to(dev)
+        q_d = torch.from_numpy(q).to(dev)
+        out_d = torch.empty(q.shape[0], dtype=torch.float64, device=dev)
+        interp = pg.Interpolant(model, pg.MIXED)
+
+        def step():
+            interp.fit_device(pts_d, vals_d, tol)
+            interp.evaluate_device(q_d, out_d)
+            return interp.fit_stats
+    for _ in range(args.warmup):
+        step()
+    pg.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        info = step()
+    ev1.record(stream)
+    pg.synchronize()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ms = ev0.elapsed_time(ev1) if args.workload != "c4" else wall * 1e3
+    line = {"metric": f"{args.workload} fit+eval points/s (mixed precision)", "value": units * args.steps / (ms * 1e-3),
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "data": "synthetic",
+            "config": cfg}
+    if args.workload == "c4":
+        its = [r["iterations"] for r in info]
+        line["fit"] = {"iterations_mean": float(np.mean(its)), "iterations_max": int(max(its)),
+                       "failed": int(sum(r["status"] != 0 for r in info)),
+                       "timing": "host wall clock (batched API takes host arrays)"}
+    else:
+        line["fit"] = info
+    print(json.dumps(line), flush=True)
 
 
 def workload(scale: float):
@@ -175,6 +257,9 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload != "c2":
+        run_other(args)
         return
     import torch
 

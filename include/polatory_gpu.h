@@ -205,6 +205,75 @@ int pgpu_interpolant_centers(const pgpu_interpolant* it, double* centers, double
 int pgpu_interpolant_bbox(const pgpu_interpolant* it, double bbox[6]);
 int pgpu_interpolant_fit_stats(const pgpu_interpolant* it, pgpu_fit_stats* out);
 
+/* ---- batched fits (no single reference counterpart: Interpolant::fit over many problems) --- */
+/* One independent fit (+ optional evaluation). Inputs are host or device pointers; outputs are
+ * written where the pointers point. status receives the PGPU_* code of this fit. */
+typedef struct pgpu_fit_problem {
+  const double* points;     /* n x 3 */
+  int64_t n;
+  const double* values;     /* n */
+  double tolerance;
+  int32_t max_iter;
+  int32_t iterations;       /* out */
+  const double* eval_points; /* m x 3, may be NULL */
+  int64_t m;
+  double* eval_out;         /* m, may be NULL */
+  double* weights_out;      /* n + l, may be NULL */
+  double residual;          /* out: inf-norm residual at the data points */
+  int32_t status;           /* out */
+  int32_t reserved;
+} pgpu_fit_problem;
+
+/* Fits every problem with the same model. Problems are taken largest first by n_workers host
+ * threads (0 = automatic), each with its own CUDA stream, so independent fits overlap on the
+ * GPU. Returns PGPU_OK when every problem succeeded, otherwise the first failing status (each
+ * problem's own status is in its struct). */
+int pgpu_fit_batch(const pgpu_model* model, int precision, pgpu_fit_problem* problems,
+                   int64_t n_problems, int n_workers);
+
+/* ---- serving (no reference counterpart) ----------------------------------------------- */
+/* A request loop over fit and evaluate requests with continuous batching: requests are
+ * admitted in arrival order as worker slots and HBM budget free up (a later request that fits
+ * may start before an earlier one that does not); admitted requests run concurrently, each on
+ * its worker's CUDA stream. Fitted models stay resident on the device in numbered slots;
+ * evaluate requests against a slot wait for that slot's fit. The caller keeps every buffer of a
+ * request alive until the request completes. */
+typedef struct pgpu_server pgpu_server;
+
+enum { PGPU_REQUEST_FIT = 0, PGPU_REQUEST_EVALUATE = 1 };
+
+typedef struct pgpu_request {
+  int32_t kind;          /* PGPU_REQUEST_FIT or PGPU_REQUEST_EVALUATE */
+  int32_t slot;          /* model slot written by a fit / read by an evaluation */
+  const pgpu_model* model; /* fit only (copied at submit) */
+  const double* points;  /* fit: data points; evaluate: query points (n x 3) */
+  int64_t n;
+  const double* values;  /* fit only */
+  double tolerance;      /* fit only */
+  int32_t max_iter;      /* fit only */
+  int32_t precision;     /* PGPU_PRECISION_* */
+  double* out;           /* evaluate: n values */
+} pgpu_request;
+
+typedef struct pgpu_server_stats {
+  int64_t submitted, completed, failed, rejected, in_flight, queued;
+  int64_t bytes_in_use, peak_bytes, budget_bytes;
+} pgpu_server_stats;
+
+/* n_workers: concurrent requests (0 = 8); hbm_budget_bytes: admission budget (0 = 150 GB). */
+int pgpu_server_create(int n_workers, int64_t hbm_budget_bytes, pgpu_server** out);
+int pgpu_server_destroy(pgpu_server* s);
+/* Queues a request; returns a ticket. PGPU_REJECTED when its estimated device memory alone
+ * exceeds the budget. */
+int pgpu_server_submit(pgpu_server* s, const pgpu_request* req, int64_t* ticket);
+/* done = 1 once the request has finished; status is its PGPU_* code and latency the seconds
+ * from submit to completion. */
+int pgpu_server_poll(pgpu_server* s, int64_t ticket, int* done, int* status, double* latency);
+int pgpu_server_wait(pgpu_server* s, int64_t ticket, int* status, double* latency);
+int pgpu_server_stats_get(pgpu_server* s, pgpu_server_stats* out);
+/* Estimated device bytes the server charges against the budget for a request. */
+int64_t pgpu_server_estimate_bytes(const pgpu_request* req);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

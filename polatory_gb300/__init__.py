@@ -19,7 +19,7 @@ __all__ = [
     "CovGeneralizedCauchy3", "CovGeneralizedCauchy5", "CovGeneralizedCauchy7",
     "CovGeneralizedCauchy9", "CovSpherical", "CovSpheroidal3", "CovSpheroidal5",
     "CovSpheroidal7", "CovSpheroidal9", "Triharmonic2D", "Triharmonic3D", "Model", "Interpolant",
-    "FmmEvaluator", "PolatoryError", "make_rbf", "PLAIN", "MIXED",
+    "FmmEvaluator", "PolatoryError", "make_rbf", "PLAIN", "MIXED", "fit_batch", "Server",
 ]
 
 PLAIN = _lib.PRECISION_PLAIN
@@ -285,6 +285,133 @@ class Interpolant:
         s = _lib.PgpuFitStats()
         check(lib.pgpu_interpolant_fit_stats(self._h, C.byref(s)))
         return {k: getattr(s, k) for k, _ in s._fields_}
+
+
+def fit_batch(model: Model, problems, tolerance, max_iter=100, precision=PLAIN, n_workers=0,
+              return_weights=True):
+    """Fits many independent problems with one model (pgpu_fit_batch).
+
+    problems: list of (points, values) or (points, values, eval_points). Returns a list of dicts
+    with 'weights', 'iterations', 'residual', 'status' and 'values' (the evaluation, if asked).
+    """
+    keep = []
+    arr = (_lib.PgpuFitProblem * len(problems))()
+    l = model.poly_basis_size
+    for i, prob in enumerate(problems):
+        pts = as_points(prob[0])
+        vals = np.ascontiguousarray(np.asarray(prob[1], dtype=np.float64).reshape(-1))
+        q = as_points(prob[2]) if len(prob) > 2 and prob[2] is not None else None
+        w = np.empty(pts.shape[0] + l) if return_weights else None
+        out = np.empty(q.shape[0]) if q is not None else None
+        keep.append((pts, vals, q, w, out))
+        p = arr[i]
+        p.points = pts.ctypes.data
+        p.n = pts.shape[0]
+        p.values = vals.ctypes.data
+        p.tolerance = float(tolerance)
+        p.max_iter = int(max_iter)
+        p.eval_points = q.ctypes.data if q is not None else None
+        p.m = q.shape[0] if q is not None else 0
+        p.eval_out = out.ctypes.data if out is not None else None
+        p.weights_out = w.ctypes.data if w is not None else None
+    rc = lib.pgpu_fit_batch(C.byref(model._c()), precision, arr, len(problems), n_workers)
+    res = []
+    for i, (pts, vals, q, w, out) in enumerate(keep):
+        res.append({"weights": w, "iterations": arr[i].iterations, "residual": arr[i].residual,
+                    "status": arr[i].status, "values": out})
+    if rc != 0:
+        msg = lib.pgpu_last_error().decode()
+        err = PolatoryError(rc, msg)
+        err.results = res
+        raise err
+    return res
+
+
+class Server:
+    """Serving loop (pgpu_server_*): fit and evaluate requests admitted under a device-memory
+    budget, run concurrently on worker streams; fitted models stay resident in numbered slots.
+
+    submit_fit / submit_evaluate return a ticket; wait(ticket) and poll(ticket) (None while
+    running) return (status, latency_seconds, result, message) where result is the evaluation
+    (None for a fit) and message the error text of a failed request.
+    """
+
+    def __init__(self, n_workers: int = 8, hbm_budget_bytes: int = 0):
+        h = C.c_void_p()
+        check(lib.pgpu_server_create(int(n_workers), int(hbm_budget_bytes), C.byref(h)))
+        self._h = h
+        self._keep = {}
+
+    def close(self):
+        if self._h:
+            check(lib.pgpu_server_destroy(self._h))
+            self._h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _submit(self, req, keep):
+        t = C.c_int64()
+        check(lib.pgpu_server_submit(self._h, C.byref(req), C.byref(t)))
+        self._keep[t.value] = keep
+        return t.value
+
+    @staticmethod
+    def estimate_bytes(kind: int, n: int, precision: int = PLAIN) -> int:
+        r = _lib.PgpuRequest()
+        r.kind, r.n, r.precision = kind, n, precision
+        return lib.pgpu_server_estimate_bytes(C.byref(r))
+
+    def submit_fit(self, slot: int, model: Model, points, values, tolerance, max_iter=100,
+                   precision=PLAIN) -> int:
+        pts = as_points(points)
+        vals = np.ascontiguousarray(np.asarray(values, dtype=np.float64).reshape(-1))
+        m = model._c()
+        r = _lib.PgpuRequest()
+        r.kind, r.slot, r.model = _lib.REQUEST_FIT, slot, C.addressof(m)
+        r.points, r.n, r.values = pts.ctypes.data, pts.shape[0], vals.ctypes.data
+        r.tolerance, r.max_iter, r.precision = float(tolerance), int(max_iter), precision
+        return self._submit(r, (pts, vals, None))
+
+    def submit_evaluate(self, slot: int, points, precision=PLAIN) -> int:
+        pts = as_points(points)
+        out = np.empty(pts.shape[0])
+        r = _lib.PgpuRequest()
+        r.kind, r.slot = _lib.REQUEST_EVALUATE, slot
+        r.points, r.n, r.out, r.precision = pts.ctypes.data, pts.shape[0], out.ctypes.data, precision
+        return self._submit(r, (pts, None, out))
+
+    def poll(self, ticket: int):
+        done, st, lat = C.c_int(), C.c_int(), C.c_double()
+        check(lib.pgpu_server_poll(self._h, ticket, C.byref(done), C.byref(st), C.byref(lat)))
+        if not done.value:
+            return None
+        return self._result(ticket, st.value, lat.value)
+
+    def wait(self, ticket: int):
+        st, lat = C.c_int(), C.c_double()
+        check(lib.pgpu_server_wait(self._h, ticket, C.byref(st), C.byref(lat)))
+        return self._result(ticket, st.value, lat.value)
+
+    def _result(self, ticket, status, latency):
+        keep = self._keep.pop(ticket)
+        msg = lib.pgpu_last_error().decode() if status != 0 else ""
+        return status, latency, keep[2], msg
+
+    def stats(self) -> dict:
+        o = _lib.PgpuServerStats()
+        check(lib.pgpu_server_stats_get(self._h, C.byref(o)))
+        return {k: getattr(o, k) for k, _ in o._fields_}
 
 
 def profile_enable(on: bool = True) -> None:

@@ -24,6 +24,8 @@ PGPU_REJECTED = 8
 
 PRECISION_PLAIN = 0
 PRECISION_MIXED = 1
+REQUEST_FIT = 0
+REQUEST_EVALUATE = 1
 
 KERNEL_VALUE = 0
 KERNEL_GRADIENT = 1
@@ -49,6 +51,27 @@ class PgpuFitStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("levels", C.c_int32), ("residual", C.c_double),
                 ("grad_residual", C.c_double), ("setup_seconds", C.c_double),
                 ("solve_seconds", C.c_double), ("n_domains", C.c_int64)]
+
+
+class PgpuFitProblem(C.Structure):
+    _fields_ = [("points", C.c_void_p), ("n", C.c_int64), ("values", C.c_void_p),
+                ("tolerance", C.c_double), ("max_iter", C.c_int32), ("iterations", C.c_int32),
+                ("eval_points", C.c_void_p), ("m", C.c_int64), ("eval_out", C.c_void_p),
+                ("weights_out", C.c_void_p), ("residual", C.c_double), ("status", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class PgpuRequest(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("slot", C.c_int32), ("model", C.c_void_p),
+                ("points", C.c_void_p), ("n", C.c_int64), ("values", C.c_void_p),
+                ("tolerance", C.c_double), ("max_iter", C.c_int32), ("precision", C.c_int32),
+                ("out", C.c_void_p)]
+
+
+class PgpuServerStats(C.Structure):
+    _fields_ = [(k, C.c_int64) for k in ("submitted", "completed", "failed", "rejected",
+                                         "in_flight", "queued", "bytes_in_use", "peak_bytes",
+                                         "budget_bytes")]
 
 
 class PolatoryError(RuntimeError):
@@ -106,6 +129,16 @@ def _load():
         "pgpu_interpolant_centers": ([P, P, P], C.c_int),
         "pgpu_interpolant_bbox": ([P, P], C.c_int),
         "pgpu_interpolant_fit_stats": ([P, C.POINTER(PgpuFitStats)], C.c_int),
+        "pgpu_fit_batch": ([C.POINTER(PgpuModel), C.c_int, C.POINTER(PgpuFitProblem), I64,
+                            C.c_int], C.c_int),
+        "pgpu_server_create": ([C.c_int, I64, C.POINTER(P)], C.c_int),
+        "pgpu_server_destroy": ([P], C.c_int),
+        "pgpu_server_submit": ([P, C.POINTER(PgpuRequest), C.POINTER(I64)], C.c_int),
+        "pgpu_server_poll": ([P, I64, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                              C.POINTER(C.c_double)], C.c_int),
+        "pgpu_server_wait": ([P, I64, C.POINTER(C.c_int), C.POINTER(C.c_double)], C.c_int),
+        "pgpu_server_stats_get": ([P, C.POINTER(PgpuServerStats)], C.c_int),
+        "pgpu_server_estimate_bytes": ([C.POINTER(PgpuRequest)], I64),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -5,6 +5,7 @@
 #include <string>
 #include <unordered_map>
 
+#include "batch.hpp"
 #include "common.hpp"
 #include "evaluator.hpp"
 #include "model.hpp"
@@ -378,6 +379,36 @@ int pgpu_direct_evaluate_noalloc(const pgpu_rbf* rbf, const double* src_points, 
   return rc;
 }
 
+namespace {
+void check_fit_args(const ModelDesc& m, int64_t mu, int64_t sigma, double tol, double grad_tol,
+                    int max_iter, double acc, double grad_acc);
+}  // namespace
+
+int pgpu_fit_batch(const pgpu_model* model, int precision, pgpu_fit_problem* problems,
+                   int64_t n_problems, int n_workers) {
+  int rc = PGPU_OK;
+  int status = guarded([&] {
+    ModelDesc m = model_from_c(model);
+    if (n_problems < 0) throw_invalid("n_problems must be non-negative");
+    if (n_problems > 0) check_ptr(problems, "problems");
+    if (precision != PGPU_PRECISION_PLAIN && precision != PGPU_PRECISION_MIXED)
+      throw_invalid("unknown precision");
+    for (int64_t i = 0; i < n_problems; ++i) {
+      auto& p = problems[i];
+      check_fit_args(m, p.n, 0, p.tolerance, INFINITY, p.max_iter, INFINITY, INFINITY);
+      check_ptr(p.points, "points");
+      check_ptr(p.values, "values");
+      p.status = PGPU_OK;
+      p.iterations = 0;
+    }
+    int device = 0;
+    PGPU_CUDA(cudaGetDevice(&device));
+    rc = run_batch(m, precision, problems, n_problems, n_workers, device);
+    if (rc != PGPU_OK) throw Error(rc, "a fit of the batch failed (see each problem's status)");
+  });
+  return status;
+}
+
 // ---- interpolant ----------------------------------------------------------------------
 
 int pgpu_interpolant_create(const pgpu_model* model, pgpu_interpolant** out) {
@@ -655,3 +686,102 @@ int pgpu_interpolant_fit_stats(const pgpu_interpolant* it, pgpu_fit_stats* out) 
 }
 
 }  // extern "C"
+
+// ---- serving ----------------------------------------------------------------------------
+
+namespace pgpu {
+int server_create(int n_workers, int64_t budget, pgpu_server** out);
+void server_destroy(pgpu_server* s);
+int64_t server_estimate(const pgpu_request& r);
+void server_submit(pgpu_server* s, const pgpu_request& r, int64_t* ticket);
+bool server_poll(pgpu_server* s, int64_t ticket, bool block, int* status, double* latency,
+                 std::string* msg);
+void server_stats(pgpu_server* s, pgpu_server_stats* o);
+}  // namespace pgpu
+
+namespace {
+
+void check_request(const pgpu_request* r) {
+  check_ptr(r, "request");
+  if (r->kind != PGPU_REQUEST_FIT && r->kind != PGPU_REQUEST_EVALUATE)
+    throw_invalid("unknown request kind");
+  if (r->precision != PGPU_PRECISION_PLAIN && r->precision != PGPU_PRECISION_MIXED)
+    throw_invalid("unknown precision");
+  if (r->n < 0) throw_invalid("n must be non-negative");
+  if (r->n > 0) check_ptr(r->points, "points");
+  if (r->kind == PGPU_REQUEST_FIT) {
+    ModelDesc m = model_from_c(r->model);
+    check_fit_args(m, r->n, 0, r->tolerance, INFINITY, r->max_iter, INFINITY, INFINITY);
+    check_ptr(r->values, "values");
+  } else if (r->n > 0) {
+    check_ptr(r->out, "out");
+  }
+}
+
+}  // namespace
+
+int pgpu_server_create(int n_workers, int64_t hbm_budget_bytes, pgpu_server** out) {
+  return guarded([&] {
+    check_ptr(out, "out");
+    if (n_workers < 0) throw_invalid("n_workers must be non-negative");
+    if (hbm_budget_bytes < 0) throw_invalid("hbm_budget_bytes must be non-negative");
+    server_create(n_workers, hbm_budget_bytes, out);
+  });
+}
+
+int pgpu_server_destroy(pgpu_server* s) {
+  return guarded([&] {
+    if (s) server_destroy(s);
+  });
+}
+
+int pgpu_server_submit(pgpu_server* s, const pgpu_request* req, int64_t* ticket) {
+  return guarded([&] {
+    check_ptr(s, "server");
+    check_ptr(ticket, "ticket");
+    check_request(req);
+    server_submit(s, *req, ticket);
+  });
+}
+
+int pgpu_server_poll(pgpu_server* s, int64_t ticket, int* done, int* status, double* latency) {
+  std::string msg;
+  int rc = guarded([&] {
+    check_ptr(s, "server");
+    check_ptr(done, "done");
+    int st = PGPU_OK;
+    double lat = 0;
+    *done = server_poll(s, ticket, false, &st, &lat, &msg) ? 1 : 0;
+    if (status) *status = st;
+    if (latency) *latency = lat;
+  });
+  if (rc == PGPU_OK && !msg.empty()) g_last_error = msg;
+  return rc;
+}
+
+int pgpu_server_wait(pgpu_server* s, int64_t ticket, int* status, double* latency) {
+  std::string msg;
+  int rc = guarded([&] {
+    check_ptr(s, "server");
+    int st = PGPU_OK;
+    double lat = 0;
+    server_poll(s, ticket, true, &st, &lat, &msg);
+    if (status) *status = st;
+    if (latency) *latency = lat;
+  });
+  if (rc == PGPU_OK && !msg.empty()) g_last_error = msg;
+  return rc;
+}
+
+int pgpu_server_stats_get(pgpu_server* s, pgpu_server_stats* out) {
+  return guarded([&] {
+    check_ptr(s, "server");
+    check_ptr(out, "out");
+    server_stats(s, out);
+  });
+}
+
+int64_t pgpu_server_estimate_bytes(const pgpu_request* req) {
+  if (!req) return -1;
+  return server_estimate(*req);
+}

@@ -52,7 +52,11 @@ void set_stream(cudaStream_t s);
 
 // Device memory from the stream-ordered pool of the current device.
 void* dev_alloc(size_t bytes);
-void dev_free(void* p);
+void dev_free(void* p, size_t bytes);
+// Device bytes this thread holds through DevBuf now, and the peak since the last reset.
+int64_t thread_device_bytes();
+int64_t thread_device_peak();
+void reset_thread_device_peak();
 
 template <class T>
 class DevBuf {
@@ -83,7 +87,7 @@ class DevBuf {
     n_ = n;
   }
   void release() {
-    if (p_) dev_free(p_);
+    if (p_) dev_free(p_, n_ * sizeof(T));
     p_ = nullptr;
     n_ = 0;
   }

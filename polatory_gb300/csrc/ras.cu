@@ -634,17 +634,21 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
     build_batch(coarse_, v);
     coarse_n_ = std::max(static_cast<int>(cd.point_indices.size()) - l_, 0);
     const int cld = std::max(NB, ((coarse_n_ + NB - 1) / NB) * NB);
-    coarse_inv_.resize(std::max<Index>(static_cast<Index>(coarse_n_) * coarse_n_, 1));
-    if (coarse_n_ > 0) {
+    // With several levels the coarse grid is solved 2L-1 times per application: keep an explicit
+    // inverse (one matrix-vector product per solve). A single-level preconditioner solves once
+    // per application and keeps the factor.
+    use_coarse_inverse_ = n_levels_ > 1 && coarse_n_ > 0;
+    if (use_coarse_inverse_) {
+      coarse_inv_.resize(static_cast<Index>(coarse_n_) * coarse_n_);
       chol_inverse_kernel<double><<<coarse_n_, 256, cld * sizeof(double), stream()>>>(
           coarse_.mats.data(), cld, coarse_n_, coarse_inv_.data());
       PGPU_LAUNCH_CHECK();
+      coarse_.mats.release();
     }
     coarse_x_.resize(std::max(coarse_n_, 1));
     coarse_g_.resize(std::max(coarse_n_, 1));
     coarse_out_.resize(48);
     coarse_out_.zero();
-    coarse_.mats.release();  // the explicit inverse replaces the factor
   }
 
   // Level point sets on the device (for the residual-update evaluators).
@@ -831,14 +835,21 @@ void RasPreconditioner<T>::solve_level(int level, const double* residuals, doubl
   coarse_rhs_kernel<<<blocks_for(std::max(n, 1), 256), 256, 0, stream()>>>(
       dp, n, l, lagrange_.data(), residuals, coarse_x_.data(), coarse_out_.data() + 32);
   PGPU_LAUNCH_CHECK();
-  if (n > 0) {
+  if (use_coarse_inverse_) {
     symv_kernel<<<blocks_for(static_cast<Index>(n) * 32, 256), 256, 0, stream()>>>(
         coarse_inv_.data(), n, coarse_x_.data(), coarse_g_.data());
     PGPU_LAUNCH_CHECK();
+    coarse_finish_kernel<<<1, 256, 0, stream()>>>(dp, n, l, lagrange_.data(), u_.data(),
+                                                  coarse_g_.data(), weights, coarse_out_.data());
+    PGPU_LAUNCH_CHECK();
+  } else {
+    const size_t smem = (static_cast<size_t>(coarse_.max_n) + 16 + 64) * sizeof(double);
+    ras_solve_kernel<double><<<1, 256, smem, stream()>>>(
+        coarse_.n.data(), coarse_.ld.data(), coarse_.mat_off.data(), coarse_.mats.data(),
+        coarse_.pt_off.data(), coarse_.pts.data(), coarse_.inner.data(), l, lagrange_.data(),
+        u_.data(), residuals, weights, 1, coarse_out_.data());
+    PGPU_LAUNCH_CHECK();
   }
-  coarse_finish_kernel<<<1, 256, 0, stream()>>>(dp, n, l, lagrange_.data(), u_.data(),
-                                                coarse_g_.data(), weights, coarse_out_.data());
-  PGPU_LAUNCH_CHECK();
   if (l > 0) {
     // Polynomial part: solve P_top c = d_head - A_top lambda (coarse_grid.hpp:124-127).
     double h[48];

@@ -77,6 +77,7 @@ class RasPreconditioner {
   DomainBatch<double> coarse_;
   DevBuf<double> coarse_inv_;  // n x n
   int coarse_n_ = 0;
+  bool use_coarse_inverse_ = false;
   DevBuf<double> coarse_x_, coarse_g_, coarse_out_;
   DevBuf<double> p_;   // mu x l orthonormalised monomials (column-major)
   DevBuf<double> ap_;  // mu x l

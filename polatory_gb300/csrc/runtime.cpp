@@ -61,16 +61,29 @@ void set_device(int device) {
   ctx();
 }
 
+namespace {
+thread_local int64_t g_thread_bytes = 0;
+thread_local int64_t g_thread_peak = 0;
+}  // namespace
+
 void* dev_alloc(size_t bytes) {
   void* p = nullptr;
   if (bytes == 0) return nullptr;
   PGPU_CUDA(cudaMallocAsync(&p, bytes, stream()));
+  g_thread_bytes += static_cast<int64_t>(bytes);
+  if (g_thread_bytes > g_thread_peak) g_thread_peak = g_thread_bytes;
   return p;
 }
 
-void dev_free(void* p) {
-  if (p) cudaFreeAsync(p, stream());
+void dev_free(void* p, size_t bytes) {
+  if (!p) return;
+  cudaFreeAsync(p, stream());
+  g_thread_bytes -= static_cast<int64_t>(bytes);
 }
+
+int64_t thread_device_bytes() { return g_thread_bytes; }
+int64_t thread_device_peak() { return g_thread_peak; }
+void reset_thread_device_peak() { g_thread_peak = g_thread_bytes; }
 
 void release_cached_memory() {
   cudaMemPool_t pool;

@@ -360,10 +360,28 @@ FitResult fit_impl(const FitRequest& req) {
     // inf-norm test of residual_evaluator.hpp:93-107). When the estimate has run far below the
     // true residual (the FP32 operator's rounding floor), FGMRES restarts from the current
     // weights on the recomputed residual: iterative refinement.
+    // Inner operator: FP32 until a restart cycle fails to halve the recomputed residual (the
+    // system is too ill-conditioned for FP32 sums at this tolerance); then FP64 for the rest.
+    struct InnerOp {
+      Operator<float>* f32;
+      Operator<double>* f64 = nullptr;
+      Index size() const { return f32->size(); }
+      void apply(const double* x, double* y) {
+        if (f64) f64->apply(x, y);
+        else f32->apply(x, y);
+      }
+    } inner{&op32};
+    std::unique_ptr<Operator<double>> op64_inner;
+    auto residual_op = [&](const double* x, double* y) {
+      if (op64) op64->apply(x, y);
+      else if (inner.f64) inner.f64->apply(x, y);
+      else op32.apply(x, y);
+    };
     int total = 0;
     Fgmres solver(M, req.max_iter);
-    solver.setup(rhs.data(), w.data(), x0_zero, op32);
+    solver.setup(rhs.data(), w.data(), x0_zero, inner);
     int base = 0;  // iterations before the current restart
+    double cycle_start_residual = INFINITY;
     while (true) {
       const double est_rms = solver.absolute_residual() / std::sqrt(static_cast<double>(mu));
       total = base + solver.iteration_count();
@@ -371,8 +389,7 @@ FitResult fit_impl(const FitRequest& req) {
         if (req.verbose) std::printf("%8d   ~%12.6e (estimate)\n", total, est_rms);
       } else {
         solver.solution(w.data());
-        if (op64) op64->apply(w.data(), r.data());
-        else op32.apply(w.data(), r.data());
+        residual_op(w.data(), r.data());
         axpby(M, 1.0, rhs.data(), -1.0, r.data());
         const double rinf = inf_norm_diff(r.data(), zero.data(), mu);
         res.residual = rinf;
@@ -380,8 +397,16 @@ FitResult fit_impl(const FitRequest& req) {
         if (rinf <= req.tolerance) break;
         const double rtrue = norm2(r.data(), M);
         if (solver.iteration_count() > 0 && solver.absolute_residual() < 0.1 * rtrue) {
+          if (!inner.f64 && rinf > 0.5 * cycle_start_residual) {
+            op64_inner = std::make_unique<Operator<double>>(model, pts.data(), mu, bbox, 0.0, P.data());
+            inner.f64 = op64_inner.get();
+            if (req.verbose) std::printf("%8d    switching the inner operator to FP64\n", total);
+          }
+          cycle_start_residual = rinf;
           base = total;
-          solver.setup(rhs.data(), w.data(), false, op32);
+          solver.setup(rhs.data(), w.data(), false, inner);
+        } else if (!std::isfinite(cycle_start_residual)) {
+          cycle_start_residual = rinf;
         }
       }
       if (total >= req.max_iter)
@@ -389,9 +414,9 @@ FitResult fit_impl(const FitRequest& req) {
       if (solver.iteration_count() == solver.max_iterations()) {
         solver.solution(w.data());
         base = total;
-        solver.setup(rhs.data(), w.data(), false, op32);
+        solver.setup(rhs.data(), w.data(), false, inner);
       }
-      solver.iterate(op32, pc);
+      solver.iterate(inner, pc);
     }
     res.iterations = total;
   }

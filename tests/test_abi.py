@@ -93,3 +93,18 @@ def test_cpd_orders_and_support():
     assert pg.CovCubic([1.0, 0.5]).support_radius_isotropic() == 0.5
     assert pg.CovSpherical([1.0, 0.7]).support_radius_isotropic() == 0.7
     assert np.isinf(pg.CovExponential([1.0, 0.5]).support_radius_isotropic())
+
+
+def test_server_estimate_and_argument_checks():
+    fit_small = pg.Server.estimate_bytes(_lib.REQUEST_FIT, 1000)
+    fit_big = pg.Server.estimate_bytes(_lib.REQUEST_FIT, 1000000)
+    fit_mixed = pg.Server.estimate_bytes(_lib.REQUEST_FIT, 1000000, pg.MIXED)
+    ev = pg.Server.estimate_bytes(_lib.REQUEST_EVALUATE, 1000000)
+    assert 0 < fit_small < fit_big
+    assert fit_mixed < fit_big
+    assert ev < fit_big
+    assert _lib.lib.pgpu_server_estimate_bytes(None) == -1
+    h = C.c_void_p()
+    assert _lib.lib.pgpu_server_create(-1, 0, C.byref(h)) == _lib.PGPU_INVALID_ARGUMENT
+    assert _lib.lib.pgpu_server_create(2, -5, C.byref(h)) == _lib.PGPU_INVALID_ARGUMENT
+    assert _lib.lib.pgpu_server_destroy(None) == _lib.PGPU_OK
