@@ -41,10 +41,99 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0, help="fraction of the default sizes")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--workload", choices=["c2", "c1", "c3", "c4"], default="c2",
+    ap.add_argument("--workload", choices=["c2", "c1", "c3", "c4", "c5"], default="c2",
                     help="c2: surface fit (default, the headline); c1: 10k cube fit + 64^3 grid; "
-                         "c3: 500k kriging fit + 10M queries; c4: 4096 uneven batched fits")
+                         "c3: 500k kriging fit + 10M queries; c4: 4096 uneven batched fits; "
+                         "c5: serving stream with Poisson arrivals")
+    ap.add_argument("--requests", type=int, default=600, help="c5: requests in the stream")
+    ap.add_argument("--rate", type=float, default=20.0, help="c5: mean arrivals per second")
     return ap.parse_args()
+
+
+def run_serving(args):
+    """Serving stream: Poisson arrivals, 70% evaluations (1k-1M query points, log-uniform)
+    against resident models and 30% fits (N log-uniform 1k-200k, biharmonic3d or cov_exponential
+    with range 0.1-0.5, tol 1e-4), admitted against a 150 GB device-memory budget. Inputs are
+    host arrays (the serving API copies them in); latency is submit-to-completion on the host
+    clock. Eight resident models are fitted before the timed stream."""
+    import polatory_gb300 as pg
+
+    g = np.random.Generator(np.random.PCG64(5))
+    n_req = max(20, int(args.requests))
+    qpool = g.random((1_000_000, 3))
+    fpool = g.random((200_000, 3))
+    fvals = np.sin(2 * np.pi * fpool[:, 0]) * np.cos(2 * np.pi * fpool[:, 1]) + fpool[:, 2] ** 2
+
+    def model_for(rng):
+        if rng.random() < 0.5:
+            return pg.Model(pg.Biharmonic3D([1.0]), 1)
+        return pg.Model(pg.CovExponential([1.0, float(rng.uniform(0.1, 0.5))]), 0)
+
+    def log_uniform(rng, lo, hi):
+        return int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
+
+    n_slots = 8
+    server = pg.Server(n_workers=8, hbm_budget_bytes=150 * 10**9)
+    for k in range(n_slots):
+        n = log_uniform(g, 1000, 200_000)
+        t = server.submit_fit(k, model_for(g), fpool[:n], fvals[:n], 1e-4, precision=pg.MIXED)
+        st = server.wait(t)
+        assert st[0] == 0, st[3]
+    plan = []
+    t_arr = 0.0
+    for i in range(n_req):
+        t_arr += g.exponential(1.0 / args.rate)
+        if g.random() < 0.7:
+            plan.append((t_arr, "evaluate", int(g.integers(n_slots)), log_uniform(g, 1000, 1_000_000)))
+        else:
+            plan.append((t_arr, "fit", int(g.integers(n_slots)), log_uniform(g, 1000, 200_000)))
+    models = [model_for(g) for _ in range(n_req)]
+    tickets = []
+    start = time.perf_counter()
+    for (ta, kind, slot, n), m in zip(plan, models):
+        delay = start + ta - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        if kind == "evaluate":
+            t = server.submit_evaluate(slot, qpool[:n], precision=pg.MIXED)
+        else:
+            t = server.submit_fit(slot, m, fpool[:n], fvals[:n], 1e-4, precision=pg.MIXED)
+        tickets.append((t, kind, n))
+    lat = {"fit": [], "evaluate": []}
+    failed = 0
+    errors = []
+    points = 0
+    for t, kind, n in tickets:
+        st, latency, _, msg = server.wait(t)
+        if st != 0:
+            failed += 1
+            if len(errors) < 3:
+                errors.append(f"{kind} n={n}: status {st}: {msg}")
+            continue
+        lat[kind].append(latency)
+        points += n
+    wall = time.perf_counter() - start
+    stats = server.stats()
+    server.close()
+    allv = lat["fit"] + lat["evaluate"]
+
+    def pct(v, q):
+        return float(np.percentile(v, q)) if v else None
+
+    line = {"metric": "c5 serving points/s (mixed precision)", "value": points / wall,
+            "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": wall * 1e3,
+            "higher_is_better": True, "data": "synthetic",
+            "config": {"workload": f"{n_req} requests, Poisson arrivals at {args.rate}/s, 70% "
+                                   "evaluate 1k-1M queries on 8 resident models, 30% fit 1k-200k "
+                                   "(bh3 degree 1 or cov_exponential range 0.1-0.5), tol 1e-4, "
+                                   "150 GB budget, 8 workers"},
+            "latency_s": {"p50": pct(allv, 50), "p99": pct(allv, 99),
+                          "fit_p50": pct(lat["fit"], 50), "fit_p99": pct(lat["fit"], 99),
+                          "evaluate_p50": pct(lat["evaluate"], 50),
+                          "evaluate_p99": pct(lat["evaluate"], 99)},
+            "failed": failed, "errors": errors, "peak_bytes": stats["peak_bytes"],
+            "timing": "host wall clock from the first arrival to the last completion"}
+    print(json.dumps(line), flush=True)
 
 
 def run_other(args):
@@ -257,6 +346,9 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "c5":
+        run_serving(args)
         return
     if args.workload != "c2":
         run_other(args)

@@ -75,7 +75,7 @@ void run_one(const ModelDesc& model, int precision, pgpu_fit_problem& p) {
 }  // namespace
 
 int run_batch(const ModelDesc& model, int precision, pgpu_fit_problem* problems, int64_t n,
-              int n_workers, int device) {
+              int n_workers, int device, std::string* first_error) {
   if (n == 0) return PGPU_OK;
   if (n_workers <= 0) n_workers = static_cast<int>(std::min<int64_t>(n, 16));
   n_workers = static_cast<int>(std::min<int64_t>(n_workers, n));
@@ -84,6 +84,7 @@ int run_batch(const ModelDesc& model, int precision, pgpu_fit_problem* problems,
   std::stable_sort(order.begin(), order.end(),
                    [&](int64_t a, int64_t b) { return problems[a].n > problems[b].n; });
   std::atomic<int64_t> next{0};
+  std::vector<std::string> messages(n);
   auto work = [&] {
     omp_set_num_threads(1);  // the host set-up of each fit runs on its own worker
     try {
@@ -99,16 +100,23 @@ int run_batch(const ModelDesc& model, int precision, pgpu_fit_problem* problems,
         p.status = PGPU_OK;
       } catch (const Error& e) {
         p.status = e.code;
-      } catch (const std::exception&) {
+        messages[order[k]] = e.what();
+      } catch (const std::exception& e) {
         p.status = PGPU_RUNTIME_ERROR;
+        messages[order[k]] = e.what();
       }
     }
   };
   std::vector<std::thread> pool;
   for (int i = 0; i < n_workers; ++i) pool.emplace_back(work);
   for (auto& t : pool) t.join();
-  for (int64_t i = 0; i < n; ++i)
-    if (problems[i].status != PGPU_OK) return problems[i].status;
+  for (int64_t i = 0; i < n; ++i) {
+    if (problems[i].status != PGPU_OK) {
+      if (first_error)
+        *first_error = "fit " + std::to_string(i) + " of the batch failed: " + messages[i];
+      return problems[i].status;
+    }
+  }
   return PGPU_OK;
 }
 

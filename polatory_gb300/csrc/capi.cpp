@@ -403,8 +403,9 @@ int pgpu_fit_batch(const pgpu_model* model, int precision, pgpu_fit_problem* pro
     }
     int device = 0;
     PGPU_CUDA(cudaGetDevice(&device));
-    rc = run_batch(m, precision, problems, n_problems, n_workers, device);
-    if (rc != PGPU_OK) throw Error(rc, "a fit of the batch failed (see each problem's status)");
+    std::string first;
+    rc = run_batch(m, precision, problems, n_problems, n_workers, device, &first);
+    if (rc != PGPU_OK) throw Error(rc, first + " (each problem's status is set)");
   });
   return status;
 }

@@ -111,6 +111,7 @@ struct Evaluator<T>::Term {
   double box_min[3];
   double box_width;
   KParams<T> kp;
+  KParams<double> kp64;
   DevBuf<P4<T>> spos, sgpos, tpos, tgpos;
   // Frame coordinates in FP64 for the FMM (it re-expresses them relative to leaf centres).
   DevBuf<P4<double>> spos_d, tpos_d;
@@ -145,6 +146,7 @@ Evaluator<T>::Evaluator(const ModelDesc& model, const Bbox3& bbox, double accura
     }
     t->box_width = w;
     t->kp = KParams<T>{static_cast<T>(r.p[0]), static_cast<T>(r.p[1])};
+    t->kp64 = KParams<double>{r.p[0], r.p[1]};
     terms_.push_back(std::move(t));
   }
 }
@@ -211,8 +213,17 @@ void Evaluator<T>::set_points(const double* pts, Index mu, const double* gpts, I
 }
 
 template <class T>
+void Evaluator<T>::set_far_field(const FarFieldConfig& c) {
+  ff_ = c;
+  ff_set_ = true;
+  for (auto& t : terms_)
+    if (t->fmm) t->fmm->set_config(c);
+}
+
+template <class T>
 void Evaluator<T>::set_weights(const double* w) {
   const int l = model_.l();
+  w_ = w;
   for (auto& t : terms_) {
     if (mu_ + sigma_ > 0) {
       prep_weights_kernel<T><<<blocks_for(mu_ + sigma_, 256), 256, 0, stream()>>>(
@@ -250,7 +261,13 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
     const bool fmm_ok = Fmm<T>::supported(t.rbf.kind) && sigma_ == 0 && mg_ == 0;
     bool use_fmm = fmm_ok && (backend_ == kBackendFmm ||
                               (backend_ == kBackendAuto && pairs > direct_pair_limit<T>()));
-    if (!use_fmm) {
+    const bool fp64_near = sizeof(T) == 4 && near64_ && sigma_ == 0 && mg_ == 0;
+    if (!use_fmm && fp64_near) {
+      DirectSources<double> src{t.spos_d.data(), w_, mu_, nullptr, nullptr, 0};
+      DirectTargets<double> trg{t.tpos_d.data(), m_, out_v, nullptr, 0, out_g};
+      direct_evaluate<double>(t.rbf.kind, t.kp64, t.a, src, trg, stream());
+      stats_.direct_pairs += static_cast<Index>(pairs);
+    } else if (!use_fmm) {
       DirectSources<T> src{t.spos.data(), t.vw.data(), mu_, t.sgpos.data(), t.gg.data(), sigma_};
       DirectTargets<T> trg{t.tpos.data(), m_, out_v, t.tgpos.data(), mg_, out_g};
       direct_evaluate<T>(t.rbf.kind, t.kp, t.a, src, trg, stream());
@@ -272,7 +289,8 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
         }
         t.fmm_sources_dirty = t.fmm_targets_dirty = false;
       }
-      t.fmm->evaluate(t.vw.data(), t.gg.data(), out_v, out_g);
+      t.fmm->set_near_fp64(fp64_near, t.kp64);
+      t.fmm->evaluate(t.vw.data(), t.gg.data(), w_, out_v, out_g);
       stats_.near_pairs += t.fmm->near_pairs();
       stats_.backend = 1;
     }

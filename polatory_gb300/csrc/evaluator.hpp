@@ -82,7 +82,11 @@ class Evaluator {
   static constexpr int kBackendAuto = 0, kBackendDirect = 1, kBackendFmm = 2;
   void set_backend(int b) { backend_ = b; }
   void force_direct(bool f) { backend_ = f ? kBackendDirect : kBackendAuto; }
-  void set_far_field(const FarFieldConfig& c) { ff_ = c; ff_set_ = true; }
+  // Far-field order / leaf level; applies to FMMs already built too (they rebuild).
+  void set_far_field(const FarFieldConfig& c);
+  // FP32 evaluators of value sources and targets: near field (or all pairs, on the direct
+  // backend) in FP64 from the FP64 coordinates and weights; the far field stays FP32.
+  void set_near_fp64(bool on) { near64_ = on; }
 
  private:
   struct Term;
@@ -94,6 +98,8 @@ class Evaluator {
   int backend_ = kBackendAuto;
   bool ff_set_ = false;
   FarFieldConfig ff_;
+  bool near64_ = false;
+  const double* w_ = nullptr;  // the weights of the last set_weights (device)
   Index mu_ = 0, sigma_ = 0, m_ = 0, mg_ = 0;
   const double* spts_ = nullptr;
   const double* sgpts_ = nullptr;

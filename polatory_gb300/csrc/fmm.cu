@@ -716,6 +716,10 @@ struct Tree {
   int lf = 0;
   DevBuf<Index> perm;
   DevBuf<P4<T>> pos;  // sorted
+  // FP32 trees only: sorted level-kSortLevel keys, and (built on first use) the leaf-relative
+  // positions in FP64 for an FP64 near field.
+  DevBuf<uint64_t> skeys;
+  DevBuf<P4<double>> pos64;
   // per level k = 0..lf
   std::vector<DevBuf<uint64_t>> keys;
   std::vector<Index> ncell;
@@ -812,6 +816,12 @@ void build_tree(Tree<T>& tr, const SortedPoints& sp, const P4<double>* pos, cons
                                                                  leaf_shift, n, box, lf,
                                                                  tr.pos.data());
   PGPU_LAUNCH_CHECK();
+  tr.pos64.release();
+  if constexpr (sizeof(T) == 4) {
+    tr.skeys.resize(n);
+    PGPU_CUDA(cudaMemcpyAsync(tr.skeys.data(), sp.keys.data(), n * sizeof(uint64_t),
+                              cudaMemcpyDeviceToDevice, st));
+  }
 
   // Run-length encode level by level: level lf from the sorted point keys, then parents.
   DevBuf<Index> flags(n), scan(n);
@@ -1192,8 +1202,20 @@ struct Fmm<T>::Impl {
   Index near_pairs = 0;
   std::vector<Index> m2l_pairs;  // interactions per level
   Cheb<T> ch;
+  // FP64 near field for an FP32 tree (set_near_fp64).
+  bool near64 = false;
+  KParams<double> kp64{};
 
   Tree<T>& ttree() { return symmetric ? src : trg; }
+
+  void ensure_pos64(Tree<T>& tr, const P4<double>* pos_in) {
+    if (tr.n == 0 || tr.pos64.size() == static_cast<size_t>(tr.n)) return;
+    tr.pos64.resize(tr.n);
+    gather_rel_pos_kernel<double><<<blocks_for(tr.n, 256), 256, 0, stream()>>>(
+        pos_in, tr.perm.data(), tr.skeys.data(), 3 * (kSortLevel - lf), tr.n, box, lf,
+        tr.pos64.data());
+    PGPU_LAUNCH_CHECK();
+  }
 
   // Leaf level from the measured occupancy: the level whose average number of sources per
   // occupied leaf is closest (in ratio) to the target — surface data fills far fewer cells than
@@ -1422,11 +1444,12 @@ struct Fmm<T>::Impl {
     }
   }
 
-  void evaluate(const T* vw, double* out) {
+  void evaluate(const T* vw, const double* w64, double* out) {
     if (!built) build();
     cudaStream_t st = stream();
     Tree<T>& tt = ttree();
     if (ns == 0 || (symmetric ? ns : nt) == 0) return;
+    const bool fp64_near = sizeof(T) == 4 && near64 && w64 != nullptr;
     gather_w_kernel<T><<<blocks_for(ns, 256), 256, 0, st>>>(vw, src.perm.data(), ns, sw.data());
     PGPU_LAUNCH_CHECK();
     if (lf >= 2) {
@@ -1437,7 +1460,23 @@ struct Fmm<T>::Impl {
       }
     }
     const Index ntl = tt.ncell[lf];
-    if (ntl > 0) {
+    if (ntl > 0 && fp64_near) {
+      ensure_pos64(src, spos_in);
+      if (!symmetric) ensure_pos64(trg, tpos_in);
+      DevBuf<double> sw64(ns);
+      gather_w_kernel<double><<<blocks_for(ns, 256), 256, 0, st>>>(w64, src.perm.data(), ns,
+                                                                   sw64.data());
+      PGPU_LAUNCH_CHECK();
+      ProfScope ps("fmm_p2p_f64", pair_flops(kind) * static_cast<double>(near_pairs));
+      dispatch_kind(kind, [&]<int K>() {
+        p2p_kernel<K, double><<<static_cast<unsigned>(ntl), 128, 0, st>>>(
+            kp64, tt.pos64.data(), tt.perm.data(), tt.start[lf].data(), p2p_table.data(),
+            src.pos64.data(), sw64.data(), src.start[lf].data(),
+            box.width / static_cast<double>(1 << lf), out);
+        return 0;
+      });
+      PGPU_LAUNCH_CHECK();
+    } else if (ntl > 0) {
       ProfScope ps(sizeof(T) == 4 ? "fmm_p2p_f32" : "fmm_p2p_f64",
                    pair_flops(kind) * static_cast<double>(near_pairs));
       dispatch_kind(kind, [&]<int K>() {
@@ -1519,8 +1558,14 @@ void Fmm<T>::set_targets(const P4<double>* pos, Index n) {
 }
 
 template <class T>
-void Fmm<T>::evaluate(const T* vw, const T*, double* out_v, double*) {
-  impl_->evaluate(vw, out_v);
+void Fmm<T>::set_near_fp64(bool on, const KParams<double>& kp64) {
+  impl_->near64 = on;
+  impl_->kp64 = kp64;
+}
+
+template <class T>
+void Fmm<T>::evaluate(const T* vw, const T*, const double* w64, double* out_v, double*) {
+  impl_->evaluate(vw, w64, out_v);
 }
 
 template <class T>

@@ -23,8 +23,12 @@ class Fmm {
   void set_points(const P4<double>* pos, Index n);
   void set_sources(const P4<double>* pos, Index n);
   void set_targets(const P4<double>* pos, Index n);
-  // Adds the potentials (value targets) and A^T-mapped gradients (gradient targets).
-  void evaluate(const T* vw, const T* gg, double* out_v, double* out_g);
+  // FP32 trees: take the near field with FP64 positions (leaf-relative), weights and sums,
+  // the far field staying in T. Ignored for FP64 trees.
+  void set_near_fp64(bool on, const KParams<double>& kp64);
+  // Adds the potentials (value targets) and A^T-mapped gradients (gradient targets). w64: the
+  // FP64 value weights (unsorted), read by an FP64 near field.
+  void evaluate(const T* vw, const T* gg, const double* w64, double* out_v, double* out_g);
   Index near_pairs() const;
 
  private:

@@ -75,10 +75,13 @@ void* dev_alloc(size_t bytes) {
   return p;
 }
 
+// Never throws: it runs in destructors, including those of process-wide caches at exit, on
+// threads that may never have used the library (their context is not created for a free).
 void dev_free(void* p, size_t bytes) {
   if (!p) return;
-  cudaFreeAsync(p, stream());
   g_thread_bytes -= static_cast<int64_t>(bytes);
+  cudaStream_t s = g_ctx.initialized ? g_ctx.stream : nullptr;
+  if (cudaFreeAsync(p, s) != cudaSuccess) cudaGetLastError();
 }
 
 int64_t thread_device_bytes() { return g_thread_bytes; }

@@ -226,7 +226,9 @@ struct pgpu_server {
     m->counter = &resident_bytes;
     resident_bytes.fetch_add(m->bytes);
     versions[it.ticket] = std::move(m);
-    slot_current[r.slot] = it.ticket;
+    // Fits on one slot may finish out of order: the slot holds the latest submitted one.
+    auto cur = slot_current.find(r.slot);
+    if (cur == slot_current.end() || cur->second < it.ticket) slot_current[r.slot] = it.ticket;
   }
 
   void run_evaluate(Item& it, int64_t* measured) {

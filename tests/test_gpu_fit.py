@@ -37,8 +37,8 @@ def test_fit_small_biharmonic(precision):
     interp.fit(pts, vals, tol)
     q = g.random((700, 3))
     got, want = check_fit(interp, model, pts, vals, tol, q)
-    tol_eval = 1e-10 if precision == pg.PLAIN else 1e-5
-    assert np.max(np.abs(got - want)) <= tol_eval
+    # Below 2^30 source-target pairs the mixed request runs the FP64 path.
+    assert np.max(np.abs(got - want)) <= 1e-10
     exact = oracle.fit_exact(model, pts, vals)
     ref = oracle.direct_evaluate(model, pts, exact, q)
     assert np.max(np.abs(got - ref)) <= 1e-3
@@ -57,8 +57,49 @@ def test_fit_c1_two_levels(precision):
     assert stats["iterations"] <= 60
     q = grid[::97]
     got, want = check_fit(interp, model, pts, vals, tol, q)
-    # The mixed path evaluates in FP32 (FP64 accumulation) and targets 1e-4 absolute accuracy.
-    assert np.max(np.abs(got - want)) <= (1e-9 if precision == pg.PLAIN else 5e-5)
+    assert np.max(np.abs(got - want)) <= 1e-9
+
+
+def test_small_mixed_request_runs_fp64_path():
+    pts, vals, grid = workloads.c1()
+    model = pg.Model(pg.Biharmonic3D([1.0]), 1)
+    a = pg.Interpolant(model, pg.PLAIN)
+    b = pg.Interpolant(model, pg.MIXED)
+    a.fit(pts, vals, 1e-5)
+    b.fit(pts, vals, 1e-5)
+    np.testing.assert_array_equal(a.weights, b.weights)
+    np.testing.assert_array_equal(a.evaluate(grid[::50]), b.evaluate(grid[::50]))
+
+
+@pytest.mark.parametrize("kind", ["biharmonic", "cov_exponential"])
+def test_fit_mixed_large(kind):
+    # Above 2^30 pairs: FP32 operator and preconditioner, FP64 residuals (iterative refinement).
+    g = np.random.Generator(np.random.PCG64(24))
+    n = 60000
+    pts = g.random((n, 3))
+    if kind == "biharmonic":
+        vals = workloads.f_c1(pts)
+        model = pg.Model(pg.Biharmonic3D([1.0]), 1)
+        tol = 1e-5
+    else:
+        vals = np.sin(4 * pts[:, 0]) + pts[:, 1]
+        rbf = pg.CovExponential([1.0, 0.3])
+        rbf.anisotropy = np.diag([1.0, 1.0, 2.0])
+        model = pg.Model(rbf, 0)
+        model.nugget = 1e-3
+        tol = 1e-4
+    mixed = pg.Interpolant(model, pg.MIXED)
+    mixed.fit(pts, vals, tol)
+    w = mixed.weights
+    fit_vals = oracle.direct_evaluate(model, pts, w, pts) + model.nugget * w[:n]
+    assert np.max(np.abs(fit_vals - vals)) <= tol
+    q = g.random((40000, 3))  # 2.4e9 pairs: FP32 evaluation
+    got = mixed.evaluate(q)
+    want = oracle.direct_evaluate(model, pts, w, q)
+    assert np.max(np.abs(got - want)) <= 1e-4
+    plain = pg.Interpolant(model, pg.PLAIN)
+    plain.fit(pts, vals, tol)
+    assert np.max(np.abs(plain.evaluate(q) - got)) <= 1e-4
 
 
 def test_fit_covariance_with_nugget():

@@ -86,6 +86,24 @@ def test_evaluation_reads_the_fit_submitted_before_it():
         np.testing.assert_array_equal(s.wait(e2)[2], want[1])
 
 
+def test_slot_holds_latest_fit_when_fits_finish_out_of_order():
+    m = pg.Model(pg.Biharmonic3D([1.0]), 1)
+    big = problem(11, 20000)
+    small = problem(12, 1000)
+    q = np.random.Generator(np.random.PCG64(13)).random((200, 3))
+    it = pg.Interpolant(m)
+    it.fit(*small, 1e-5)
+    want = it.evaluate(q)
+    with pg.Server(n_workers=4) as s:
+        t1 = s.submit_fit(0, m, *big, 1e-5)    # finishes last
+        t2 = s.submit_fit(0, m, *small, 1e-5)  # submitted last: the slot's model
+        assert s.wait(t2)[0] == 0
+        assert s.wait(t1)[0] == 0
+        st, _, out, msg = s.wait(s.submit_evaluate(0, q))
+        assert st == 0, msg
+        np.testing.assert_array_equal(out, want)
+
+
 def test_admission_within_budget():
     m = pg.Model(pg.Biharmonic3D([1.0]), 1)
     one = pg.Server.estimate_bytes(_lib.REQUEST_FIT, 3000)
