@@ -26,6 +26,7 @@
 
 #include "fmm.hpp"
 #include "linalg.hpp"
+#include "m2l_tc.hpp"
 #include "profile.hpp"
 
 namespace pgpu {
@@ -692,6 +693,119 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// Near field of the odd polyharmonic kernels (-p0 rho, p0 rho^3 with rho^2 = r^2 + p1^2) in
+// float-float arithmetic: positions, weights and sums carried as unevaluated pairs of floats
+// (about 44 significant bits), on the FP32 pipes. Differences use TwoSum, squares and
+// products FMA-based TwoProd, the square root one Newton step from rsqrtf. Each 128-source
+// tile is summed in float-float and added to an FP64 total.
+__device__ __forceinline__ void ff_split(double x, float& hi, float& lo) {
+  hi = static_cast<float>(x);
+  lo = static_cast<float>(x - static_cast<double>(hi));
+}
+
+__device__ __forceinline__ void ff_two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float v = s - a;
+  e = (a - (s - v)) + (b - v);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(128)
+    p2p_ff_kernel(KParams<double> kp, const P4<double>* __restrict__ tpos,
+                  const Index* __restrict__ tperm, const Index* __restrict__ tleaf_start,
+                  const int* __restrict__ table, const P4<double>* __restrict__ spos,
+                  const double* __restrict__ sw, const Index* __restrict__ sleaf_start,
+                  double wleaf, double* __restrict__ out) {
+  __shared__ float s_p[8][128];  // x, y, z, w as (hi, lo)
+  __shared__ int s_nb[27];
+  const Index leaf = blockIdx.x;
+  if (threadIdx.x < 27) s_nb[threadIdx.x] = table[leaf * 27 + threadIdx.x];
+  __syncthreads();
+  float c_hi, c_lo;  // p1^2
+  ff_split(kp.p1 * kp.p1, c_hi, c_lo);
+  const bool reg = kp.p1 != 0.0;
+  const Index tb = tleaf_start[leaf], te = tleaf_start[leaf + 1];
+  for (Index i0 = tb; i0 < te; i0 += blockDim.x) {
+    const Index i = i0 + threadIdx.x;
+    const bool active = i < te;
+    const P4<double> t = active ? tpos[i] : P4<double>{0.0, 0.0, 0.0, 0.0};
+    double tot = 0.0;
+    for (int nb = 0; nb < 27; ++nb) {
+      const int s = s_nb[nb];
+      if (s < 0) continue;
+      float txh, txl, tyh, tyl, tzh, tzl;
+      ff_split(t.x - static_cast<double>(nb / 9 - 1) * wleaf, txh, txl);
+      ff_split(t.y - static_cast<double>((nb / 3) % 3 - 1) * wleaf, tyh, tyl);
+      ff_split(t.z - static_cast<double>(nb % 3 - 1) * wleaf, tzh, tzl);
+      const Index sb = sleaf_start[s], se = sleaf_start[s + 1];
+      for (Index base = sb; base < se; base += 128) {
+        const int cnt = static_cast<int>(min(static_cast<Index>(128), se - base));
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+          const P4<double> p = spos[base + threadIdx.x];
+          ff_split(p.x, s_p[0][threadIdx.x], s_p[1][threadIdx.x]);
+          ff_split(p.y, s_p[2][threadIdx.x], s_p[3][threadIdx.x]);
+          ff_split(p.z, s_p[4][threadIdx.x], s_p[5][threadIdx.x]);
+          ff_split(sw[base + threadIdx.x], s_p[6][threadIdx.x], s_p[7][threadIdx.x]);
+        }
+        __syncthreads();
+        float ah = 0.0f, al = 0.0f;
+#pragma unroll 2
+        for (int j = 0; j < cnt; ++j) {
+          float dxh, dxe, dyh, dye, dzh, dze;
+          ff_two_sum(txh, -s_p[0][j], dxh, dxe);
+          ff_two_sum(tyh, -s_p[2][j], dyh, dye);
+          ff_two_sum(tzh, -s_p[4][j], dzh, dze);
+          dxe += txl - s_p[1][j];
+          dye += tyl - s_p[3][j];
+          dze += tzl - s_p[5][j];
+          // r^2 = sum (h + e)^2 ~ h^2 + 2 h e.
+          const float px = dxh * dxh, py = dyh * dyh, pz = dzh * dzh;
+          const float pxe = fmaf(2.0f * dxh, dxe, fmaf(dxh, dxh, -px));
+          const float pye = fmaf(2.0f * dyh, dye, fmaf(dyh, dyh, -py));
+          const float pze = fmaf(2.0f * dzh, dze, fmaf(dzh, dzh, -pz));
+          float a, ea, r2h, eb;
+          ff_two_sum(px, py, a, ea);
+          ff_two_sum(a, pz, r2h, eb);
+          float r2l = ea + eb + pxe + pye + pze;
+          if (reg) {
+            float sh, se2;
+            ff_two_sum(r2h, c_hi, sh, se2);
+            r2h = sh;
+            r2l += se2 + c_lo;
+          }
+          {
+            const float nh = r2h + r2l;
+            r2l = r2l - (nh - r2h);
+            r2h = nh;
+          }
+          const float rinv = rsqrtf(fmaxf(r2h, 1e-30f));
+          const float rh = r2h * rinv;
+          const float rl = (fmaf(-rh, rh, r2h) + r2l) * (0.5f * rinv);
+          float ph, pl;
+          if constexpr (KIND == PGPU_RBF_BH3) {
+            ph = rh;
+            pl = rl;
+          } else {
+            ph = rh * r2h;
+            pl = fmaf(rh, r2h, -ph) + fmaf(rh, r2l, rl * r2h);
+          }
+          const float wh = s_p[6][j], wl = s_p[7][j];
+          const float th = wh * ph;
+          const float tl = fmaf(wh, ph, -th) + fmaf(wh, pl, wl * ph);
+          float sh, e2;
+          ff_two_sum(ah, th, sh, e2);
+          al += e2 + tl;
+          ah = sh;
+        }
+        tot += static_cast<double>(ah) + static_cast<double>(al);
+      }
+    }
+    const double scale = KIND == PGPU_RBF_BH3 ? -kp.p0 : kp.p0;
+    if (active) out[tperm[i]] += scale * tot;
+  }
+}
+
 template <class T>
 __global__ void count_pairs_kernel(const Index* __restrict__ tleaf_start, Index ntl,
                                    const int* __restrict__ table,
@@ -1045,6 +1159,9 @@ struct M2LOps {
   int r = 0;  // padded rank; 0 = dense operators in K
   std::shared_ptr<DevBuf<T>> K;
   DevBuf<T> U, V, C;
+  // Tensor-core operator blocks (FP32, order 6), made on first use under tc_mu.
+  std::mutex tc_mu;
+  std::shared_ptr<M2LTcBlocks> tc;
 };
 
 struct SvdBasis {
@@ -1205,6 +1322,9 @@ struct Fmm<T>::Impl {
   // FP64 near field for an FP32 tree (set_near_fp64).
   bool near64 = false;
   KParams<double> kp64{};
+  // Timeout flag of the tensor-core M2L (set on the device, checked after each evaluation).
+  DevBuf<int> tc_err;
+  bool tc_used = false;
 
   Tree<T>& ttree() { return symmetric ? src : trg; }
 
@@ -1394,8 +1514,29 @@ struct Fmm<T>::Impl {
         PGPU_LAUNCH_CHECK();
       }
       if (src.ncell[k] > 0) {
-        const M2LOps<T>& ops = *kmats[k];
-        if (ops.r == 0) {
+        M2LOps<T>& ops = *kmats[k];
+        bool tc = false;
+        if constexpr (sizeof(T) == 4 && P3 == 216) {
+          tc = ops.r == 0 && n_t >= m2l_tc_min_cells() && m2l_tc_enabled();
+          if (tc) {
+            std::shared_ptr<M2LTcBlocks> blocks;
+            {
+              std::lock_guard<std::mutex> lk(ops.tc_mu);
+              if (!ops.tc) ops.tc = std::make_shared<M2LTcBlocks>(make_m2l_tc_blocks(ops.K->data()));
+              blocks = ops.tc;
+            }
+            if (!tc_used) {
+              tc_err.resize(1);
+              tc_err.zero();
+              tc_used = true;
+            }
+            ProfScope ps("fmm_m2l_tc", 2.0 * P3 * P3 * static_cast<double>(m2l_pairs[k]));
+            m2l_tc_apply(*blocks, m2l_table[k].data(), n_t, M[k].data(), L[k].data(),
+                         tc_err.data(), st);
+          }
+        }
+        if (tc) {
+        } else if (ops.r == 0) {
           ProfScope ps(f32 ? "fmm_m2l_f32" : "fmm_m2l_f64",
                        2.0 * P3 * P3 * static_cast<double>(m2l_pairs[k]));
           (void)smem;
@@ -1458,6 +1599,12 @@ struct Fmm<T>::Impl {
         case 8: run_far<8>(st, out); break;
         default: run_far<6>(st, out); break;
       }
+      if (tc_used) {
+        int e = 0;
+        PGPU_CUDA(cudaMemcpyAsync(&e, tc_err.data(), sizeof(int), cudaMemcpyDeviceToHost, st));
+        sync();
+        if (e != 0) throw Error(PGPU_RUNTIME_ERROR, "tensor-core M2L: a wait timed out");
+      }
     }
     const Index ntl = tt.ncell[lf];
     if (ntl > 0 && fp64_near) {
@@ -1467,15 +1614,28 @@ struct Fmm<T>::Impl {
       gather_w_kernel<double><<<blocks_for(ns, 256), 256, 0, st>>>(w64, src.perm.data(), ns,
                                                                    sw64.data());
       PGPU_LAUNCH_CHECK();
-      ProfScope ps("fmm_p2p_f64", pair_flops(kind) * static_cast<double>(near_pairs));
-      dispatch_kind(kind, [&]<int K>() {
-        p2p_kernel<K, double><<<static_cast<unsigned>(ntl), 128, 0, st>>>(
-            kp64, tt.pos64.data(), tt.perm.data(), tt.start[lf].data(), p2p_table.data(),
-            src.pos64.data(), sw64.data(), src.start[lf].data(),
-            box.width / static_cast<double>(1 << lf), out);
-        return 0;
-      });
-      PGPU_LAUNCH_CHECK();
+      const double wl = box.width / static_cast<double>(1 << lf);
+      if (kind == PGPU_RBF_BH3 || kind == PGPU_RBF_TH3) {
+        ProfScope ps("fmm_p2p_ff", pair_flops(kind) * static_cast<double>(near_pairs));
+        if (kind == PGPU_RBF_BH3)
+          p2p_ff_kernel<PGPU_RBF_BH3><<<static_cast<unsigned>(ntl), 128, 0, st>>>(
+              kp64, tt.pos64.data(), tt.perm.data(), tt.start[lf].data(), p2p_table.data(),
+              src.pos64.data(), sw64.data(), src.start[lf].data(), wl, out);
+        else
+          p2p_ff_kernel<PGPU_RBF_TH3><<<static_cast<unsigned>(ntl), 128, 0, st>>>(
+              kp64, tt.pos64.data(), tt.perm.data(), tt.start[lf].data(), p2p_table.data(),
+              src.pos64.data(), sw64.data(), src.start[lf].data(), wl, out);
+        PGPU_LAUNCH_CHECK();
+      } else {
+        ProfScope ps("fmm_p2p_f64", pair_flops(kind) * static_cast<double>(near_pairs));
+        dispatch_kind(kind, [&]<int K>() {
+          p2p_kernel<K, double><<<static_cast<unsigned>(ntl), 128, 0, st>>>(
+              kp64, tt.pos64.data(), tt.perm.data(), tt.start[lf].data(), p2p_table.data(),
+              src.pos64.data(), sw64.data(), src.start[lf].data(), wl, out);
+          return 0;
+        });
+        PGPU_LAUNCH_CHECK();
+      }
     } else if (ntl > 0) {
       ProfScope ps(sizeof(T) == 4 ? "fmm_p2p_f32" : "fmm_p2p_f64",
                    pair_flops(kind) * static_cast<double>(near_pairs));

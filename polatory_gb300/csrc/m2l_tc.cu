@@ -1,0 +1,483 @@
+// Tensor-core M2L for the FP32 far field at order 6 (p^3 = 216 interpolation nodes per cell).
+//
+// One CTA owns 128 target cells of a level (one M = 128 tile). For every offset o present
+// among its cells and every 16-node chunk of the source nodes it forms
+//   D_o[cell][a] = sum_b M_{s(cell, o)}[b] * K_o[a][b]
+// with tcgen05.mma (kind::tf32, M = 128, N = 224, K = 8) into one of two TMEM accumulators
+// (offsets alternate between them). While the tensor core fills one, the CTA adds the other,
+// complete, offset into per-thread FP32 running sums (round-to-nearest): the tensor core's own
+// accumulation then spans 81 products only, which keeps its rounding from building up over the
+// ~300 offsets of a cell. Nothing leaves the SM but the final sums; the result is
+// deterministic. FP32 accuracy comes from splitting both operands into a TF32 head and tail:
+//   A B ~ A_hi B_hi + A_hi B_lo + A_lo B_hi   (relative error about 2^-22 per product).
+// The operator chunks (head and tail, 224 x 16 each, already in the canonical no-swizzle
+// K-major core-matrix layout) arrive by bulk TMA copies completing on an mbarrier; the gathered
+// multipole rows arrive by cp.async, and their head/tail split is computed in shared memory.
+// Four pipeline stages: while the tensor core works on one stage, the CTA fills the next.
+//
+// Layout of one operand chunk in shared memory (no swizzle, K-major): core matrices of 8 rows x
+// 16 bytes (4 TF32 values) stored contiguously (128 B); the 4 core matrices of one 8-row group
+// along K are adjacent (leading-dimension byte offset 128 B) and consecutive 8-row groups are
+// 512 B apart (stride-dimension byte offset).
+//
+// Every wait on an mbarrier is bounded; a wait that runs out sets *err, the CTA drains the work
+// it has in flight, frees its TMEM and returns.
+#include <algorithm>
+#include <cstdint>
+#include <mutex>
+
+#include "common.hpp"
+#include "m2l_tc.hpp"
+#include "profile.hpp"
+
+namespace pgpu {
+
+namespace {
+
+constexpr int kD = 216;           // p^3 at order 6
+constexpr int kN = 224;           // MMA N (target nodes, padded)
+constexpr int kChunk = 16;        // source nodes per pipeline step
+constexpr int kChunks = 14;       // ceil(216 / 16)
+constexpr int kCells = 128;       // target cells per CTA (one M = 128 tile)
+constexpr int kStages = 4;
+constexpr int kNOffsets = 343;
+constexpr int kAFloats = kCells * kChunk;  // 2048
+constexpr int kBFloats = kN * kChunk;      // 3584
+constexpr int kStageFloats = 2 * kAFloats + 2 * kBFloats;
+constexpr uint32_t kBBytes = kBFloats * 4;  // 14336
+constexpr int kTmemCols = 512;
+constexpr int kBars = 2 * kStages + 3;  // loads, stage releases, two accumulators, final drain
+
+// Shared-memory layout (bytes from a 1024-aligned base).
+constexpr int kSmemStages = kStages * kStageFloats * 4;        // 180,224
+constexpr int kSmemBars = kSmemStages;
+constexpr int kSmemMisc = kSmemBars + 8 * kBars;               // tmem address, flags
+constexpr int kSmemList = kSmemMisc + 16;                      // offset list (343 ints)
+constexpr int kSmemMask = kSmemList + 4 * kNOffsets;           // offset bitmask (11 words)
+constexpr int kSmemTotal = kSmemMask + 4 * 12;
+constexpr int kSmemLaunch = kSmemTotal + 1024;                 // room to align the base
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ float tf32_round(float x) {
+  uint32_t u = __float_as_uint(x);
+  u = (u + 0x1000u) & 0xFFFFE000u;
+  return __uint_as_float(u);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: about two seconds at most.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (int it = 0; it < (1 << 21); ++it) {
+    if (mbar_try(bar, parity)) return true;
+    __nanosleep(256);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
+                                         uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src),
+               "r"(src_bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor: no swizzle, K-major, LBO 128 B, SBO 512 B.
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((saddr >> 4) & 0x3FFFu);
+  d |= static_cast<uint64_t>(128u >> 4) << 16;
+  d |= static_cast<uint64_t>(512u >> 4) << 32;
+  d |= static_cast<uint64_t>(1u) << 46;  // descriptor version
+  return d;                              // base offset 0, layout type 0 (no swizzle)
+}
+
+// Instruction descriptor: kind::tf32, FP32 accumulate, A and B K-major, M = 128, N = 224.
+constexpr uint32_t kIdesc = (1u << 4)             // D format F32
+                            | (2u << 7)           // A format TF32
+                            | (2u << 10)          // B format TF32
+                            | ((kN >> 3) << 17)   // N / 8
+                            | ((128u >> 4) << 24);  // M / 16
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// Offset of element (row, k) of a 128-row-tile chunk in the core-matrix layout (floats).
+__device__ __host__ __forceinline__ int core_off(int row, int k) {
+  return (row >> 3) * 128 + (k >> 2) * 32 + (row & 7) * 4 + (k & 3);
+}
+
+__global__ void __launch_bounds__(256, 1)
+    m2l_tc_kernel(const float* __restrict__ kb_hi, const float* __restrict__ kb_lo,
+                  const int* __restrict__ table, Index nt, const float* __restrict__ Ms,
+                  float* __restrict__ L, float* __restrict__ part, int* __restrict__ err) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  float* stage_f = reinterpret_cast<float*>(smem);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kSmemBars);
+  uint32_t* misc = reinterpret_cast<uint32_t*>(smem + kSmemMisc);  // [0] tmem, [1] abort, [2] n
+  int* olist = reinterpret_cast<int*>(smem + kSmemList);
+  uint32_t* omask = reinterpret_cast<uint32_t*>(smem + kSmemMask);
+  // mbarriers: [0, kStages) operand loads, [kStages, 2 kStages) stage released by the MMAs,
+  // [2 kStages, 2 kStages + 2) accumulator of an offset complete.
+  auto load_bar = [&](int s) { return smem_u32(&bars[s]); };
+  auto free_bar = [&](int s) { return smem_u32(&bars[kStages + s]); };
+  auto acc_bar = [&](int b) { return smem_u32(&bars[2 * kStages + b]); };
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  const Index t0 = static_cast<Index>(blockIdx.x) * kCells;
+  // Gather role: thread tid loads row tid % 128, k-groups 2 (tid / 128) and 2 (tid / 128) + 1.
+  const int g_row = tid & 127;
+  const int g_j0 = 2 * (tid >> 7);
+  const Index g_cell = t0 + g_row;
+  const bool g_valid = g_cell < nt;
+  // Drain role: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its cells), columns
+  // 112 (w / 4) .. + 111.
+  const int lane_base = 32 * (warp & 3);
+  const int col_base = 112 * (warp >> 2);
+  const Index d_cell = t0 + lane_base + (tid & 31);
+
+  // Offsets present among the CTA's cells.
+  if (tid < 12) omask[tid] = 0;
+  __syncthreads();
+  if (tid < kCells && g_valid) {
+    const int* row = table + g_cell * kNOffsets;
+    for (int o = 0; o < kNOffsets; ++o)
+      if (row[o] >= 0) atomicOr(&omask[o >> 5], 1u << (o & 31));
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int n = 0;
+    for (int o = 0; o < kNOffsets; ++o)
+      if (omask[o >> 5] & (1u << (o & 31))) olist[n++] = o;
+    misc[2] = static_cast<uint32_t>(n);
+    misc[1] = 0;
+    for (int s = 0; s < kBars; ++s) mbar_init(smem_u32(&bars[s]), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // Group blockIdx.y of gridDim.y takes a contiguous share of the offsets; with several groups
+  // each writes its partial sums to part (summed afterwards in group order).
+  const int n_all = static_cast<int>(misc[2]);
+  const int groups = static_cast<int>(gridDim.y);
+  const int q_beg = static_cast<int>((static_cast<long>(blockIdx.y) * n_all) / groups);
+  const int q_end = static_cast<int>((static_cast<long>(blockIdx.y + 1) * n_all) / groups);
+  const int n_off = q_end - q_beg;
+  float* out_base = groups == 1 ? L : part + static_cast<Index>(blockIdx.y) * nt * kD;
+  if (n_off == 0) {
+    if (groups > 1 && d_cell < nt) {
+      float* dst = out_base + d_cell * kD + col_base;
+      for (int j = 0; j < 112 && col_base + j < kD; ++j) dst[j] = 0.0f;
+    }
+    return;
+  }
+
+  // TMEM: two accumulators of 224 columns (columns 0 and 256), one per offset in turn.
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&misc[0])),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = misc[0];
+
+  // Running sums of this thread's 112 columns, accumulated in FP32 with round-to-nearest.
+  float sum[112];
+#pragma unroll
+  for (int j = 0; j < 112; ++j) sum[j] = 0.0f;
+  bool ok = true;
+  // Adds the accumulator of offset q (complete once acc_bar fires) into the running sums.
+  auto drain = [&](int q) {
+    const int b = q & 1;
+    if (!mbar_wait(acc_bar(b), (q >> 1) & 1)) {
+      ok = false;
+      return;
+    }
+    tc_fence_after();
+    const uint32_t base = tmem + (static_cast<uint32_t>(lane_base) << 16) +
+                          static_cast<uint32_t>(b * 256 + col_base);
+#pragma unroll
+    for (int u = 0; u < 7; ++u) {
+      float v[16];
+      tmem_ld16(base + static_cast<uint32_t>(16 * u), v);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) sum[16 * u + j] += v[j];
+    }
+    tc_fence_before();
+  };
+
+  const int n_iter = n_off * kChunks;
+  auto a_hi = [&](int s) { return stage_f + s * kStageFloats; };
+  auto a_lo = [&](int s) { return stage_f + s * kStageFloats + kAFloats; };
+  auto b_hi = [&](int s) { return stage_f + s * kStageFloats + 2 * kAFloats; };
+  auto b_lo = [&](int s) { return stage_f + s * kStageFloats + 2 * kAFloats + kBFloats; };
+
+  // Issues the loads of iteration i into stage i % kStages.
+  auto load = [&](int i) {
+    const int s = i % kStages;
+    const int o = olist[q_beg + i / kChunks];
+    const int c = i % kChunks;
+    if (tid == 0) {
+      mbar_expect_tx(load_bar(s), 2 * kBBytes);
+      const size_t blk = (static_cast<size_t>(o) * kChunks + c) * kBFloats;
+      bulk_g2s(smem_u32(b_hi(s)), kb_hi + blk, kBBytes, load_bar(s));
+      bulk_g2s(smem_u32(b_lo(s)), kb_lo + blk, kBBytes, load_bar(s));
+    }
+    const int src = g_valid ? table[g_cell * kNOffsets + o] : -1;
+    float* dst = a_hi(s);
+#pragma unroll
+    for (int jj = 0; jj < 2; ++jj) {
+      const int j = g_j0 + jj;
+      const int k = c * kChunk + 4 * j;
+      const bool have = src >= 0 && k < kD;
+      const float* g = have ? Ms + static_cast<Index>(src) * kD + k : Ms;
+      cp_async16(smem_u32(dst + core_off(g_row, 4 * j)), g, have ? 16u : 0u);
+    }
+    cp_async_commit();
+  };
+
+  load(0);
+  for (int i = 0; i < n_iter; ++i) {
+    const int s = i % kStages;
+    const int q = i / kChunks;
+    const int c = i % kChunks;
+    if (i + 1 < n_iter) {
+      const int s1 = (i + 1) % kStages;
+      // Stage s1 was last read by the MMAs of iteration i + 1 - kStages.
+      if (i + 1 >= kStages && !mbar_wait(free_bar(s1), ((i + 1) / kStages - 1) & 1)) ok = false;
+      load(i + 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    // The accumulator that offset q + 1 will overwrite holds offset q - 1: drain it now.
+    if (c == 1 && q >= 1) drain(q - 1);
+    // Head/tail split of this thread's gathered segments.
+#pragma unroll
+    for (int jj = 0; jj < 2; ++jj) {
+      const int off = core_off(g_row, 4 * (g_j0 + jj));
+      float4* ph = reinterpret_cast<float4*>(a_hi(s) + off);
+      float4* pl = reinterpret_cast<float4*>(a_lo(s) + off);
+      const float4 x = *ph;
+      const float4 h{tf32_round(x.x), tf32_round(x.y), tf32_round(x.z), tf32_round(x.w)};
+      *ph = h;
+      *pl = float4{x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w};
+    }
+    fence_proxy_async();
+    if (!ok) atomicExch(reinterpret_cast<int*>(&misc[1]), 1);
+    __syncthreads();
+    if (misc[1] != 0) break;
+    if (tid == 0) {
+      if (!mbar_wait(load_bar(s), (i / kStages) & 1)) {
+        atomicExch(reinterpret_cast<int*>(&misc[1]), 1);
+      } else {
+        tc_fence_after();
+        const uint32_t d = tmem + static_cast<uint32_t>((q & 1) * 256);
+        const uint32_t ah = smem_u32(a_hi(s)), al = smem_u32(a_lo(s));
+        const uint32_t bh = smem_u32(b_hi(s)), bl = smem_u32(b_lo(s));
+#pragma unroll
+        for (int ks = 0; ks < 2; ++ks) {
+          const uint32_t ko = static_cast<uint32_t>(ks * 256);
+          // The first product of an offset overwrites its accumulator.
+          mma_tf32(d, make_desc(ah + ko), make_desc(bh + ko), (c == 0 && ks == 0) ? 0u : 1u);
+          mma_tf32(d, make_desc(ah + ko), make_desc(bl + ko), 1u);
+          mma_tf32(d, make_desc(al + ko), make_desc(bh + ko), 1u);
+        }
+        mma_commit(free_bar(s));
+        if (c == kChunks - 1) mma_commit(acc_bar(q & 1));
+      }
+    }
+  }
+  cp_async_wait<0>();
+  __syncthreads();
+  bool aborted = misc[1] != 0;
+  if (!aborted) {
+    drain(n_off - 1);
+    if (!ok) atomicExch(reinterpret_cast<int*>(&misc[1]), 1);
+  }
+  // Drain every MMA still in flight before TMEM is freed.
+  if (tid == 0) mma_commit(smem_u32(&bars[kBars - 1]));
+  const bool drained = mbar_wait(smem_u32(&bars[kBars - 1]), 0);
+  __syncthreads();
+  aborted = misc[1] != 0 || !drained;
+  if (tid == 0 && aborted) atomicExch(err, 1);
+  if (!aborted && d_cell < nt) {
+    float* dst = out_base + d_cell * kD + col_base;
+    if (groups == 1) {
+#pragma unroll
+      for (int j = 0; j < 112; ++j)
+        if (col_base + j < kD) dst[j] += sum[j];
+    } else {
+#pragma unroll
+      for (int j = 0; j < 112; ++j)
+        if (col_base + j < kD) dst[j] = sum[j];
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols)
+                 : "memory");
+  }
+}
+
+// Operator chunks in the core-matrix layout: for offset o and chunk c, the 224 x 16 block
+// B[a][b'] = K_o[a][16 c + b'] (zero outside 216 x 216), head and tail.
+__global__ void m2l_tc_blocks_kernel(const float* __restrict__ K, float* __restrict__ hi,
+                                     float* __restrict__ lo) {
+  const Index total = static_cast<Index>(kNOffsets) * kChunks * kBFloats;
+  for (Index e = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x; e < total;
+       e += static_cast<Index>(gridDim.x) * blockDim.x) {
+    const Index blk = e / kBFloats;
+    const int o = static_cast<int>(blk / kChunks), c = static_cast<int>(blk % kChunks);
+    const int w = static_cast<int>(e % kBFloats);
+    // Invert core_off: w = (a / 8) * 128 + (kk / 4) * 32 + (a % 8) * 4 + kk % 4.
+    const int a = (w / 128) * 8 + (w % 32) / 4;
+    const int kk = ((w % 128) / 32) * 4 + (w % 4);
+    const int b = c * kChunk + kk;
+    const float v = (a < kD && b < kD) ? K[(static_cast<Index>(o) * kD + a) * kD + b] : 0.0f;
+    const float h = tf32_round(v);
+    hi[e] = h;
+    lo[e] = tf32_round(v - h);
+  }
+}
+
+}  // namespace
+
+bool m2l_tc_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("PGPU_M2L_TC");
+    return e == nullptr || std::atoi(e) != 0;
+  }();
+  return on;
+}
+
+M2LTcBlocks make_m2l_tc_blocks(const float* K) {
+  M2LTcBlocks b;
+  const size_t n = static_cast<size_t>(kNOffsets) * kChunks * kBFloats;
+  b.hi.resize(n);
+  b.lo.resize(n);
+  m2l_tc_blocks_kernel<<<8 * num_sms(), 256, 0, stream()>>>(K, b.hi.data(), b.lo.data());
+  PGPU_LAUNCH_CHECK();
+  sync();  // the blocks are shared with other threads' streams
+  return b;
+}
+
+Index m2l_tc_min_cells() { return 1; }
+
+__global__ void m2l_tc_reduce_kernel(const float* __restrict__ part, int groups, Index n,
+                                     float* __restrict__ L) {
+  const Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = 0.0f;
+  for (int g = 0; g < groups; ++g) s += part[static_cast<Index>(g) * n + i];
+  L[i] += s;
+}
+
+void m2l_tc_apply(const M2LTcBlocks& b, const int* table, Index nt, const float* Ms, float* L,
+                  int* err, cudaStream_t st) {
+  if (nt <= 0) return;
+  static std::once_flag attr_flag;
+  std::call_once(attr_flag, [] {
+    PGPU_CUDA(cudaFuncSetAttribute(m2l_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   kSmemLaunch));
+  });
+  const Index tiles = (nt + kCells - 1) / kCells;
+  // Small levels split each tile's offsets over several CTAs so that about two waves run.
+  const int groups = static_cast<int>(
+      std::min<Index>(16, std::max<Index>(1, (2 * num_sms() + tiles - 1) / tiles)));
+  DevBuf<float> part;
+  if (groups > 1) part.resize(static_cast<size_t>(groups) * nt * kD);
+  m2l_tc_kernel<<<dim3(static_cast<unsigned>(tiles), groups), 256, kSmemLaunch, st>>>(
+      b.hi.data(), b.lo.data(), table, nt, Ms, L, part.data(), err);
+  PGPU_LAUNCH_CHECK();
+  if (groups > 1) {
+    const Index n = nt * kD;
+    m2l_tc_reduce_kernel<<<blocks_for(n, 256), 256, 0, st>>>(part.data(), groups, n, L);
+    PGPU_LAUNCH_CHECK();
+  }
+}
+
+}  // namespace pgpu

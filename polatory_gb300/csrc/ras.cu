@@ -155,13 +155,26 @@ __global__ void potrf_diag_kernel(int kb, const int* __restrict__ lds,
   for (int c = 0; c < NB; ++c) a[lane][c] = m[lane + static_cast<Index>(c) * ld];
   __syncwarp();
   int modified = 0;
+  // FP32 factors: pivots below 2^-20 of the block's largest diagonal entry are raised to it, so
+  // that an ill-conditioned domain matrix gives a bounded (approximate) factor instead of one
+  // that overflows.
+  T floor_d = T(0);
+  if constexpr (sizeof(T) == 4) {
+    if (lane == 0) {
+      T dmax = T(0);
+      for (int j = 0; j < NB; ++j) dmax = fmax(dmax, fabs(a[j][j]));
+      floor_d = dmax * T(9.5367431640625e-07);
+    }
+  }
   for (int j = 0; j < NB; ++j) {
     if (lane == 0) {
       T dj = a[j][j];
-      if (!(dj > T(0))) {
+      if (!(dj > floor_d)) {
         // Modified pivot (the matrix lost definiteness to rounding): the preconditioner only
-        // needs an approximate factor, so continue with |d| (or 1 when d vanished).
+        // needs an approximate factor, so continue with |d| (or 1 when d vanished), at least
+        // the floor above.
         dj = fabs(dj) > T(0) ? T(fabs(dj)) : T(1);
+        if (dj < floor_d) dj = floor_d;
         ++modified;
       }
       a[j][j] = sqrt(dj);

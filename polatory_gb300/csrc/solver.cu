@@ -26,6 +26,12 @@ namespace pgpu {
 
 namespace {
 
+// Raised by the mixed path when an FP32 stage produced a non-finite value; fit() then runs the
+// plain FP64 path instead.
+struct NonFinite : Error {
+  NonFinite() : Error(PGPU_RUNTIME_ERROR, "non-finite value in the mixed-precision solve") {}
+};
+
 // 2^30 pairs: an FP64 direct sum of this size takes a few milliseconds.
 constexpr double kMixedMinPairs = 1073741824.0;
 
@@ -168,6 +174,7 @@ struct Convergence {
   bool converged = false;
   double residual = 0;
   bool exact = false;
+  double probe_rms = 0;  // root mean square of the exact residual at the probe points
 };
 
 // ResidualEvaluator (residual_evaluator.hpp:56-151), value points only.
@@ -238,6 +245,8 @@ class ResidualEvaluator {
         axpy(n_probe_, nugget, tmp_.data(), fit_.data());
       }
       cv.residual = inf_norm_diff(fit_.data(), probe_values_.data(), n_probe_);
+      axpby(n_probe_, 1.0, probe_values_.data(), -1.0, fit_.data());
+      cv.probe_rms = norm2(fit_.data(), n_probe_) / std::sqrt(static_cast<double>(n_probe_));
       cv.exact = n_probe_ == mu_;
       if (cv.residual > tol) return cv;
       if (cv.exact) {
@@ -378,10 +387,11 @@ FitResult fit_impl(const FitRequest& req) {
     }
     if (req.verbose) std::printf("%8s%16s\n", "iter", "residual");
     // The reference's operator (accuracy 0) interpolates the far field at a high order. Here the
-    // operator starts at order 6; when the Krylov residual estimate has run far below the
-    // tolerance while the checked residual stays above it, the far-field error is what remains:
-    // the order of the operator (and of the full residual check, unless an accuracy was given)
-    // is raised to 8 once, FGMRES restarting from the current weights.
+    // operator starts at order 6; when the Krylov residual estimate (root mean square) has run
+    // ten times below the exact residual's root mean square at the probe points while the check
+    // fails, the operator's far-field error is what remains: the order of the operator (and of
+    // the full residual check, unless an accuracy was given) is raised to 8 once, FGMRES
+    // restarting from the current weights.
     int order = 6;
     op.set_order(order);
     int base = 0;
@@ -395,7 +405,7 @@ FitResult fit_impl(const FitRequest& req) {
       if (total >= req.max_iter)
         throw Error(PGPU_MAX_ITER, "reached the maximum number of iterations");
       const double est_rms = solver.absolute_residual() / std::sqrt(static_cast<double>(mu));
-      if (order < 8 && solver.iteration_count() > 0 && est_rms < 0.1 * req.tolerance) {
+      if (order < 8 && solver.iteration_count() > 0 && est_rms < 0.1 * cv.probe_rms) {
         order = 8;
         op.set_order(order);
         re.set_default_order(order);
@@ -472,39 +482,81 @@ FitResult fit_impl(const FitRequest& req) {
     solver.setup(rhs.data(), w.data(), x0_zero, inner);
     int base = 0;  // iterations before the current restart
     double cycle_start_residual = INFINITY;
+    // Ratio of the inf-norm to the root mean square of the last recomputed residual. The next
+    // check waits until the estimate times this ratio predicts at most twice the tolerance.
+    double peak_ratio = 1.0;
     while (true) {
       const double est_rms = solver.absolute_residual() / std::sqrt(static_cast<double>(mu));
       total = base + solver.iteration_count();
-      if (solver.iteration_count() > 0 && est_rms > req.tolerance) {
+      const bool fresh = solver.iteration_count() == 0;
+      if (fresh && x0_zero && base == 0) {
+        // Zero weights: the residual is the data itself, no operator needed.
+        res.residual = inf_norm_diff(rhs.data(), zero.data(), mu);
+        peak_ratio = std::max(1.0, res.residual / est_rms);
+        if (req.verbose) std::printf("%8d    %12.6e\n", total, res.residual);
+        if (res.residual <= req.tolerance) break;
+      } else if (!fresh && std::isfinite(est_rms) &&
+                 (est_rms > req.tolerance || est_rms * peak_ratio > 2.0 * req.tolerance)) {
         if (req.verbose) std::printf("%8d   ~%12.6e (estimate)\n", total, est_rms);
       } else {
         solver.solution(w.data());
         double rinf = residual();
-        if (rinf <= req.tolerance && residual_grade != kFp64) {
+        bool converged = false;
+        // Near the tolerance the residual operator must resolve it: its largest deviation from
+        // exact FP64 sums at the probe points must be at most half the tolerance, else the next
+        // grade takes the residuals from here on.
+        while (residual_grade < kFp64 && rinf <= 4.0 * req.tolerance && std::isfinite(rinf)) {
           const Index np = re.n_probe();
           const double* rp = re.probe_residual(w.data());
           gather(r.data(), re.probe_idx(), np, rp32.data());
           const double dev = inf_norm_diff(rp32.data(), rp, np);
           const double rprobe = inf_norm_diff(rp, zero.data(), np);
           if (req.verbose)
-            std::printf("%8d    %12.6e (hybrid), probe %12.6e, deviation %9.3e\n", total, rinf,
-                        rprobe, dev);
-          if (rprobe <= req.tolerance && dev <= 0.5 * req.tolerance) {
-            res.residual = std::max(rinf, rprobe);
+            std::printf("%8d    %12.6e (grade %d), probe %12.6e, deviation %9.3e\n", total, rinf,
+                        residual_grade, rprobe, dev);
+          if (dev <= 0.5 * req.tolerance) {
+            converged = rinf <= req.tolerance && rprobe <= req.tolerance;
+            if (converged) rinf = std::max(rinf, rprobe);
             break;
           }
-          residual_grade = kFp64;
+          ++residual_grade;
           rinf = residual();
         }
+        const double rtrue = norm2(r.data(), M);
+        if (!std::isfinite(rinf) || !std::isfinite(rtrue) || !std::isfinite(est_rms))
+          throw NonFinite();
         res.residual = rinf;
         if (req.verbose) std::printf("%8d    %12.6e\n", total, rinf);
-        if (rinf <= req.tolerance) break;
-        const double rtrue = norm2(r.data(), M);
+        if (converged || (residual_grade == kFp64 && rinf <= req.tolerance)) break;
+        peak_ratio = std::max(1.0, rinf / (rtrue / std::sqrt(static_cast<double>(M))));
         if (solver.iteration_count() > 0 && solver.absolute_residual() < 0.1 * rtrue) {
-          if (inner.grade < kFp64 && rinf > 0.5 * cycle_start_residual) {
-            ++inner.grade;
-            if (req.verbose)
-              std::printf("%8d    inner operator grade %d\n", total, inner.grade);
+          if (rinf > 0.5 * cycle_start_residual) {
+            // The last cycle did not halve the residual. If the residual operator's own error
+            // is a quarter of the residual or more, it is the residual grade that rises (the
+            // refinement was chasing its rounding); otherwise the inner operator's.
+            bool raised = false;
+            if (residual_grade < kFp64) {
+              const Index np = re.n_probe();
+              const double* rp = re.probe_residual(w.data());
+              gather(r.data(), re.probe_idx(), np, rp32.data());
+              const double dev = inf_norm_diff(rp32.data(), rp, np);
+              if (dev > 0.25 * rinf) {
+                ++residual_grade;
+                rinf = residual();
+                raised = true;
+                if (req.verbose)
+                  std::printf("%8d    residual grade %d: %12.6e\n", total, residual_grade, rinf);
+                if (rinf <= req.tolerance) {
+                  res.residual = rinf;
+                  break;
+                }
+              }
+            }
+            if (!raised && inner.grade < kFp64) {
+              ++inner.grade;
+              if (req.verbose)
+                std::printf("%8d    inner operator grade %d\n", total, inner.grade);
+            }
           }
           cycle_start_residual = rinf;
           base = total;
@@ -543,12 +595,15 @@ void evaluate_impl(const EvaluateRequest& req) {
 FitResult fit(const FitRequest& req) {
   if (req.sigma > 0) throw Error(PGPU_NOT_IMPLEMENTED, "gradient data points are not supported yet");
   const double mu = static_cast<double>(req.mu);
-  if (req.precision == PGPU_PRECISION_PLAIN || !mixed_pays(mu, mu)) {
-    FitRequest plain = req;
-    plain.precision = PGPU_PRECISION_PLAIN;
+  FitRequest plain = req;
+  plain.precision = PGPU_PRECISION_PLAIN;
+  if (req.precision == PGPU_PRECISION_PLAIN || !mixed_pays(mu, mu)) return fit_impl<double>(plain);
+  try {
+    return fit_impl<float>(req);
+  } catch (const NonFinite&) {
+    if (req.verbose) std::printf("fit: non-finite value in FP32, running the FP64 path\n");
     return fit_impl<double>(plain);
   }
-  return fit_impl<float>(req);
 }
 
 void evaluate(const EvaluateRequest& req) {

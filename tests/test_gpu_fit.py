@@ -137,3 +137,28 @@ def test_max_iter_reached():
     interp = pg.Interpolant(pg.Model(pg.Biharmonic3D([1.0]), 1))
     with pytest.raises(pg.PolatoryError, match="reached the maximum number of iterations"):
         interp.fit(pts, vals, 1e-12, max_iter=2)
+
+
+@pytest.mark.parametrize("kind", ["bh3", "exp"])
+def test_fit_mixed_fmm_hybrid_residual(kind):
+    # 120k points: the FP32 operator runs the FMM and residuals are checked with the hybrid
+    # operator (FP32 far field; float-float near field for the polyharmonic kernel, FP64 for the
+    # covariance). At tol 1e-5 the biharmonic fit needs the FP64 grade for its last residuals.
+    # The exact residual at 4000 sampled data points (oracle) must be within the tolerance.
+    g = np.random.Generator(np.random.PCG64(25))
+    n = 120000
+    pts = g.random((n, 3))
+    vals = workloads.f_c1(pts)
+    if kind == "bh3":
+        model = pg.Model(pg.Biharmonic3D([1.0]), 1)
+        tol = 1e-5
+    else:
+        model = pg.Model(pg.CovExponential([1.0, 0.2]), 0)
+        model.nugget = 1e-3
+        tol = 1e-4
+    it = pg.Interpolant(model, pg.MIXED)
+    it.fit(pts, vals, tol)
+    w = it.weights
+    idx = g.choice(n, 4000, replace=False)
+    fit_vals = oracle.direct_evaluate(model, pts, w, pts[idx]) + model.nugget * w[idx]
+    assert np.max(np.abs(fit_vals - vals[idx])) <= tol

@@ -102,3 +102,40 @@ def test_fmm_empty_and_tiny():
     ev.set_target_points(np.zeros((0, 3)))
     ev.set_weights(np.ones(5))
     assert ev.evaluate().shape == (0,)
+
+
+@pytest.mark.parametrize("cls,params", [(pg.Biharmonic3D, [1.0]), (pg.Triharmonic3D, [1.0]),
+                                        (pg.CovExponential, [1.0, 0.3])],
+                         ids=["bh3", "th3", "exp"])
+def test_fmm_mixed_tensor_core_m2l(cls, params):
+    # 400k uniform sources at leaf level 5: every level runs the tensor-core M2L (TF32
+    # head/tail split; the small levels split their offsets over several CTAs). Against the
+    # FP64 FMM with the same order and tree, the difference is rounding only; against the exact
+    # sums, the order-6 bound.
+    src, trg, w = sample(400000, 4000, 33)
+    rbf = cls(params)
+    lo = np.minimum(src.min(0), trg.min(0))
+    hi = np.maximum(src.max(0), trg.max(0))
+    out = {}
+    for prec in (pg.MIXED, pg.PLAIN):
+        ev = pg.FmmEvaluator(rbf, np.concatenate([lo, hi]), precision=prec)
+        ev.configure(backend=2, order=6, leaf_level=5)
+        ev.set_source_points(src)
+        ev.set_target_points(trg)
+        ev.set_weights(w)
+        out[prec] = ev.evaluate()
+    m = pg.Model(rbf, rbf.cpd_order - 1)._c()
+    m.poly_degree = -1
+    want = oracle.direct_evaluate(m, src, w, trg)
+    # Mean |phi| over the unit cube times sum |w| (from 2000 sampled pairs).
+    g = np.random.Generator(np.random.PCG64(1))
+    i, j = g.integers(0, src.shape[0], 2000), g.integers(0, trg.shape[0], 2000)
+    phis = [oracle.rbf_evaluate(rbf._kind, rbf.parameters, rbf.anisotropy, d)[0]
+            for d in trg[j] - src[i]]
+    scale = np.abs(w).sum() * np.mean(np.abs(phis))
+    assert np.all(np.isfinite(out[pg.MIXED]))
+    d32 = np.max(np.abs(out[pg.MIXED] - out[pg.PLAIN]))
+    e64 = np.max(np.abs(out[pg.PLAIN] - want))
+    print(f"fp32 vs fp64 fmm {d32:.3e}, fp64 fmm vs exact {e64:.3e}, scale {scale:.3e}")
+    assert d32 <= 1e-6 * scale
+    assert np.max(np.abs(out[pg.MIXED] - want)) <= BOUND[6] * scale
