@@ -1,6 +1,8 @@
 // Evaluator<T> implementation: per-RBF frames (A-transformed, centred positions), weight
 // preparation, and the choice between the exact direct backend and the FMM backend.
 #include <algorithm>
+#include <numeric>
+#include <random>
 
 #include "direct.hpp"
 #include "evaluator.hpp"
@@ -119,6 +121,8 @@ struct Evaluator<T>::Term {
   std::unique_ptr<Fmm<T>> fmm;
   bool fmm_sources_dirty = true;
   bool fmm_targets_dirty = true;
+  // Far-field order chosen for a finite accuracy (0: not chosen yet).
+  int order = 0;
 };
 
 template <class T>
@@ -154,6 +158,60 @@ Evaluator<T>::Evaluator(const ModelDesc& model, const Bbox3& bbox, double accura
 template <class T>
 Evaluator<T>::~Evaluator() = default;
 
+namespace {
+
+__global__ void gather_p4_kernel(const P4<double>* __restrict__ src, const Index* __restrict__ idx,
+                                 Index n, P4<double>* __restrict__ dst) {
+  const Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[idx[i]];
+}
+
+}  // namespace
+
+// FmmAccuracyEstimator::find_best_configuration (fmm_accuracy_estimator.hpp:74-121): up to
+// 10,000 of the source points (a default-seeded std::mt19937 shuffle) are the sample targets;
+// their exact FP64 sums are compared with the FMM at increasing orders (4, 6, 8 here; the
+// reference's uniform interpolation tries 8 to 20), and the first order whose inf-norm error is
+// within the accuracy is kept. None: "failed to construct an evaluator that meets the desired
+// accuracy".
+template <class T>
+int Evaluator<T>::estimate_order(Term& t, double accuracy) {
+  const Index ns = std::min<Index>(mu_, 10000);
+  std::vector<Index> idx(mu_);
+  std::iota(idx.begin(), idx.end(), Index{0});
+  std::shuffle(idx.begin(), idx.end(), std::mt19937{});
+  idx.resize(ns);
+  DevBuf<Index> di;
+  di.upload(idx);
+  DevBuf<P4<double>> samp(ns);
+  gather_p4_kernel<<<blocks_for(ns, 256), 256, 0, stream()>>>(t.spos_d.data(), di.data(), ns,
+                                                              samp.data());
+  PGPU_LAUNCH_CHECK();
+  DevBuf<double> exact(ns), approx(ns);
+  exact.zero();
+  {
+    DirectSources<double> src{t.spos_d.data(), w_, mu_, nullptr, nullptr, 0};
+    DirectTargets<double> trg{samp.data(), ns, exact.data(), nullptr, 0, nullptr};
+    direct_evaluate<double>(t.rbf.kind, t.kp64, t.a, src, trg, stream());
+  }
+  double rel_min[3];
+  for (int k = 0; k < 3; ++k) rel_min[k] = t.box_min[k] - t.origin[k];
+  for (int p : {4, 6, 8}) {
+    Fmm<T> f(t.rbf.kind, t.kp, t.a, rel_min, t.box_width, accuracy);
+    FarFieldConfig c;
+    c.order = p;
+    f.set_config(c);
+    f.set_sources(t.spos_d.data(), mu_);
+    f.set_targets(samp.data(), ns);
+    approx.zero();
+    f.evaluate(t.vw.data(), nullptr, w_, approx.data(), nullptr);
+    const double err = inf_norm_diff(approx.data(), exact.data(), ns);
+    if (verbose()) std::printf("fmm accuracy estimate: order %d error %.3e (target %.3e)\n", p, err, accuracy);
+    if (err <= accuracy) return p;
+  }
+  throw Error(PGPU_RUNTIME_ERROR, "failed to construct an evaluator that meets the desired accuracy");
+}
+
 template <class T>
 void Evaluator<T>::set_sources(const double* pts, Index mu, const double* gpts, Index sigma) {
   symmetric_ = false;
@@ -178,6 +236,7 @@ void Evaluator<T>::set_sources(const double* pts, Index mu, const double* gpts, 
     t->vw.resize(mu);
     t->gg.resize(3 * sigma);
     t->fmm_sources_dirty = true;
+    t->order = 0;  // the accuracy estimate depends on the sources (and weights)
   }
 }
 
@@ -273,12 +332,24 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
       direct_evaluate<T>(t.rbf.kind, t.kp, t.a, src, trg, stream());
       stats_.direct_pairs += static_cast<Index>(pairs);
     } else {
+      double acc = std::min(accuracy_, grad_accuracy_);
+      // Accuracy split over the RBFs (interpolation/operator.hpp:88-90).
+      const double term_acc = acc / static_cast<double>(terms_.size());
+      const bool order_free = !ff_set_ || ff_.order == 0;
+      if (order_free && std::isfinite(acc) && acc > 0.0 && t.order == 0) {
+        t.order = estimate_order(t, term_acc);
+        t.fmm.reset();
+      }
       if (!t.fmm) {
-        double acc = std::min(accuracy_, grad_accuracy_);
         double rel_min[3];
         for (int k = 0; k < 3; ++k) rel_min[k] = t.box_min[k] - t.origin[k];
-        t.fmm = std::make_unique<Fmm<T>>(t.rbf.kind, t.kp, t.a, rel_min, t.box_width, acc);
-        if (ff_set_) t.fmm->set_config(ff_);
+        t.fmm = std::make_unique<Fmm<T>>(t.rbf.kind, t.kp, t.a, rel_min, t.box_width, term_acc);
+        if (ff_set_ || t.order > 0) {
+          FarFieldConfig c = ff_set_ ? ff_ : FarFieldConfig{};
+          if (order_free && t.order > 0) c.order = t.order;
+          t.fmm->set_config(c);
+        }
+        t.fmm_sources_dirty = t.fmm_targets_dirty = true;
       }
       if (t.fmm_sources_dirty || t.fmm_targets_dirty) {
         if (symmetric_) {

@@ -90,6 +90,7 @@ class Evaluator {
 
  private:
   struct Term;
+  int estimate_order(Term& t, double accuracy);
 
   ModelDesc model_;
   Bbox3 bbox_;

@@ -1283,10 +1283,11 @@ std::shared_ptr<M2LOps<T>> m2l_ops(int kind, const KParams<T>& kp, double r_cell
 
 int order_for_accuracy(double accuracy) {
   // accuracy = inf: the reference's default order 6 (fmm_accuracy_estimator.hpp:77-79);
-  // accuracy = 0 (the fit operator): the highest order kept here.
-  // Order 6 Chebyshev already reaches ~1e-9 of the sum's conditioning on the parity tests,
-  // which the reference's order-12 uniform interpolation targets for the fit operator.
-  if (std::isinf(accuracy) || accuracy <= 0.0) return 6;
+  // accuracy = 0: the highest order kept here (the reference interpolates at order 12 on a
+  // uniform grid). A finite accuracy has its order chosen by the evaluator's estimate, which
+  // sets it explicitly; this fallback maps it by magnitude.
+  if (std::isinf(accuracy)) return 6;
+  if (accuracy <= 0.0) return 8;
   if (accuracy >= 1e-4) return 6;
   return 8;
 }

@@ -8,9 +8,11 @@
 // Mixed path (PGPU_PRECISION_MIXED): iterative refinement. The outer loop recomputes the
 // residual with the FP64 operator (same convergence test as above); each inner FGMRES runs the
 // FP32 operator and an FP32 RAS preconditioner with FP64 Krylov vectors, Arnoldi and Givens.
-// Mixed precision engages only where it pays: fits and evaluations of at most kMixedMinPairs
-// source-target pairs run the plain FP64 path (their sums are cheap, and small systems with
-// cancelling weights need FP64 sums to reach 1e-5-level tolerances).
+// Mixed precision engages FP32 sums only where they pay: fits and evaluations of at most
+// kMixedMinPairs source-target pairs keep FP64 sums (they are cheap, and small systems with
+// cancelling weights need FP64 sums to reach 1e-5-level tolerances); such fits still factor
+// and apply the preconditioner in FP32, the part of a small fit that costs the most, unless
+// the kernel's conditional positive definiteness order is 2 or more.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -376,7 +378,7 @@ FitResult fit_impl(const FitRequest& req) {
   res.setup_seconds = wall_seconds() - t0;
   double t1 = wall_seconds();
 
-  if (req.precision == PGPU_PRECISION_PLAIN) {
+  if (req.precision == PGPU_PRECISION_PLAIN || req.plain_loop) {
     // Operator at accuracy 0 as interpolation/solver.hpp:40.
     Operator<double> op(model, pts.data(), mu, bbox, 0.0, P.data());
     Fgmres solver(M, req.max_iter);
@@ -401,6 +403,7 @@ FitResult fit_impl(const FitRequest& req) {
       const int total = base + solver.iteration_count();
       if (req.verbose) std::printf("%8d%4s%12.6e\n", total, cv.exact ? "" : "~", cv.residual);
       res.residual = cv.residual;
+      if (sizeof(T) == 4 && !std::isfinite(solver.absolute_residual())) throw NonFinite();
       if (cv.converged) break;
       if (total >= req.max_iter)
         throw Error(PGPU_MAX_ITER, "reached the maximum number of iterations");
@@ -436,6 +439,7 @@ FitResult fit_impl(const FitRequest& req) {
     // tolerance (the check resolves the tolerance). Otherwise residuals are taken with the FP64
     // operator from then on.
     Operator<float> op32(model, pts.data(), mu, bbox, 0.0, P.data());
+    op32.set_order(6);  // the tensor-core M2L's order; refinement absorbs its truncation
     std::unique_ptr<Operator<double>> op64;
     auto fp64_op = [&] {
       if (!op64) {
@@ -597,8 +601,18 @@ FitResult fit(const FitRequest& req) {
   const double mu = static_cast<double>(req.mu);
   FitRequest plain = req;
   plain.precision = PGPU_PRECISION_PLAIN;
-  if (req.precision == PGPU_PRECISION_PLAIN || !mixed_pays(mu, mu)) return fit_impl<double>(plain);
+  if (req.precision == PGPU_PRECISION_PLAIN) return fit_impl<double>(plain);
+  // Kernels of conditional positive definiteness order 2 and above (triharmonic, thin-plate)
+  // give domain matrices too ill-conditioned for an FP32 Cholesky factor: their small fits keep
+  // the FP64 preconditioner.
+  if (!mixed_pays(mu, mu) && req.model->cpd_order() >= 2) return fit_impl<double>(plain);
   try {
+    if (!mixed_pays(mu, mu)) {
+      // Small systems: FP64 operator and residuals (exact direct sums), FP32 preconditioner.
+      FitRequest small = req;
+      small.plain_loop = true;
+      return fit_impl<float>(small);
+    }
     return fit_impl<float>(req);
   } catch (const NonFinite&) {
     if (req.verbose) std::printf("fit: non-finite value in FP32, running the FP64 path\n");

@@ -38,6 +38,9 @@ struct FitRequest {
   const double* initial_weights = nullptr;  // host, mu + 3 sigma + l, or null
   int precision = PGPU_PRECISION_PLAIN;
   bool verbose = false;
+  // Internal: the plain solve loop (FP64 operator and residuals) with the preconditioner in the
+  // fit's arithmetic type (set by fit() for mixed requests below the mixed-operator threshold).
+  bool plain_loop = false;
 };
 
 FitResult fit(const FitRequest& req);

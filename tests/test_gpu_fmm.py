@@ -139,3 +139,35 @@ def test_fmm_mixed_tensor_core_m2l(cls, params):
     print(f"fp32 vs fp64 fmm {d32:.3e}, fp64 fmm vs exact {e64:.3e}, scale {scale:.3e}")
     assert d32 <= 1e-6 * scale
     assert np.max(np.abs(out[pg.MIXED] - want)) <= BOUND[6] * scale
+
+
+@pytest.mark.parametrize("precision", [pg.PLAIN, pg.MIXED], ids=["plain", "mixed"])
+def test_fmm_accuracy_estimate(precision):
+    # A finite accuracy selects the order by comparing the FMM with exact sums at up to 10,000
+    # sampled source points (fmm_accuracy_estimator.hpp:74-121); an unreachable accuracy fails
+    # with the reference's message.
+    src, trg, w = sample(30000, 3000, 34)
+    rbf = pg.Biharmonic3D([1.0])
+    scale = np.abs(w).sum() * 0.66
+    acc = (1e-6 if precision == pg.PLAIN else 3e-6) * scale
+    lo = np.minimum(src.min(0), trg.min(0))
+    hi = np.maximum(src.max(0), trg.max(0))
+    ev = pg.FmmEvaluator(rbf, np.concatenate([lo, hi]), precision=precision)
+    ev.configure(backend=2, order=0, leaf_level=-1)
+    ev.set_accuracy(acc)
+    ev.set_source_points(src)
+    ev.set_target_points(trg)
+    ev.set_weights(w)
+    got = ev.evaluate()
+    m = pg.Model(rbf, 0)._c()
+    m.poly_degree = -1
+    want = oracle.direct_evaluate(m, src, w, trg)
+    assert np.max(np.abs(got - want)) <= 2.0 * acc
+    bad = pg.FmmEvaluator(rbf, np.concatenate([lo, hi]), precision=precision)
+    bad.configure(backend=2, order=0, leaf_level=-1)
+    bad.set_accuracy(1e-13 * scale)
+    bad.set_source_points(src)
+    bad.set_target_points(trg)
+    bad.set_weights(w)
+    with pytest.raises(pg.PolatoryError, match="failed to construct an evaluator"):
+        bad.evaluate()
