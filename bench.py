@@ -215,6 +215,51 @@ def run_other(args):
     print(json.dumps(line), flush=True)
 
 
+def roofline(name, region, ms_step, sms):
+    """Achieved rate of one profiled region against the peak of the unit that bounds it.
+
+    Flop regions count algorithmic flops (pairs x flops per pair, 2 p^6 per M2L interaction);
+    the tensor-core M2L executes three TF32 products per algorithmic product (head/tail split),
+    and is compared with the TF32 dense rate, half the measured BF16 rate. Byte regions count
+    algorithmic bytes. traffic: DRAM bytes per launch from an ncu capture of the same kernel
+    (profiles/traffic.json), or null."""
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    clk_max = peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = sms * 128 * 2 * clk_max * 1e6 / 1e12
+    fp64_peak = sms * 2 * 2 * clk_max * 1e6 / 1e12
+    secs = region["ms"] * 1e-3
+    if region["bytes"] > 0 and region["flops"] / max(region["bytes"], 1) < 4:
+        roof = {"bound": "hbm", "achieved": region["bytes"] / secs / 1e9,
+                "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
+                "peak_source": "hbm_gbs of measured" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"}
+    elif name == "fmm_m2l_tc":
+        bf16 = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops", 1900.0))
+        roof = {"bound": "tensor", "achieved": 3.0 * region["flops"] / secs / 1e12,
+                "peak": bf16 / 2.0, "unit": "TFLOP/s",
+                "peak_source": "TF32 dense = half the sustained BF16 rate of measured",
+                "useful_tflops": region["flops"] / secs / 1e12}
+    else:
+        f64 = "f64" in name
+        roof = {"bound": "fp64-cuda-core" if f64 else "fp32-cuda-core",
+                "achieved": region["flops"] / secs / 1e12,
+                "peak": fp64_peak if f64 else fp32_peak, "unit": "TFLOP/s",
+                "peak_source": f"nominal {'FP64' if f64 else 'FP32'} CUDA-core FMA rate: {sms} SMs x "
+                               f"{2 if f64 else 128} x 2 flops x {clk_max:.0f} MHz"}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["kernel"] = name
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        t = json.loads(tf.read_text()).get(name)
+        if t:
+            traffic = t["dram_bytes_per_launch"]
+    roof["traffic"] = traffic
+    roof["launches"] = region["calls"]
+    roof["ms_total"] = region["ms"]
+    roof["share_of_step"] = region["ms"] / ms_step
+    return roof
+
+
 def workload(scale: float):
     from polatory_gb300 import workloads
 
@@ -440,34 +485,18 @@ def main():
         return
     # Roofline of the dominant kernel (device time per region from the live CUDA events).
     dom_name, dom = max(report.items(), key=lambda kv: kv[1]["ms"])
-    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    clk_max = peaks.get("sm_max_mhz", 2070.0)
-    fp32_peak = sms * 128 * 2 * clk_max * 1e6 / 1e12  # TFLOP/s, CUDA-core FP32 FMA
-    fp64_peak = sms * 2 * 2 * clk_max * 1e6 / 1e12
-    if dom["bytes"] > 0 and dom["flops"] / max(dom["bytes"], 1) < 4:
-        achieved = dom["bytes"] / (dom["ms"] * 1e-3) / 1e9
-        roof = {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs", 6800.0),
-                "unit": "GB/s", "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
-    else:
-        achieved = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
-        f32 = dom_name.endswith("f32")
-        roof = {"bound": "fp32-cuda-core" if f32 else "fp64-cuda-core", "achieved": achieved,
-                "peak": fp32_peak if f32 else fp64_peak, "unit": "TFLOP/s",
-                "peak_source": f"nominal {'FP32' if f32 else 'FP64'} CUDA-core FMA rate: {sms} SMs x "
-                               f"{128 if f32 else 2} x 2 flops x {clk_max:.0f} MHz"}
-    roof["frac"] = roof["achieved"] / roof["peak"]
-    roof["kernel"] = dom_name
-    roof["traffic"] = None
-    roof["launches"] = dom["calls"]
-    roof["ms_total"] = dom["ms"]
-    roof["share_of_step"] = dom["ms"] / ms
+    roof = roofline(dom_name, dom, ms, sms)
+    top = sorted(report.items(), key=lambda kv: -kv[1]["ms"])[:6]
+    regions = {k: {kk: vv for kk, vv in roofline(k, v, ms, sms).items() if kk != "kernel"}
+               for k, v in top}
     cpu = None if args.no_cpu else cpu_baseline(pts, vals, q)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": cfg, "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
+        "regions": regions,
         "cpu_baseline": cpu, "clocks": clk.summary(), "plain_fp64": plain,
         "fit": {"iterations": iters, "levels": stats["levels"], "residual": stats["residual"],
                 "setup_s": stats["setup_seconds"], "solve_s": stats["solve_seconds"],

@@ -806,6 +806,46 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// Near field with one thread per target point, for target trees whose leaves hold few points
+// (evaluation points spread over a volume while the sources sit on a surface): the block-per-
+// leaf kernel above would leave most of its threads idle. Sources are read through the cache;
+// threads of one leaf read the same sources (broadcast).
+template <int KIND, class T>
+__global__ void __launch_bounds__(128)
+    p2p_point_kernel(KParams<T> kp, const P4<T>* __restrict__ tpos, const Index* __restrict__ tperm,
+                     const int* __restrict__ tleaf, Index nt, const int* __restrict__ table,
+                     const P4<T>* __restrict__ spos, const T* __restrict__ sw,
+                     const Index* __restrict__ sleaf_start, T wleaf, double* __restrict__ out) {
+  const Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= nt) return;
+  const P4<T> t = tpos[i];
+  const int* nbs = table + static_cast<Index>(tleaf[i]) * 27;
+  double tot = 0.0;
+  for (int nb = 0; nb < 27; ++nb) {
+    const int s = nbs[nb];
+    if (s < 0) continue;
+    const T tx = t.x - static_cast<T>(nb / 9 - 1) * wleaf;
+    const T ty = t.y - static_cast<T>((nb / 3) % 3 - 1) * wleaf;
+    const T tz = t.z - static_cast<T>(nb % 3 - 1) * wleaf;
+    const Index sb = sleaf_start[s], se = sleaf_start[s + 1];
+    T acc = T(0);
+    for (Index j = sb; j < se; ++j) {
+      const P4<T> q = spos[j];
+      const T dx = tx - q.x, dy = ty - q.y, dz = tz - q.z;
+      acc += rbf_value_fast<KIND>(dx * dx + dy * dy + dz * dz, kp) * sw[j];
+    }
+    tot += static_cast<double>(acc);
+  }
+  out[tperm[i]] += tot;
+}
+
+// Leaf index of every sorted point.
+__global__ void leaf_of_kernel(const Index* __restrict__ start, Index nleaf, int* __restrict__ leaf) {
+  const Index l = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (l >= nleaf) return;
+  for (Index i = start[l]; i < start[l + 1]; ++i) leaf[i] = static_cast<int>(l);
+}
+
 template <class T>
 __global__ void count_pairs_kernel(const Index* __restrict__ tleaf_start, Index ntl,
                                    const int* __restrict__ table,
@@ -1314,6 +1354,7 @@ struct Fmm<T>::Impl {
   // M2L tables per level (target cells x 343) and P2P table (target leaves x 27).
   std::vector<DevBuf<int>> m2l_table;
   DevBuf<int> p2p_table;
+  DevBuf<int> tleaf;  // leaf of each sorted target point (sparse target leaves only)
   std::vector<std::shared_ptr<M2LOps<T>>> kmats;
   std::vector<DevBuf<T>> M, L, Mt, Lt;  // Mt/Lt: compressed expansions (rank r) when used
   DevBuf<T> sw;
@@ -1416,6 +1457,15 @@ struct Fmm<T>::Impl {
       PGPU_CUDA(cudaMemcpyAsync(&h, tot.data(), sizeof(h), cudaMemcpyDeviceToHost, st));
       sync();
       near_pairs = static_cast<Index>(h);
+      const Index ntp = symmetric ? ns : nt;
+      if (!symmetric && ntp < 32 * ntl) {
+        tleaf.resize(ntp);
+        leaf_of_kernel<<<blocks_for(ntl, 128), 128, 0, st>>>(tt.start[lf].data(), ntl,
+                                                             tleaf.data());
+        PGPU_LAUNCH_CHECK();
+      } else {
+        tleaf.release();
+      }
     }
     const Index p3 = static_cast<Index>(p) * p * p;
     M.clear();
@@ -1638,15 +1688,25 @@ struct Fmm<T>::Impl {
         PGPU_LAUNCH_CHECK();
       }
     } else if (ntl > 0) {
-      ProfScope ps(sizeof(T) == 4 ? "fmm_p2p_f32" : "fmm_p2p_f64",
+      ProfScope ps(symmetric ? (sizeof(T) == 4 ? "fmm_p2p_f32" : "fmm_p2p_f64")
+                             : (sizeof(T) == 4 ? "fmm_p2p_f32_st" : "fmm_p2p_f64_st"),
                    pair_flops(kind) * static_cast<double>(near_pairs));
-      dispatch_kind(kind, [&]<int K>() {
-        p2p_kernel<K, T><<<static_cast<unsigned>(ntl), 128, 0, st>>>(
-            kp, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), p2p_table.data(),
-            src.pos.data(), sw.data(), src.start[lf].data(),
-            static_cast<T>(box.width / static_cast<double>(1 << lf)), out);
-        return 0;
-      });
+      const T wl = static_cast<T>(box.width / static_cast<double>(1 << lf));
+      if (tleaf.size() > 0) {
+        dispatch_kind(kind, [&]<int K>() {
+          p2p_point_kernel<K, T><<<blocks_for(nt, 128), 128, 0, st>>>(
+              kp, tt.pos.data(), tt.perm.data(), tleaf.data(), nt, p2p_table.data(),
+              src.pos.data(), sw.data(), src.start[lf].data(), wl, out);
+          return 0;
+        });
+      } else {
+        dispatch_kind(kind, [&]<int K>() {
+          p2p_kernel<K, T><<<static_cast<unsigned>(ntl), 128, 0, st>>>(
+              kp, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), p2p_table.data(),
+              src.pos.data(), sw.data(), src.start[lf].data(), wl, out);
+          return 0;
+        });
+      }
       PGPU_LAUNCH_CHECK();
     }
   }

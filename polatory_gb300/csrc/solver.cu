@@ -435,9 +435,9 @@ FitResult fit_impl(const FitRequest& req) {
     // accepted as the reference accepts its FMM residual (residual_evaluator.hpp:93-107), with
     // exact FP64 sums at up to 1024 sampled data points (the probe points of
     // residual_evaluator.hpp:119-124) within the tolerance too, and one more condition: the
-    // hybrid residual's largest deviation from the exact one at the probes is at most half the
-    // tolerance (the check resolves the tolerance). Otherwise residuals are taken with the FP64
-    // operator from then on.
+    // residual operator's largest deviation from the exact one at the probes is at most half
+    // the tolerance (the check resolves the tolerance). Otherwise residuals are taken with the
+    // next grade from then on.
     Operator<float> op32(model, pts.data(), mu, bbox, 0.0, P.data());
     op32.set_order(6);  // the tensor-core M2L's order; refinement absorbs its truncation
     std::unique_ptr<Operator<double>> op64;
@@ -448,15 +448,27 @@ FitResult fit_impl(const FitRequest& req) {
       }
       return op64.get();
     };
-    enum Grade { kFp32 = 0, kHybrid = 1, kFp64 = 2 };
+    // Grades: FP32 (order 6); hybrid (FP64-class near field, FP32 far field at order 6);
+    // hybrid at order 8 (for kernels whose far field order 6 does not resolve the tolerance,
+    // such as short-range covariances at coarse levels); FP64 at order 8.
+    enum Grade { kFp32 = 0, kHybrid = 1, kHybrid8 = 2, kFp64 = 3 };
+    std::unique_ptr<Operator<float>> op32_8;
     auto apply_graded = [&](int grade, const double* x, double* y) {
       if (grade == kFp64) {
         fp64_op()->apply(x, y);
-      } else {
-        op32.evaluator().set_near_fp64(grade == kHybrid);
-        op32.apply(x, y);
-        op32.evaluator().set_near_fp64(false);
+        return;
       }
+      Operator<float>* op = &op32;
+      if (grade == kHybrid8) {
+        if (!op32_8) {
+          op32_8 = std::make_unique<Operator<float>>(model, pts.data(), mu, bbox, 0.0, P.data());
+          op32_8->set_order(8);
+        }
+        op = op32_8.get();
+      }
+      op->evaluator().set_near_fp64(grade != kFp32);
+      op->apply(x, y);
+      op->evaluator().set_near_fp64(false);
     };
     int residual_grade = kHybrid;
     DevBuf<double> r(M), zero(M), rp32(std::max<Index>(re.n_probe(), 1));
@@ -483,8 +495,19 @@ FitResult fit_impl(const FitRequest& req) {
     } inner{&op32, apply_graded};
     int total = 0;
     Fgmres solver(M, req.max_iter);
+    // Iterative refinement: w = wb + the current cycle's FGMRES solution. The first cycle solves
+    // for the data from the initial weights (wb = 0); every later cycle solves
+    // A_inner d = r from zero for the recomputed residual r = rhs - A w, and wb holds the
+    // weights it started from.
+    DevBuf<double> wb(M), dw(M);
+    wb.zero();
     solver.setup(rhs.data(), w.data(), x0_zero, inner);
-    int base = 0;  // iterations before the current restart
+    auto current = [&] {
+      solver.solution(dw.data());
+      copy(w.data(), wb.data(), M);
+      axpy(M, 1.0, dw.data(), w.data());
+    };
+    int base = 0;  // iterations before the current cycle
     double cycle_start_residual = INFINITY;
     // Ratio of the inf-norm to the root mean square of the last recomputed residual. The next
     // check waits until the estimate times this ratio predicts at most twice the tolerance.
@@ -503,7 +526,7 @@ FitResult fit_impl(const FitRequest& req) {
                  (est_rms > req.tolerance || est_rms * peak_ratio > 2.0 * req.tolerance)) {
         if (req.verbose) std::printf("%8d   ~%12.6e (estimate)\n", total, est_rms);
       } else {
-        solver.solution(w.data());
+        current();
         double rinf = residual();
         bool converged = false;
         // Near the tolerance the residual operator must resolve it: its largest deviation from
@@ -524,6 +547,7 @@ FitResult fit_impl(const FitRequest& req) {
             break;
           }
           ++residual_grade;
+          cycle_start_residual = INFINITY;  // residuals of another operator
           rinf = residual();
         }
         const double rtrue = norm2(r.data(), M);
@@ -561,23 +585,23 @@ FitResult fit_impl(const FitRequest& req) {
               if (req.verbose)
                 std::printf("%8d    inner operator grade %d\n", total, inner.grade);
             }
+            cycle_start_residual = raised ? INFINITY : rinf;
+          } else {
+            cycle_start_residual = rinf;
           }
-          cycle_start_residual = rinf;
+          // New cycle: A_inner d = r from zero, on top of the current weights.
           base = total;
-          solver.setup(rhs.data(), w.data(), false, inner);
+          copy(wb.data(), w.data(), M);
+          solver.setup(r.data(), nullptr, true, inner);
         } else if (!std::isfinite(cycle_start_residual)) {
           cycle_start_residual = rinf;
         }
       }
       if (total >= req.max_iter)
         throw Error(PGPU_MAX_ITER, "reached the maximum number of iterations");
-      if (solver.iteration_count() == solver.max_iterations()) {
-        solver.solution(w.data());
-        base = total;
-        solver.setup(rhs.data(), w.data(), false, inner);
-      }
       solver.iterate(inner, pc);
     }
+    current();
     res.iterations = total;
   }
   res.solve_seconds = wall_seconds() - t1;
