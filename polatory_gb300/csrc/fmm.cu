@@ -571,21 +571,26 @@ __global__ void m2l_reduce_kernel(const T* __restrict__ part, int groups, Index 
   L[i] += s;
 }
 
+// Targets per block in the near field and L2P: leaves crowded with targets (evaluation points
+// falling into few source leaves) are split into chunks of this size.
+constexpr int kP2PChunk = 256;
+
 template <int P, class T>
 __global__ void __launch_bounds__(128)
     l2p_kernel(Cheb<T> ch, const P4<T>* __restrict__ tpos, const Index* __restrict__ perm,
-               const Index* __restrict__ leaf_start, const uint64_t* __restrict__ leaf_keys,
+               const Index* __restrict__ leaf_start, const int* __restrict__ chunk_leaf,
                Box box, int lf, const T* __restrict__ L, double* __restrict__ out) {
   constexpr int P3 = P * P * P;
   __shared__ T s_l[P3];
-  const Index leaf = blockIdx.x;
+  // One block per chunk of at most kP2PChunk targets of one leaf (the P2P chunk table).
+  const Index leaf = chunk_leaf[2 * blockIdx.x];
   for (int e = threadIdx.x; e < P3; e += blockDim.x) s_l[e] = L[leaf * P3 + e];
   __syncthreads();
-  (void)leaf_keys;
   const double wk = box.width / static_cast<double>(1 << lf);
   const T ctr[3] = {T(0), T(0), T(0)};  // tree positions are relative to the leaf centre
   const T inv_r = static_cast<T>(2.0 / wk);
-  const Index beg = leaf_start[leaf], end = leaf_start[leaf + 1];
+  const Index beg = leaf_start[leaf] + static_cast<Index>(chunk_leaf[2 * blockIdx.x + 1]) * kP2PChunk;
+  const Index end = min(leaf_start[leaf + 1], beg + kP2PChunk);
   for (Index i = beg + threadIdx.x; i < end; i += blockDim.x) {
     P4<T> pt = tpos[i];
     T sx[P], sy[P], sz[P];
@@ -609,22 +614,47 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-// Near field: one block per target leaf, each thread one target, source tiles in shared memory.
+// Near field: one block per chunk of a target leaf, each thread one or two targets, source
+// tiles in shared memory.
+
+// Chunks of kP2PChunk targets per leaf: count, then (after an exclusive scan) the chunk table
+// (leaf, chunk index within the leaf).
+__global__ void chunk_count_kernel(const Index* __restrict__ start, Index nleaf,
+                                   int* __restrict__ cnt) {
+  const Index l = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (l >= nleaf) return;
+  const Index n = start[l + 1] - start[l];
+  cnt[l] = static_cast<int>((n + kP2PChunk - 1) / kP2PChunk);
+}
+
+__global__ void chunk_fill_kernel(const int* __restrict__ cnt, const int* __restrict__ off,
+                                  Index nleaf, int* __restrict__ chunk_leaf) {
+  const Index l = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (l >= nleaf) return;
+  for (int c = 0; c < cnt[l]; ++c) {
+    chunk_leaf[2 * (off[l] + c)] = static_cast<int>(l);
+    chunk_leaf[2 * (off[l] + c) + 1] = c;
+  }
+}
 template <int KIND, class T>
 __global__ void __launch_bounds__(128)
     p2p_kernel(KParams<T> kp, const P4<T>* __restrict__ tpos, const Index* __restrict__ tperm,
-               const Index* __restrict__ tleaf_start, const int* __restrict__ table,
-               const P4<T>* __restrict__ spos, const T* __restrict__ sw,
-               const Index* __restrict__ sleaf_start, T wleaf, double* __restrict__ out) {
+               const Index* __restrict__ tleaf_start, const int* __restrict__ chunk_leaf,
+               const int* __restrict__ table, const P4<T>* __restrict__ spos,
+               const T* __restrict__ sw, const Index* __restrict__ sleaf_start, T wleaf,
+               double* __restrict__ out) {
   // Positions are relative to their leaf centres; the neighbour slot nb = 9 (dx+1) + 3 (dy+1) +
   // (dz+1) puts the source leaf centre at the target's + (dx, dy, dz) * wleaf, so
   // d = (t - (dx, dy, dz) wleaf) - s involves only leaf-sized numbers.
+  // One block per chunk of at most kP2PChunk targets of one leaf (chunk_leaf: per chunk the
+  // leaf and the chunk's index within it), so leaves crowded with targets spread over blocks.
   __shared__ P4<T> s_p[128];
   __shared__ int s_nb[27];
-  const Index leaf = blockIdx.x;
-  if (threadIdx.x < 27) s_nb[threadIdx.x] = table[leaf * 27 + threadIdx.x];
+  const int leaf = chunk_leaf[2 * blockIdx.x];
+  if (threadIdx.x < 27) s_nb[threadIdx.x] = table[static_cast<Index>(leaf) * 27 + threadIdx.x];
   __syncthreads();
-  const Index tb = tleaf_start[leaf], te = tleaf_start[leaf + 1];
+  const Index tb = tleaf_start[leaf] + static_cast<Index>(chunk_leaf[2 * blockIdx.x + 1]) * kP2PChunk;
+  const Index te = min(tleaf_start[leaf + 1], tb + kP2PChunk);
   // NT targets per thread (1 or 2, uniform over the block): each source read from shared memory
   // serves NT targets.
   auto pass = [&]<int NT>(Index i0) {
@@ -1355,6 +1385,8 @@ struct Fmm<T>::Impl {
   std::vector<DevBuf<int>> m2l_table;
   DevBuf<int> p2p_table;
   DevBuf<int> tleaf;  // leaf of each sorted target point (sparse target leaves only)
+  DevBuf<int> chunk_leaf;  // P2P chunk -> (target leaf, chunk index within the leaf)
+  Index n_chunks = 0;
   std::vector<std::shared_ptr<M2LOps<T>>> kmats;
   std::vector<DevBuf<T>> M, L, Mt, Lt;  // Mt/Lt: compressed expansions (rank r) when used
   DevBuf<T> sw;
@@ -1457,6 +1489,27 @@ struct Fmm<T>::Impl {
       PGPU_CUDA(cudaMemcpyAsync(&h, tot.data(), sizeof(h), cudaMemcpyDeviceToHost, st));
       sync();
       near_pairs = static_cast<Index>(h);
+      {
+        DevBuf<int> cnt(ntl), off(ntl);
+        chunk_count_kernel<<<blocks_for(ntl, 128), 128, 0, st>>>(tt.start[lf].data(), ntl,
+                                                                 cnt.data());
+        PGPU_LAUNCH_CHECK();
+        size_t sb = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, sb, cnt.data(), off.data(), ntl, st);
+        DevBuf<unsigned char> stmp(sb);
+        PGPU_CUDA(cub::DeviceScan::ExclusiveSum(stmp.data(), sb, cnt.data(), off.data(), ntl, st));
+        int last_cnt = 0, last_off = 0;
+        PGPU_CUDA(cudaMemcpyAsync(&last_cnt, cnt.data() + ntl - 1, sizeof(int),
+                                  cudaMemcpyDeviceToHost, st));
+        PGPU_CUDA(cudaMemcpyAsync(&last_off, off.data() + ntl - 1, sizeof(int),
+                                  cudaMemcpyDeviceToHost, st));
+        sync();
+        n_chunks = static_cast<Index>(last_off) + last_cnt;
+        chunk_leaf.resize(2 * std::max<Index>(n_chunks, 1));
+        chunk_fill_kernel<<<blocks_for(ntl, 128), 128, 0, st>>>(cnt.data(), off.data(), ntl,
+                                                                chunk_leaf.data());
+        PGPU_LAUNCH_CHECK();
+      }
       const Index ntp = symmetric ? ns : nt;
       if (!symmetric && ntp < 32 * ntl) {
         tleaf.resize(ntp);
@@ -1629,8 +1682,8 @@ struct Fmm<T>::Impl {
     if (tt.ncell[lf] > 0) {
       const double npt = static_cast<double>(symmetric ? ns : nt);
       ProfScope ps(f32 ? "fmm_l2p_f32" : "fmm_l2p_f64", npt * (2.0 * P3 + 6.0 * P * P));
-      l2p_kernel<P, T><<<static_cast<unsigned>(tt.ncell[lf]), 128, 0, st>>>(
-          ch, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), tt.keys[lf].data(), box, lf,
+      l2p_kernel<P, T><<<static_cast<unsigned>(n_chunks), 128, 0, st>>>(
+          ch, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), chunk_leaf.data(), box, lf,
           L[lf].data(), out);
       PGPU_LAUNCH_CHECK();
     }
@@ -1680,9 +1733,9 @@ struct Fmm<T>::Impl {
       } else {
         ProfScope ps("fmm_p2p_f64", pair_flops(kind) * static_cast<double>(near_pairs));
         dispatch_kind(kind, [&]<int K>() {
-          p2p_kernel<K, double><<<static_cast<unsigned>(ntl), 128, 0, st>>>(
-              kp64, tt.pos64.data(), tt.perm.data(), tt.start[lf].data(), p2p_table.data(),
-              src.pos64.data(), sw64.data(), src.start[lf].data(), wl, out);
+          p2p_kernel<K, double><<<static_cast<unsigned>(n_chunks), 128, 0, st>>>(
+              kp64, tt.pos64.data(), tt.perm.data(), tt.start[lf].data(), chunk_leaf.data(),
+              p2p_table.data(), src.pos64.data(), sw64.data(), src.start[lf].data(), wl, out);
           return 0;
         });
         PGPU_LAUNCH_CHECK();
@@ -1701,9 +1754,9 @@ struct Fmm<T>::Impl {
         });
       } else {
         dispatch_kind(kind, [&]<int K>() {
-          p2p_kernel<K, T><<<static_cast<unsigned>(ntl), 128, 0, st>>>(
-              kp, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), p2p_table.data(),
-              src.pos.data(), sw.data(), src.start[lf].data(), wl, out);
+          p2p_kernel<K, T><<<static_cast<unsigned>(n_chunks), 128, 0, st>>>(
+              kp, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), chunk_leaf.data(),
+              p2p_table.data(), src.pos.data(), sw.data(), src.start[lf].data(), wl, out);
           return 0;
         });
       }
