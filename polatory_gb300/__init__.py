@@ -457,6 +457,8 @@ class FmmEvaluator:
         check(lib.pgpu_evaluator_create(C.byref(self._rbf), kernel, int(symmetric), ptr(b),
                                         precision, C.byref(self._h)))
         self._n_trg = 0
+        # Outputs per target: 3 for the gradient-transpose and Hessian kernels.
+        self._kn = 3 if kernel in (_lib.KERNEL_GRADIENT_TRANSPOSE, _lib.KERNEL_HESSIAN) else 1
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -490,6 +492,7 @@ class FmmEvaluator:
         check(lib.pgpu_evaluator_set_weights(self._h, ptr(w), w.shape[0]))
 
     def evaluate(self) -> np.ndarray:
-        out = np.empty(self._n_trg)
-        check(lib.pgpu_evaluator_evaluate(self._h, ptr(out), self._n_trg))
+        n = self._kn * self._n_trg
+        out = np.empty(n)
+        check(lib.pgpu_evaluator_evaluate(self._h, ptr(out), n))
         return out

@@ -220,8 +220,11 @@ int pgpu_evaluator_create(const pgpu_rbf* rbf, int kernel_kind, int symmetric,
     check_ptr(rbf, "rbf");
     check_ptr(out, "out");
     check_ptr(bbox, "bbox");
-    if (kernel_kind != PGPU_KERNEL_VALUE)
-      throw Error(PGPU_NOT_IMPLEMENTED, "only the value kernel is exposed as an evaluator so far");
+    if (kernel_kind < PGPU_KERNEL_VALUE || kernel_kind > PGPU_KERNEL_HESSIAN)
+      throw_invalid("unknown kernel kind");
+    if (symmetric && (kernel_kind == PGPU_KERNEL_GRADIENT ||
+                      kernel_kind == PGPU_KERNEL_GRADIENT_TRANSPOSE))
+      throw_invalid("symmetric evaluators take the value or the Hessian kernel");
     pgpu_model m{};
     m.n_rbfs = 1;
     m.rbfs[0] = *rbf;
@@ -278,25 +281,39 @@ int pgpu_evaluator_configure(pgpu_evaluator* ev, int backend, int order, int lea
 }
 
 namespace {
+// Inputs per source (km) and outputs per target (kn) of a kernel kind: gradient sources carry
+// three weights (GradientKernel, HessianKernel: km = 3, fmm/gradient_kernel.hpp:28-29), gradient
+// targets receive three outputs (GradientTransposeKernel, HessianKernel: kn = 3).
+bool grad_sources(int kind) {
+  return kind == PGPU_KERNEL_GRADIENT || kind == PGPU_KERNEL_HESSIAN;
+}
+bool grad_targets(int kind) {
+  return kind == PGPU_KERNEL_GRADIENT_TRANSPOSE || kind == PGPU_KERNEL_HESSIAN;
+}
+
+// The kernel kinds are the blocks of one Evaluator: value or gradient point sets on either
+// side (interpolation/evaluator.hpp:97-124 wires a_, f_, ft_, h_ the same way).
 void rebuild(pgpu_evaluator* ev) {
+  auto wire = [ev](auto& e) {
+    e.set_backend(ev->backend);
+    e.set_far_field(ev->ff);
+    const bool gs = grad_sources(ev->kernel_kind), gt = grad_targets(ev->kernel_kind);
+    if (ev->symmetric) {
+      if (gs) e.set_points(nullptr, 0, ev->src.data(), ev->n_src);
+      else e.set_points(ev->src.data(), ev->n_src, nullptr, 0);
+      return;
+    }
+    if (gs) e.set_sources(nullptr, 0, ev->src.data(), ev->n_src);
+    else e.set_sources(ev->src.data(), ev->n_src, nullptr, 0);
+    if (gt) e.set_targets(nullptr, 0, ev->trg.data(), ev->n_trg);
+    else e.set_targets(ev->trg.data(), ev->n_trg, nullptr, 0);
+  };
   if (ev->precision == PGPU_PRECISION_PLAIN) {
     ev->e64 = std::make_unique<Evaluator<double>>(ev->model, ev->bbox, ev->accuracy, ev->accuracy);
-    ev->e64->set_backend(ev->backend);
-    ev->e64->set_far_field(ev->ff);
-    if (ev->symmetric) ev->e64->set_points(ev->src.data(), ev->n_src, nullptr, 0);
-    else {
-      ev->e64->set_sources(ev->src.data(), ev->n_src, nullptr, 0);
-      ev->e64->set_targets(ev->trg.data(), ev->n_trg, nullptr, 0);
-    }
+    wire(*ev->e64);
   } else {
     ev->e32 = std::make_unique<Evaluator<float>>(ev->model, ev->bbox, ev->accuracy, ev->accuracy);
-    ev->e32->set_backend(ev->backend);
-    ev->e32->set_far_field(ev->ff);
-    if (ev->symmetric) ev->e32->set_points(ev->src.data(), ev->n_src, nullptr, 0);
-    else {
-      ev->e32->set_sources(ev->src.data(), ev->n_src, nullptr, 0);
-      ev->e32->set_targets(ev->trg.data(), ev->n_trg, nullptr, 0);
-    }
+    wire(*ev->e32);
   }
 }
 }  // namespace
@@ -342,7 +359,8 @@ int pgpu_evaluator_set_points(pgpu_evaluator* ev, const double* points, int64_t 
 int pgpu_evaluator_set_weights(pgpu_evaluator* ev, const double* weights, int64_t n) {
   return guarded([&] {
     check_ptr(ev, "evaluator");
-    if (n != ev->n_src) throw_invalid("weights must have km * n_sources entries");
+    if (n != (grad_sources(ev->kernel_kind) ? 3 : 1) * ev->n_src)
+      throw_invalid("weights must have km * n_sources entries");
     copy_in(ev->w, weights, n);
     ev->weights_set = true;
   });
@@ -351,7 +369,8 @@ int pgpu_evaluator_set_weights(pgpu_evaluator* ev, const double* weights, int64_
 int pgpu_evaluator_evaluate(pgpu_evaluator* ev, double* out, int64_t n) {
   return guarded([&] {
     check_ptr(ev, "evaluator");
-    if (n != ev->n_trg) throw_invalid("out must have kn * n_targets entries");
+    if (n != (grad_targets(ev->kernel_kind) ? 3 : 1) * ev->n_trg)
+      throw_invalid("out must have kn * n_targets entries");
     if (!ev->weights_set) throw_runtime("weights have not been set");
     if (!ev->e64 && !ev->e32) rebuild(ev);
     ev->out.resize(std::max<int64_t>(n, 1));

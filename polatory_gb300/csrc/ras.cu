@@ -6,9 +6,15 @@
 // point i, u_i[k] = A(p_k, x_i) and v_i = A11 L_i (p_k the polynomial points),
 //   (Q^T A Q)_ij = A(x_i, x_j) - u_i.L_j - L_i.u_j + L_i.v_j,
 // which equals the four-block product of fine_grid.hpp:80-84 with q_top = -L^T.
+#include <omp.h>
+
 #include <algorithm>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
+#include <exception>
+#include <mutex>
+#include <thread>
 
 #include "kernels.cuh"
 #include "linalg.hpp"
@@ -576,23 +582,64 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
     div_points = a_points.data();
   }
 
+  // The host divides the levels (finest first) on a helper thread and publishes each level's
+  // domains as soon as they exist; meanwhile this thread runs the device set-up of the levels
+  // already published, so the GPU assembles and factors the finest level while the host picks
+  // its coarse points and divides the coarser levels.
   std::vector<std::vector<Domain>> level_domains(n_levels_);
-  for (int level = n_levels_ - 1; level >= 1; --level) {
-    std::vector<Index> no_grad;
-    const double t0 = wall_seconds();
-    DomainDivider divider(div_points, nullptr, point_idcs_[level], no_grad, poly_idcs_);
-    const double t1 = wall_seconds();
-    double finest = std::log(static_cast<double>(mu_)) / std::log(kFineToCoarseRatio);
-    double coarsest = std::log(static_cast<double>(kNCoarsestPoints)) / std::log(kFineToCoarseRatio);
-    Index n_coarse = static_cast<Index>(std::pow(
-        kFineToCoarseRatio, coarsest + (level - 1) * (finest - coarsest) / (n_levels_ - 1)));
-    point_idcs_[level - 1] = divider.choose_coarse_points(n_coarse).first;
-    level_domains[level] = std::move(divider.domains());
-    if (verbose())
-      std::printf("ras level %d: %zu points, %zu domains, divide %.3f s, coarse points %.3f s\n",
-                  level, point_idcs_[level].size(), level_domains[level].size(), t1 - t0,
-                  wall_seconds() - t1);
-  }
+  std::mutex div_mu;
+  std::condition_variable div_cv;
+  int published = n_levels_;  // levels >= published are available
+  std::exception_ptr div_error;
+  const int omp_threads = omp_get_max_threads();
+  std::thread divide_thread([&] {
+    omp_set_num_threads(omp_threads);
+    try {
+      for (int level = n_levels_ - 1; level >= 1; --level) {
+        std::vector<Index> no_grad;
+        const double t0 = wall_seconds();
+        DomainDivider divider(div_points, nullptr, point_idcs_[level], no_grad, poly_idcs_);
+        const double t1 = wall_seconds();
+        {
+          std::lock_guard<std::mutex> lk(div_mu);
+          level_domains[level] = std::move(divider.domains());
+          published = level;
+        }
+        div_cv.notify_all();
+        double finest = std::log(static_cast<double>(mu_)) / std::log(kFineToCoarseRatio);
+        double coarsest = std::log(static_cast<double>(kNCoarsestPoints)) / std::log(kFineToCoarseRatio);
+        Index n_coarse = static_cast<Index>(std::pow(
+            kFineToCoarseRatio, coarsest + (level - 1) * (finest - coarsest) / (n_levels_ - 1)));
+        auto coarse = divider.choose_coarse_points(n_coarse).first;
+        if (verbose())
+          std::printf("ras level %d: %zu points, %zu domains, divide %.3f s, coarse points %.3f s\n",
+                      level, point_idcs_[level].size(), level_domains[level].size(), t1 - t0,
+                      wall_seconds() - t1);
+        std::lock_guard<std::mutex> lk(div_mu);
+        point_idcs_[level - 1] = std::move(coarse);
+      }
+    } catch (...) {
+      std::lock_guard<std::mutex> lk(div_mu);
+      div_error = std::current_exception();
+      published = 0;
+    }
+    {
+      std::lock_guard<std::mutex> lk(div_mu);
+      published = 0;
+    }
+    div_cv.notify_all();
+  });
+  struct Joiner {
+    std::thread& t;
+    ~Joiner() {
+      if (t.joinable()) t.join();
+    }
+  } joiner{divide_thread};
+  auto wait_level = [&](int level) {
+    std::unique_lock<std::mutex> lk(div_mu);
+    div_cv.wait(lk, [&] { return published <= level; });
+    if (div_error) std::rethrow_exception(div_error);
+  };
   const double t_dev = wall_seconds();
 
   // Device-side per-point data.
@@ -636,9 +683,12 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
   }
 
   for (int level = n_levels_ - 1; level >= 1; --level) {
+    wait_level(level);
     fine_[level] = std::make_unique<DomainBatch<T>>();
     build_batch(*fine_[level], level_domains[level]);
   }
+  divide_thread.join();
+  if (div_error) std::rethrow_exception(div_error);
   {
     Domain cd;
     cd.point_indices = point_idcs_[0];
