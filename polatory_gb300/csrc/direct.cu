@@ -173,7 +173,89 @@ void launch_direct(int kind, const KParams<T>& kp, const Mat3& a, const DirectSo
   }
 }
 
+// Value sources to value targets for the odd polyharmonic kernels in float-float arithmetic
+// (about 44 significant bits on the FP32 pipes): FP64-class sums at a fraction of the FP64
+// cost. Positions are the FP64 frame coordinates; same tiling and source split as above.
+template <int KIND>
+__global__ void __launch_bounds__(kThreads)
+    direct_ff_kernel(KParams<double> kp, const P4<double>* __restrict__ vpos,
+                     const double* __restrict__ vw, Index nv, const P4<double>* __restrict__ tpos,
+                     Index nt, double* __restrict__ out, double* __restrict__ part, Index chunk) {
+  __shared__ float s_p[8][kTile];
+  const Index i = static_cast<Index>(blockIdx.x) * kThreads + threadIdx.x;
+  const bool active = i < nt;
+  const P4<double> t = active ? tpos[i] : P4<double>{0.0, 0.0, 0.0, 0.0};
+  float txh, txl, tyh, tyl, tzh, tzl;
+  ff_split(t.x, txh, txl);
+  ff_split(t.y, tyh, tyl);
+  ff_split(t.z, tzh, tzl);
+  float c_hi, c_lo;
+  ff_split(kp.p1 * kp.p1, c_hi, c_lo);
+  const bool reg = kp.p1 != 0.0;
+  const Index s0 = static_cast<Index>(blockIdx.y) * chunk;
+  const Index s1 = min(nv, s0 + chunk);
+  double tot = 0.0;
+  for (Index base = s0; base < s1; base += kTile) {
+    const int cnt = static_cast<int>(min(static_cast<Index>(kTile), s1 - base));
+    __syncthreads();
+    if (threadIdx.x < cnt) {
+      const P4<double> p = vpos[base + threadIdx.x];
+      ff_split(p.x, s_p[0][threadIdx.x], s_p[1][threadIdx.x]);
+      ff_split(p.y, s_p[2][threadIdx.x], s_p[3][threadIdx.x]);
+      ff_split(p.z, s_p[4][threadIdx.x], s_p[5][threadIdx.x]);
+      ff_split(vw[base + threadIdx.x], s_p[6][threadIdx.x], s_p[7][threadIdx.x]);
+    }
+    __syncthreads();
+    float ah = 0.0f, al = 0.0f;
+#pragma unroll 2
+    for (int j = 0; j < cnt; ++j)
+      ff_poly_accumulate<KIND>(txh, txl, tyh, tyl, tzh, tzl, s_p[0][j], s_p[1][j], s_p[2][j],
+                               s_p[3][j], s_p[4][j], s_p[5][j], s_p[6][j], s_p[7][j], reg, c_hi,
+                               c_lo, ah, al);
+    tot += static_cast<double>(ah) + static_cast<double>(al);
+  }
+  if (!active) return;
+  const double v = (KIND == PGPU_RBF_BH3 ? -kp.p0 : kp.p0) * tot;
+  if (part) part[static_cast<Index>(blockIdx.y) * nt + i] = v;
+  else out[i] += v;
+}
+
 }  // namespace
+
+bool direct_evaluate_ff(int kind, const KParams<double>& kp, const P4<double>* spos,
+                        const double* w, Index ns, const P4<double>* tpos, Index nt, double* out,
+                        cudaStream_t st) {
+  if (kind != PGPU_RBF_BH3 && kind != PGPU_RBF_TH3) return false;
+  if (nt == 0 || ns == 0) return true;
+  const int bx = blocks_for(nt, kThreads);
+  const int want = 4 * num_sms();
+  int chunks = 1;
+  if (bx < want) {
+    chunks = (want + bx - 1) / bx;
+    const Index max_chunks = (ns + 4 * kTile - 1) / (4 * kTile);
+    if (chunks > max_chunks) chunks = static_cast<int>(max_chunks < 1 ? 1 : max_chunks);
+    if (chunks > 65535) chunks = 65535;
+  }
+  Index chunk = (ns + chunks - 1) / chunks;
+  chunk = ((chunk + kTile - 1) / kTile) * kTile;
+  chunks = static_cast<int>((ns + chunk - 1) / chunk);
+  ProfScope ps("direct_ff", pair_flops(kind) * static_cast<double>(nt) * static_cast<double>(ns));
+  DevBuf<double> part;
+  if (chunks > 1) part.resize(static_cast<size_t>(chunks) * nt);
+  dim3 grid(bx, chunks);
+  if (kind == PGPU_RBF_BH3)
+    direct_ff_kernel<PGPU_RBF_BH3><<<grid, kThreads, 0, st>>>(kp, spos, w, ns, tpos, nt, out,
+                                                              chunks > 1 ? part.data() : nullptr, chunk);
+  else
+    direct_ff_kernel<PGPU_RBF_TH3><<<grid, kThreads, 0, st>>>(kp, spos, w, ns, tpos, nt, out,
+                                                              chunks > 1 ? part.data() : nullptr, chunk);
+  PGPU_LAUNCH_CHECK();
+  if (chunks > 1) {
+    reduce_parts_kernel<<<blocks_for(nt, 256), 256, 0, st>>>(part.data(), chunks, nt, out);
+    PGPU_LAUNCH_CHECK();
+  }
+  return true;
+}
 
 template <class T>
 void direct_evaluate(int kind, const KParams<T>& kp, const Mat3& a, const DirectSources<T>& src,

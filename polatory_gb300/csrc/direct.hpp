@@ -34,4 +34,11 @@ template <class T>
 void direct_evaluate(int kind, const KParams<T>& kp, const Mat3& a, const DirectSources<T>& src,
                      const DirectTargets<T>& trg, cudaStream_t st);
 
+// Value sources to value targets of the odd polyharmonic kernels (bh3, th3) in float-float
+// arithmetic: FP64-class accuracy on the FP32 pipes. Returns false for other kernels (the
+// caller then uses the FP64 kernel). Positions: FP64 frame coordinates; out is added to.
+bool direct_evaluate_ff(int kind, const KParams<double>& kp, const P4<double>* spos,
+                        const double* w, Index ns, const P4<double>* tpos, Index nt, double* out,
+                        cudaStream_t st);
+
 }  // namespace pgpu

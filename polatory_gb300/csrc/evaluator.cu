@@ -321,10 +321,18 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
     bool use_fmm = fmm_ok && (backend_ == kBackendFmm ||
                               (backend_ == kBackendAuto && pairs > direct_pair_limit<T>()));
     const bool fp64_near = sizeof(T) == 4 && near64_ && sigma_ == 0 && mg_ == 0;
+    const bool values_only = sigma_ == 0 && mg_ == 0;
     if (!use_fmm && fp64_near) {
-      DirectSources<double> src{t.spos_d.data(), w_, mu_, nullptr, nullptr, 0};
-      DirectTargets<double> trg{t.tpos_d.data(), m_, out_v, nullptr, 0, out_g};
-      direct_evaluate<double>(t.rbf.kind, t.kp64, t.a, src, trg, stream());
+      if (!direct_evaluate_ff(t.rbf.kind, t.kp64, t.spos_d.data(), w_, mu_, t.tpos_d.data(), m_,
+                              out_v, stream())) {
+        DirectSources<double> src{t.spos_d.data(), w_, mu_, nullptr, nullptr, 0};
+        DirectTargets<double> trg{t.tpos_d.data(), m_, out_v, nullptr, 0, out_g};
+        direct_evaluate<double>(t.rbf.kind, t.kp64, t.a, src, trg, stream());
+      }
+      stats_.direct_pairs += static_cast<Index>(pairs);
+    } else if (!use_fmm && sizeof(T) == 8 && ff_direct_ && values_only &&
+               direct_evaluate_ff(t.rbf.kind, t.kp64, t.spos_d.data(), w_, mu_, t.tpos_d.data(),
+                                  m_, out_v, stream())) {
       stats_.direct_pairs += static_cast<Index>(pairs);
     } else if (!use_fmm) {
       DirectSources<T> src{t.spos.data(), t.vw.data(), mu_, t.sgpos.data(), t.gg.data(), sigma_};

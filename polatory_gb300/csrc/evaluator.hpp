@@ -87,6 +87,10 @@ class Evaluator {
   // FP32 evaluators of value sources and targets: near field (or all pairs, on the direct
   // backend) in FP64 from the FP64 coordinates and weights; the far field stays FP32.
   void set_near_fp64(bool on) { near64_ = on; }
+  // FP64 evaluators: value-to-value direct sums of the odd polyharmonic kernels in float-float
+  // arithmetic (FP64-class accuracy on the FP32 pipes). Off by default (the plain path keeps
+  // FP64 arithmetic throughout).
+  void set_ff_direct(bool on) { ff_direct_ = on; }
 
  private:
   struct Term;
@@ -100,6 +104,7 @@ class Evaluator {
   bool ff_set_ = false;
   FarFieldConfig ff_;
   bool near64_ = false;
+  bool ff_direct_ = false;
   const double* w_ = nullptr;  // the weights of the last set_weights (device)
   Index mu_ = 0, sigma_ = 0, m_ = 0, mg_ = 0;
   const double* spts_ = nullptr;

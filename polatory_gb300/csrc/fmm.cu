@@ -728,17 +728,6 @@ __global__ void __launch_bounds__(128)
 // (about 44 significant bits), on the FP32 pipes. Differences use TwoSum, squares and
 // products FMA-based TwoProd, the square root one Newton step from rsqrtf. Each 128-source
 // tile is summed in float-float and added to an FP64 total.
-__device__ __forceinline__ void ff_split(double x, float& hi, float& lo) {
-  hi = static_cast<float>(x);
-  lo = static_cast<float>(x - static_cast<double>(hi));
-}
-
-__device__ __forceinline__ void ff_two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float v = s - a;
-  e = (a - (s - v)) + (b - v);
-}
-
 template <int KIND>
 __global__ void __launch_bounds__(128)
     p2p_ff_kernel(KParams<double> kp, const P4<double>* __restrict__ tpos,
@@ -781,53 +770,10 @@ __global__ void __launch_bounds__(128)
         __syncthreads();
         float ah = 0.0f, al = 0.0f;
 #pragma unroll 2
-        for (int j = 0; j < cnt; ++j) {
-          float dxh, dxe, dyh, dye, dzh, dze;
-          ff_two_sum(txh, -s_p[0][j], dxh, dxe);
-          ff_two_sum(tyh, -s_p[2][j], dyh, dye);
-          ff_two_sum(tzh, -s_p[4][j], dzh, dze);
-          dxe += txl - s_p[1][j];
-          dye += tyl - s_p[3][j];
-          dze += tzl - s_p[5][j];
-          // r^2 = sum (h + e)^2 ~ h^2 + 2 h e.
-          const float px = dxh * dxh, py = dyh * dyh, pz = dzh * dzh;
-          const float pxe = fmaf(2.0f * dxh, dxe, fmaf(dxh, dxh, -px));
-          const float pye = fmaf(2.0f * dyh, dye, fmaf(dyh, dyh, -py));
-          const float pze = fmaf(2.0f * dzh, dze, fmaf(dzh, dzh, -pz));
-          float a, ea, r2h, eb;
-          ff_two_sum(px, py, a, ea);
-          ff_two_sum(a, pz, r2h, eb);
-          float r2l = ea + eb + pxe + pye + pze;
-          if (reg) {
-            float sh, se2;
-            ff_two_sum(r2h, c_hi, sh, se2);
-            r2h = sh;
-            r2l += se2 + c_lo;
-          }
-          {
-            const float nh = r2h + r2l;
-            r2l = r2l - (nh - r2h);
-            r2h = nh;
-          }
-          const float rinv = rsqrtf(fmaxf(r2h, 1e-30f));
-          const float rh = r2h * rinv;
-          const float rl = (fmaf(-rh, rh, r2h) + r2l) * (0.5f * rinv);
-          float ph, pl;
-          if constexpr (KIND == PGPU_RBF_BH3) {
-            ph = rh;
-            pl = rl;
-          } else {
-            ph = rh * r2h;
-            pl = fmaf(rh, r2h, -ph) + fmaf(rh, r2l, rl * r2h);
-          }
-          const float wh = s_p[6][j], wl = s_p[7][j];
-          const float th = wh * ph;
-          const float tl = fmaf(wh, ph, -th) + fmaf(wh, pl, wl * ph);
-          float sh, e2;
-          ff_two_sum(ah, th, sh, e2);
-          al += e2 + tl;
-          ah = sh;
-        }
+        for (int j = 0; j < cnt; ++j)
+          ff_poly_accumulate<KIND>(txh, txl, tyh, tyl, tzh, tzl, s_p[0][j], s_p[1][j], s_p[2][j],
+                                   s_p[3][j], s_p[4][j], s_p[5][j], s_p[6][j], s_p[7][j], reg,
+                                   c_hi, c_lo, ah, al);
         tot += static_cast<double>(ah) + static_cast<double>(al);
       }
     }

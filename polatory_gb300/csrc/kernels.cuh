@@ -90,4 +90,75 @@ inline double pair_flops(int kind) {
   }
 }
 
+#ifdef __CUDACC__
+// ---- float-float arithmetic for the odd polyharmonic kernels ---------------------------------
+// Values carried as unevaluated pairs of floats (about 44 significant bits) on the FP32 pipes:
+// differences by TwoSum, squares and products by FMA-based TwoProd, the square root one Newton
+// step from rsqrtf.
+__device__ __forceinline__ void ff_split(double x, float& hi, float& lo) {
+  hi = static_cast<float>(x);
+  lo = static_cast<float>(x - static_cast<double>(hi));
+}
+
+__device__ __forceinline__ void ff_two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float v = s - a;
+  e = (a - (s - v)) + (b - v);
+}
+
+// Adds w * phi(|t - s|) / p0 to the float-float accumulator (ah, al) for -p0 rho (bh3) or
+// p0 rho^3 (th3), rho^2 = r^2 + p1^2 with (c_hi, c_lo) = p1^2 (reg: p1 != 0).
+template <int KIND>
+__device__ __forceinline__ void ff_poly_accumulate(float txh, float txl, float tyh, float tyl,
+                                                   float tzh, float tzl, float sxh, float sxl,
+                                                   float syh, float syl, float szh, float szl,
+                                                   float wh, float wl, bool reg, float c_hi,
+                                                   float c_lo, float& ah, float& al) {
+  float dxh, dxe, dyh, dye, dzh, dze;
+  ff_two_sum(txh, -sxh, dxh, dxe);
+  ff_two_sum(tyh, -syh, dyh, dye);
+  ff_two_sum(tzh, -szh, dzh, dze);
+  dxe += txl - sxl;
+  dye += tyl - syl;
+  dze += tzl - szl;
+  // r^2 = sum (h + e)^2 ~ h^2 + 2 h e.
+  const float px = dxh * dxh, py = dyh * dyh, pz = dzh * dzh;
+  const float pxe = fmaf(2.0f * dxh, dxe, fmaf(dxh, dxh, -px));
+  const float pye = fmaf(2.0f * dyh, dye, fmaf(dyh, dyh, -py));
+  const float pze = fmaf(2.0f * dzh, dze, fmaf(dzh, dzh, -pz));
+  float a, ea, r2h, eb;
+  ff_two_sum(px, py, a, ea);
+  ff_two_sum(a, pz, r2h, eb);
+  float r2l = ea + eb + pxe + pye + pze;
+  if (reg) {
+    float sh, se2;
+    ff_two_sum(r2h, c_hi, sh, se2);
+    r2h = sh;
+    r2l += se2 + c_lo;
+  }
+  {
+    const float nh = r2h + r2l;
+    r2l = r2l - (nh - r2h);
+    r2h = nh;
+  }
+  const float rinv = rsqrtf(fmaxf(r2h, 1e-30f));
+  const float rh = r2h * rinv;
+  const float rl = (fmaf(-rh, rh, r2h) + r2l) * (0.5f * rinv);
+  float ph, pl;
+  if constexpr (KIND == PGPU_RBF_BH3) {
+    ph = rh;
+    pl = rl;
+  } else {
+    ph = rh * r2h;
+    pl = fmaf(rh, r2h, -ph) + fmaf(rh, r2l, rl * r2h);
+  }
+  const float th = wh * ph;
+  const float tl = fmaf(wh, ph, -th) + fmaf(wh, pl, wl * ph);
+  float sh, e2;
+  ff_two_sum(ah, th, sh, e2);
+  al += e2 + tl;
+  ah = sh;
+}
+#endif
+
 }  // namespace pgpu

@@ -229,41 +229,122 @@ __global__ void trsm_panel_kernel(int kb, const int* __restrict__ lds,
   for (int c = 0; c < NB; ++c) m[r + static_cast<Index>(kb * NB + c) * ld] = x[c];
 }
 
+// Trailing update with the panels [kb0, kb0 + np) of the factor, C(i, j) -= sum_q L(i, q)
+// L(j, q)^T over 32 x 32 tiles. col != 0: only block column c = kb0 + np, block rows i >= c
+// (the left-looking update of the next panel inside a group); otherwise every lower tile with
+// i, j >= kb0 + np. Grouping np panels per trailing update reads and writes the trailing
+// matrices once per group instead of once per panel.
 template <class T>
-__global__ void syrk_update_kernel(int kb, const int* __restrict__ lds,
+__global__ void syrk_update_kernel(int kb0, int np, int col, const int* __restrict__ lds,
                                    const Index* __restrict__ mat_off, T* __restrict__ mats) {
   const Index d = blockIdx.x;
   const int ld = lds[d];
   const int nbd = ld / NB;
-  const int rem = nbd - kb - 1;
-  if (rem <= 0) return;
-  const Index ntiles = static_cast<Index>(rem) * (rem + 1) / 2;
-  if (static_cast<Index>(blockIdx.y) >= ntiles) return;
-  int ti, tj;
-  tile_of(blockIdx.y, ti, tj);
-  const int bi = kb + 1 + ti, bj = kb + 1 + tj;
-  T* m = mats + mat_off[d];
-  __shared__ T pi[NB][NB + 1];  // pi[k][i] = L(bi*NB + i, kb*NB + k)
-  __shared__ T pj[NB][NB + 1];
-  for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
-    int rr = e % NB, kk = e / NB;
-    pi[kk][rr] = m[(bi * NB + rr) + static_cast<Index>(kb * NB + kk) * ld];
-    pj[kk][rr] = m[(bj * NB + rr) + static_cast<Index>(kb * NB + kk) * ld];
+  const int first = kb0 + np;
+  if (first >= nbd) return;
+  int bi, bj;
+  if (col) {
+    bi = first + static_cast<int>(blockIdx.y);
+    bj = first;
+    if (bi >= nbd) return;
+  } else {
+    const int rem = nbd - first;
+    const Index ntiles = static_cast<Index>(rem) * (rem + 1) / 2;
+    if (static_cast<Index>(blockIdx.y) >= ntiles) return;
+    int ti, tj;
+    tile_of(blockIdx.y, ti, tj);
+    bi = first + ti;
+    bj = first + tj;
   }
-  __syncthreads();
+  T* m = mats + mat_off[d];
+  __shared__ T pi[NB][NB + 1];  // pi[k][i] = L(bi*NB + i, q*NB + k)
+  __shared__ T pj[NB][NB + 1];
   const int i = threadIdx.x & 31;
   const int jy = threadIdx.x >> 5;  // 0..7
   T acc[4] = {T(0), T(0), T(0), T(0)};
+  for (int q = kb0; q < kb0 + np; ++q) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
+      const int rr = e % NB, kk = e / NB;
+      pi[kk][rr] = m[(bi * NB + rr) + static_cast<Index>(q * NB + kk) * ld];
+      pj[kk][rr] = m[(bj * NB + rr) + static_cast<Index>(q * NB + kk) * ld];
+    }
+    __syncthreads();
 #pragma unroll 8
-  for (int k = 0; k < NB; ++k) {
-    const T a = pi[k][i];
+    for (int k = 0; k < NB; ++k) {
+      const T a = pi[k][i];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) acc[q] += a * pj[k][jy + 8 * q];
+      for (int qq = 0; qq < 4; ++qq) acc[qq] += a * pj[k][jy + 8 * qq];
+    }
   }
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int j = jy + 8 * q;
-    m[(bi * NB + i) + static_cast<Index>(bj * NB + j) * ld] -= acc[q];
+  for (int qq = 0; qq < 4; ++qq) {
+    const int j = jy + 8 * qq;
+    m[(bi * NB + i) + static_cast<Index>(bj * NB + j) * ld] -= acc[qq];
+  }
+}
+
+// Trailing update of a panel group over 64 x 64 tiles (register-tiled: 256 threads, 4 x 4
+// outputs each), C(i, j) -= sum over the panels [kb0, kb0 + np) of L(i, q) L(j, q)^T for the
+// lower tiles from block kb0 + np on. Tiles cover two 32-blocks per side; rows or columns past
+// the domain's last block are skipped, and so is the part of a diagonal tile above the
+// diagonal blocks.
+template <class T>
+__global__ void __launch_bounds__(256)
+    syrk64_update_kernel(int kb0, int np, const int* __restrict__ lds,
+                         const Index* __restrict__ mat_off, T* __restrict__ mats) {
+  const Index d = blockIdx.x;
+  const int ld = lds[d];
+  const int nbd = ld / NB;
+  const int first = kb0 + np;
+  if (first >= nbd) return;
+  const int rem2 = (nbd - first + 1) / 2;
+  const Index ntiles = static_cast<Index>(rem2) * (rem2 + 1) / 2;
+  if (static_cast<Index>(blockIdx.y) >= ntiles) return;
+  int ti, tj;
+  tile_of(blockIdx.y, ti, tj);
+  const int r0 = (first + 2 * ti) * NB, c0 = (first + 2 * tj) * NB;
+  T* m = mats + mat_off[d];
+  __shared__ __align__(16) T sa[NB][64 + 4];  // sa[k][r] = L(r0 + r, q*NB + k)
+  __shared__ __align__(16) T sb[NB][64 + 4];  // sb[k][c] = L(c0 + c, q*NB + k)
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  T acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
+  for (int q = kb0; q < kb0 + np; ++q) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < 64 * NB; e += blockDim.x) {
+      const int rr = e % 64, kk = e / 64;
+      const Index col = static_cast<Index>(q * NB + kk) * ld;
+      sa[kk][rr] = (r0 + rr < ld) ? m[(r0 + rr) + col] : T(0);
+      sb[kk][rr] = (c0 + rr < ld) ? m[(c0 + rr) + col] : T(0);
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int k = 0; k < NB; ++k) {
+      T av[4], bv[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) av[a] = sa[k][ty * 4 + a];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) bv[b] = sb[k][tx * 4 + b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int r = r0 + ty * 4 + a;
+    if (r >= ld) continue;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int c = c0 + tx * 4 + b;
+      if (c >= ld || c / NB > r / NB) continue;  // past the domain, or an upper block
+      m[r + static_cast<Index>(c) * ld] -= acc[a][b];
+    }
   }
 }
 
@@ -855,19 +936,35 @@ void RasPreconditioner<T>::build_batch(DomainBatch<U>& b, const std::vector<Doma
     PGPU_LAUNCH_CHECK();
   }
 
-  // Blocked Cholesky over all domains.
-  for (int kb = 0; kb < nbmax; ++kb) {
-    potrf_diag_kernel<U><<<static_cast<unsigned>(b.n_dom), 32, 0, stream()>>>(
-        kb, b.ld.data(), b.mat_off.data(), b.mats.data(), b.info.data());
-    PGPU_LAUNCH_CHECK();
-    const int rows_below = b.max_n - (kb + 1) * NB;
-    if (rows_below <= 0) continue;
-    dim3 gp(static_cast<unsigned>(b.n_dom), static_cast<unsigned>((rows_below + 127) / 128));
-    trsm_panel_kernel<U><<<gp, 128, 0, stream()>>>(kb, b.ld.data(), b.mat_off.data(), b.mats.data());
-    PGPU_LAUNCH_CHECK();
-    const int rem = nbmax - kb - 1;
-    dim3 gs(static_cast<unsigned>(b.n_dom), static_cast<unsigned>(static_cast<Index>(rem) * (rem + 1) / 2));
-    syrk_update_kernel<U><<<gs, 256, 0, stream()>>>(kb, b.ld.data(), b.mat_off.data(), b.mats.data());
+  // Blocked Cholesky over all domains, in groups of kGroup panels: inside a group each panel is
+  // updated left-looking by the group's earlier panels, factored and solved below; then one
+  // trailing update applies the whole group.
+  constexpr int kGroup = 4;
+  const unsigned nd = static_cast<unsigned>(b.n_dom);
+  for (int g0 = 0; g0 < nbmax; g0 += kGroup) {
+    const int np = std::min(kGroup, nbmax - g0);
+    for (int p = 0; p < np; ++p) {
+      const int kb = g0 + p;
+      if (p > 0) {
+        syrk_update_kernel<U><<<dim3(nd, static_cast<unsigned>(nbmax - kb)), 256, 0, stream()>>>(
+            g0, p, 1, b.ld.data(), b.mat_off.data(), b.mats.data());
+        PGPU_LAUNCH_CHECK();
+      }
+      potrf_diag_kernel<U><<<nd, 32, 0, stream()>>>(kb, b.ld.data(), b.mat_off.data(),
+                                                    b.mats.data(), b.info.data());
+      PGPU_LAUNCH_CHECK();
+      const int rows_below = b.max_n - (kb + 1) * NB;
+      if (rows_below <= 0) continue;
+      dim3 gp(nd, static_cast<unsigned>((rows_below + 127) / 128));
+      trsm_panel_kernel<U><<<gp, 128, 0, stream()>>>(kb, b.ld.data(), b.mat_off.data(), b.mats.data());
+      PGPU_LAUNCH_CHECK();
+    }
+    const int rem = nbmax - g0 - np;
+    if (rem <= 0) continue;
+    const int rem2 = (rem + 1) / 2;
+    dim3 gs(nd, static_cast<unsigned>(static_cast<Index>(rem2) * (rem2 + 1) / 2));
+    syrk64_update_kernel<U><<<gs, 256, 0, stream()>>>(g0, np, b.ld.data(), b.mat_off.data(),
+                                                      b.mats.data());
     PGPU_LAUNCH_CHECK();
   }
   invert_diag_kernel<U><<<dim3(static_cast<unsigned>(b.n_dom), nbmax), 32, 0, stream()>>>(

@@ -271,6 +271,7 @@ class ResidualEvaluator {
     if (!p64_) {
       p64_ = std::make_unique<Evaluator<double>>(model_, bbox_, INFINITY, INFINITY);
       p64_->force_direct(true);
+      p64_->set_ff_direct(precision_ == PGPU_PRECISION_MIXED);
       p64_->set_sources(pts_dev_, mu_, nullptr, 0);
       p64_->set_targets(probe_pts_.data(), n_probe_, nullptr, 0);
     }
@@ -288,6 +289,7 @@ class ResidualEvaluator {
   Evaluator<double>& full() {
     if (!full_) {
       full_ = std::make_unique<Evaluator<double>>(model_, bbox_, accuracy_, accuracy_);
+      full_->set_ff_direct(precision_ == PGPU_PRECISION_MIXED);
       if (order_ > 0) {
         FarFieldConfig c;
         c.order = order_;
@@ -381,6 +383,9 @@ FitResult fit_impl(const FitRequest& req) {
   if (req.precision == PGPU_PRECISION_PLAIN || req.plain_loop) {
     // Operator at accuracy 0 as interpolation/solver.hpp:40.
     Operator<double> op(model, pts.data(), mu, bbox, 0.0, P.data());
+    // Mixed requests below the FP32 threshold: FP64-class float-float direct sums where they
+    // exist (odd polyharmonic kernels).
+    op.evaluator().set_ff_direct(req.precision == PGPU_PRECISION_MIXED);
     Fgmres solver(M, req.max_iter);
     solver.setup(rhs.data(), w.data(), x0_zero, op);
     if (!x0_zero && solver.relative_residual() == 0.0) {
@@ -612,6 +617,7 @@ FitResult fit_impl(const FitRequest& req) {
 template <class T>
 void evaluate_impl(const EvaluateRequest& req) {
   Evaluator<T> ev(*req.model, req.bbox, req.accuracy, req.grad_accuracy);
+  ev.set_ff_direct(req.precision == PGPU_PRECISION_MIXED);
   ev.set_sources(req.centers_dev, req.mu, req.grad_centers_dev, req.sigma);
   ev.set_targets(req.points_dev, req.m, req.grad_points_dev, req.mg);
   ev.set_weights(req.weights_dev);
@@ -629,12 +635,12 @@ FitResult fit(const FitRequest& req) {
   // Kernels of conditional positive definiteness order 2 and above (triharmonic, thin-plate)
   // give domain matrices too ill-conditioned for an FP32 Cholesky factor: their small fits keep
   // the FP64 preconditioner.
-  if (!mixed_pays(mu, mu) && req.model->cpd_order() >= 2) return fit_impl<double>(plain);
+  FitRequest small = req;
+  small.plain_loop = true;
+  if (!mixed_pays(mu, mu) && req.model->cpd_order() >= 2) return fit_impl<double>(small);
   try {
     if (!mixed_pays(mu, mu)) {
-      // Small systems: FP64 operator and residuals (exact direct sums), FP32 preconditioner.
-      FitRequest small = req;
-      small.plain_loop = true;
+      // Small systems: FP64-class operator and residuals (direct sums), FP32 preconditioner.
       return fit_impl<float>(small);
     }
     return fit_impl<float>(req);

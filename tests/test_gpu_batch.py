@@ -35,8 +35,8 @@ def test_batch_uneven_fits(precision):
         fit_vals = oracle.direct_evaluate(model, p, w, p)
         assert np.max(np.abs(fit_vals - v)) <= tol
         want = oracle.direct_evaluate(model, p, w, q)
-        # Fits below 2^30 pairs run the FP64 path in either precision.
-        assert np.max(np.abs(r["values"] - want)) <= 1e-9
+        # Below 2^30 pairs the sums are FP64 (plain) or float-float, FP64-class (mixed).
+        assert np.max(np.abs(r["values"] - want)) <= (1e-9 if precision == pg.PLAIN else 1e-8)
 
 
 def test_batch_result_equals_single_fit():
