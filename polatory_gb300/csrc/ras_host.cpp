@@ -4,6 +4,8 @@
 // [0, k) / [k, n) of the sorted order matters, which yields the same point sets.
 #include "ras_host.hpp"
 
+#include <omp.h>
+
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -65,6 +67,142 @@ void bbox_of(const Geo& g, const std::vector<MixedPoint>& pts, double* mn, doubl
   }
 }
 
+// ---- parallel selection for the large splits --------------------------------------------
+// The first generations of a division split a few huge point sets, which one thread per set
+// would do serially. Above this size a split runs data-parallel: the same point sets as
+// nth_element at the same ranks (ties among identical points resolved arbitrarily, as
+// nth_element does).
+Index g_par_split_min = 262144;
+
+// Bounding box of [b, e), parallel over the range.
+void bbox_range_par(const Geo& g, const MixedPoint* pts, Index n, double* mn, double* mx) {
+  for (int k = 0; k < 3; ++k) {
+    mn[k] = INFINITY;
+    mx[k] = -INFINITY;
+  }
+#pragma omp parallel
+  {
+    double lmn[3] = {INFINITY, INFINITY, INFINITY}, lmx[3] = {-INFINITY, -INFINITY, -INFINITY};
+#pragma omp for schedule(static) nowait
+    for (Index i = 0; i < n; ++i) {
+      const double* c = g.at(pts[i]);
+      for (int k = 0; k < 3; ++k) {
+        lmn[k] = std::min(lmn[k], c[k]);
+        lmx[k] = std::max(lmx[k], c[k]);
+      }
+    }
+#pragma omp critical
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = std::min(mn[k], lmn[k]);
+      mx[k] = std::max(mx[k], lmx[k]);
+    }
+  }
+}
+
+// Rearranges pts[0, n) so that, for the sorted cut ranks c_0 < c_1 < ..., every slice
+// [c_j, c_{j+1}) holds the elements of those ranks under less (what nth_element at each cut
+// gives). Buckets by the primary coordinate (quantiles of a sample), counts in parallel, sorts
+// only the buckets holding a cut, then scatters in parallel.
+void par_multi_select(const Geo& g, MixedPoint* pts, Index n, const LexLess& less,
+                      const std::vector<Index>& cuts) {
+  const int ax0 = less.axes[0];
+  // Primary keys gathered once (the points are scattered in memory).
+  std::vector<double> keys(n);
+#pragma omp parallel for schedule(static)
+  for (Index i = 0; i < n; ++i) keys[i] = g.at(pts[i])[ax0];
+  // Splitters: 4095 quantiles of a regular sample of the primary keys.
+  const Index ns = std::min<Index>(n, 65536);
+  std::vector<double> sample(ns);
+  for (Index i = 0; i < ns; ++i) sample[i] = keys[(i * n) / ns];
+  std::sort(sample.begin(), sample.end());
+  std::vector<double> spl;
+  const int nb_want = 4096;
+  for (int j = 1; j < nb_want; ++j) {
+    const double v = sample[(static_cast<Index>(j) * ns) / nb_want];
+    if (spl.empty() || v > spl.back()) spl.push_back(v);
+  }
+  const int nb = static_cast<int>(spl.size()) + 1;
+  auto bucket_of = [&](double k) {
+    return static_cast<int>(std::upper_bound(spl.begin(), spl.end(), k) - spl.begin());
+  };
+  std::vector<int> bk(n);
+  const int nt = omp_get_max_threads();
+  std::vector<std::vector<Index>> cnt(nt, std::vector<Index>(nb, 0));
+#pragma omp parallel
+  {
+    auto& c = cnt[omp_get_thread_num()];
+#pragma omp for schedule(static)
+    for (Index i = 0; i < n; ++i) {
+      bk[i] = bucket_of(keys[i]);
+      ++c[bk[i]];
+    }
+  }
+  std::vector<Index> start(nb + 1, 0);
+  for (int b = 0; b < nb; ++b) {
+    Index t = 0;
+    for (int th = 0; th < nt; ++th) t += cnt[th][b];
+    start[b + 1] = start[b] + t;
+  }
+  // Group of an element: the number of cuts at or below its rank. Buckets without a cut
+  // inside have one group for all their elements; the others are sorted and split exactly.
+  std::vector<char> exact(nb, 0);
+  for (Index c : cuts) {
+    const int b = static_cast<int>(std::upper_bound(start.begin(), start.end(), c) - start.begin()) - 1;
+    if (b >= 0 && b < nb && c > start[b]) exact[b] = 1;
+  }
+  auto group_of_rank = [&](Index r) {
+    return static_cast<int>(std::upper_bound(cuts.begin(), cuts.end(), r) - cuts.begin());
+  };
+  std::vector<int> bucket_group(nb);
+  for (int b = 0; b < nb; ++b) bucket_group[b] = group_of_rank(start[b]);
+  // Elements of the exact buckets, sorted.
+  std::vector<std::vector<MixedPoint>> ex(nb);
+  for (Index i = 0; i < n; ++i)
+    if (exact[bk[i]]) ex[bk[i]].push_back(pts[i]);
+  std::vector<MixedPoint> out(n);
+  const int ng = static_cast<int>(cuts.size()) + 1;
+  std::vector<Index> gstart(ng + 1, 0);
+  for (int j = 0; j < ng - 1; ++j) gstart[j + 1] = cuts[j];
+  gstart[ng] = n;
+  std::vector<Index> gfill(ng, 0);
+  // Exact buckets first (sequential, they are small).
+  for (int b = 0; b < nb; ++b) {
+    if (!exact[b]) continue;
+    auto& v = ex[b];
+    std::sort(v.begin(), v.end(), less);
+    for (Index j = 0; j < static_cast<Index>(v.size()); ++j) {
+      const int gi = group_of_rank(start[b] + j);
+      out[gstart[gi] + gfill[gi]++] = v[j];
+    }
+  }
+  // The rest: per-thread counts per group, then a parallel scatter.
+  std::vector<std::vector<Index>> gc(nt, std::vector<Index>(ng, 0));
+#pragma omp parallel
+  {
+    auto& c = gc[omp_get_thread_num()];
+#pragma omp for schedule(static)
+    for (Index i = 0; i < n; ++i)
+      if (!exact[bk[i]]) ++c[bucket_group[bk[i]]];
+  }
+  std::vector<std::vector<Index>> goff(nt, std::vector<Index>(ng, 0));
+  for (int gi = 0; gi < ng; ++gi) {
+    Index o = gstart[gi] + gfill[gi];
+    for (int th = 0; th < nt; ++th) {
+      goff[th][gi] = o;
+      o += gc[th][gi];
+    }
+  }
+#pragma omp parallel
+  {
+    auto& o = goff[omp_get_thread_num()];
+#pragma omp for schedule(static)
+    for (Index i = 0; i < n; ++i)
+      if (!exact[bk[i]]) out[o[bucket_group[bk[i]]]++] = pts[i];
+  }
+#pragma omp parallel for schedule(static)
+  for (Index i = 0; i < n; ++i) pts[i] = out[i];
+}
+
 // std::ceil((d - 0.5) / 2.0) + std::floor((d + 0.5) / 2.0) (domain_divider.hpp:311-313).
 double round_half_to_even(double d) { return std::ceil((d - 0.5) / 2.0) + std::floor((d + 0.5) / 2.0); }
 
@@ -74,16 +212,18 @@ Index last_le(const std::vector<Index>& prefix, Index v) {
 }
 
 // Splits one domain into two overlapping halves (domain_divider.hpp:161-269).
-void divide_domain(const Geo& g, const Domain& d, Domain& left, Domain& right) {
+void divide_domain(const Geo& g, const Domain& d, Domain& left, Domain& right, bool par_ok) {
   const Index mu = d.num_points(), sigma = d.num_grad_points();
-  std::vector<MixedPoint> mp;
-  mp.reserve(mu + sigma);
-  for (Index i = 0; i < mu; ++i) mp.push_back({d.point_indices[i], d.inner_point[i] != 0, false});
+  const bool par = par_ok && sigma == 0 && mu >= g_par_split_min;
+  std::vector<MixedPoint> mp(mu + sigma);
+#pragma omp parallel for schedule(static) if (par)
+  for (Index i = 0; i < mu; ++i) mp[i] = {d.point_indices[i], d.inner_point[i] != 0, false};
   for (Index i = 0; i < sigma; ++i)
-    mp.push_back({d.grad_point_indices[i], d.inner_grad_point[i] != 0, true});
+    mp[mu + i] = {d.grad_point_indices[i], d.inner_grad_point[i] != 0, true};
 
   double mn[3], mx[3];
-  bbox_of(g, mp, mn, mx);
+  if (par) bbox_range_par(g, mp.data(), static_cast<Index>(mp.size()), mn, mx);
+  else bbox_of(g, mp, mn, mx);
   LexLess less{&g, axes_by_width(mn, mx)};
 
   const Index n_points = mu + sigma;
@@ -101,10 +241,17 @@ void divide_domain(const Geo& g, const Domain& d, Domain& left, Domain& right) {
     left_part = left_mult;
     right_part = right_mult;
     mid = mid_mult;
-    std::nth_element(mp.begin(), mp.begin() + mid, mp.end(), less);
-    if (left_part < mid) std::nth_element(mp.begin(), mp.begin() + left_part, mp.begin() + mid, less);
-    if (right_part > mid && right_part < n_points)
-      std::nth_element(mp.begin() + mid, mp.begin() + right_part, mp.end(), less);
+    if (par) {
+      std::vector<Index> cuts;
+      for (Index c : {left_part, mid, right_part})
+        if (c > 0 && c < n_points && (cuts.empty() || c > cuts.back())) cuts.push_back(c);
+      par_multi_select(g, mp.data(), n_points, less, cuts);
+    } else {
+      std::nth_element(mp.begin(), mp.begin() + mid, mp.end(), less);
+      if (left_part < mid) std::nth_element(mp.begin(), mp.begin() + left_part, mp.begin() + mid, less);
+      if (right_part > mid && right_part < n_points)
+        std::nth_element(mp.begin() + mid, mp.begin() + right_part, mp.end(), less);
+    }
   } else {
     std::sort(mp.begin(), mp.end(), less);
     std::vector<Index> prefix{0};
@@ -115,6 +262,26 @@ void divide_domain(const Geo& g, const Domain& d, Domain& left, Domain& right) {
     mid = last_le(prefix, mid_mult);
   }
 
+  if (par) {
+    // Value points only: fill both halves in parallel.
+    left.point_indices.resize(right_part);
+    left.inner_point.resize(right_part);
+    right.point_indices.resize(n_points - left_part);
+    right.inner_point.resize(n_points - left_part);
+#pragma omp parallel for schedule(static)
+    for (Index i = 0; i < n_points; ++i) {
+      const auto& p = mp[i];
+      if (i < right_part) {
+        left.point_indices[i] = p.index;
+        left.inner_point[i] = (p.inner && i < mid) ? 1 : 0;
+      }
+      if (i >= left_part) {
+        right.point_indices[i - left_part] = p.index;
+        right.inner_point[i - left_part] = (p.inner && i >= mid) ? 1 : 0;
+      }
+    }
+    return;
+  }
   for (Index i = 0; i < right_part; ++i) {
     const auto& p = mp[i];
     const char inner = (p.inner && i < mid) ? 1 : 0;
@@ -183,29 +350,60 @@ struct Segment {
 // bbox centre (the reference takes the first such point in its sorted parent order; two-point
 // clusters always tie). nullptr for the root (input order).
 void init_segment(const Geo& g, std::vector<MixedPoint>& pts, Segment& s,
-                  const LexLess* parent_less = nullptr) {
+                  const LexLess* parent_less = nullptr, bool par = false) {
   double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
   s.has_grad = false;
-  for (Index i = s.b; i < s.e; ++i) {
-    const double* c = g.at(pts[i]);
-    for (int k = 0; k < 3; ++k) {
-      mn[k] = std::min(mn[k], c[k]);
-      mx[k] = std::max(mx[k], c[k]);
+  if (par) {
+    bbox_range_par(g, pts.data() + s.b, s.e - s.b, mn, mx);
+    for (Index i = s.b; i < s.e && !s.has_grad; ++i) s.has_grad |= pts[i].grad;
+  } else {
+    for (Index i = s.b; i < s.e; ++i) {
+      const double* c = g.at(pts[i]);
+      for (int k = 0; k < 3; ++k) {
+        mn[k] = std::min(mn[k], c[k]);
+        mx[k] = std::max(mx[k], c[k]);
+      }
+      s.has_grad |= pts[i].grad;
     }
-    s.has_grad |= pts[i].grad;
   }
   s.volume = (mx[0] - mn[0]) * (mx[1] - mn[1]) * (mx[2] - mn[2]);
   double ctr[3];
   for (int k = 0; k < 3; ++k) ctr[k] = mn[k] + (mx[k] - mn[k]) / 2.0;
-  double best = INFINITY;
-  for (Index i = s.b; i < s.e; ++i) {
-    const double* q = g.at(pts[i]);
-    double dx = q[0] - ctr[0], dy = q[1] - ctr[1], dz = q[2] - ctr[2];
-    double d2 = dx * dx + dy * dy + dz * dz;
-    if (d2 < best || (d2 == best && parent_less && (*parent_less)(pts[i], s.center))) {
-      best = d2;
-      s.center = pts[i];
+  // The point nearest to the centre; ties go to the parent's lexicographic order, then to the
+  // earlier position (chunks are combined in order, so the parallel scan picks the same one).
+  auto better = [&](double d2, const MixedPoint& p, double best, const MixedPoint& cur) {
+    return d2 < best || (d2 == best && parent_less && (*parent_less)(p, cur));
+  };
+  auto scan = [&](Index b, Index e, double& best, MixedPoint& c) {
+    for (Index i = b; i < e; ++i) {
+      const double* q = g.at(pts[i]);
+      double dx = q[0] - ctr[0], dy = q[1] - ctr[1], dz = q[2] - ctr[2];
+      double d2 = dx * dx + dy * dy + dz * dz;
+      if (better(d2, pts[i], best, c)) {
+        best = d2;
+        c = pts[i];
+      }
     }
+  };
+  double best = INFINITY;
+  if (par) {
+    const int nt = omp_get_max_threads();
+    std::vector<double> tb(nt, INFINITY);
+    std::vector<MixedPoint> tc(nt, s.center);
+    const Index n = s.e - s.b;
+#pragma omp parallel num_threads(nt)
+    {
+      const int t = omp_get_thread_num();
+      const Index b = s.b + (n * t) / nt, e = s.b + (n * (t + 1)) / nt;
+      scan(b, e, tb[t], tc[t]);
+    }
+    for (int t = 0; t < nt; ++t)
+      if (tb[t] < INFINITY && better(tb[t], tc[t], best, s.center)) {
+        best = tb[t];
+        s.center = tc[t];
+      }
+  } else {
+    scan(s.b, s.e, best, s.center);
   }
   if (s.has_grad) {
     LexLess less{&g, axes_by_width(mn, mx)};
@@ -216,15 +414,20 @@ void init_segment(const Geo& g, std::vector<MixedPoint>& pts, Segment& s,
 // Splits a segment at the position minimising |2 prefix(i) - size| with the tie rule of
 // std::min_element and the comparator of domain_divider.hpp:82-88; children are initialised.
 void split_segment(const Geo& g, std::vector<MixedPoint>& pts, const Segment& s, Segment& left,
-                   Segment& right) {
+                   Segment& right, bool par_ok = false) {
   const Index n = s.e - s.b;
+  const bool par = par_ok && !s.has_grad && n >= g_par_split_min;
   Index mid = 0;
   double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-  for (Index i = s.b; i < s.e; ++i) {
-    const double* c = g.at(pts[i]);
-    for (int k = 0; k < 3; ++k) {
-      mn[k] = std::min(mn[k], c[k]);
-      mx[k] = std::max(mx[k], c[k]);
+  if (par) {
+    bbox_range_par(g, pts.data() + s.b, n, mn, mx);
+  } else {
+    for (Index i = s.b; i < s.e; ++i) {
+      const double* c = g.at(pts[i]);
+      for (int k = 0; k < 3; ++k) {
+        mn[k] = std::min(mn[k], c[k]);
+        mx[k] = std::max(mx[k], c[k]);
+      }
     }
   }
   const LexLess less{&g, axes_by_width(mn, mx)};
@@ -250,18 +453,24 @@ void split_segment(const Geo& g, std::vector<MixedPoint>& pts, const Segment& s,
         bestd = di;
       }
     }
-    if (mid > 0 && mid < n)
-      std::nth_element(pts.begin() + s.b, pts.begin() + s.b + mid, pts.begin() + s.e, less);
+    if (mid > 0 && mid < n) {
+      if (par)
+        par_multi_select(g, pts.data() + s.b, n, less, {mid});
+      else
+        std::nth_element(pts.begin() + s.b, pts.begin() + s.b + mid, pts.begin() + s.e, less);
+    }
   }
   left.b = s.b;
   left.e = s.b + mid;
   right.b = s.b + mid;
   right.e = s.e;
-  if (left.e > left.b) init_segment(g, pts, left, &less);
-  if (right.e > right.b) init_segment(g, pts, right, &less);
+  if (left.e > left.b) init_segment(g, pts, left, &less, par);
+  if (right.e > right.b) init_segment(g, pts, right, &less, par);
 }
 
 }  // namespace
+
+void set_parallel_split_min(Index n) { g_par_split_min = n; }
 
 DomainDivider::DomainDivider(const double* points, const double* grad_points,
                              const std::vector<Index>& point_indices,
@@ -286,13 +495,26 @@ DomainDivider::DomainDivider(const double* points, const double* grad_points,
     const Index n = static_cast<Index>(current.size());
     std::vector<char> split(n, 0);
     std::vector<Domain> lefts(n), rights(n);
-#pragma omp parallel for schedule(dynamic, 1)
+    std::vector<Index> big, small;
+    Index n_split = 0;
     for (Index i = 0; i < n; ++i) {
-      auto& d = current[i];
+      const auto& d = current[i];
+      if (d.num_points() + 3 * d.num_grad_points() > kMaxLeafSize) ++n_split;
+    }
+    // While there are fewer domains to split than threads, the huge ones split data-parallel.
+    const bool few = n_split < omp_get_max_threads();
+    for (Index i = 0; i < n; ++i) {
+      const auto& d = current[i];
       if (d.num_points() + 3 * d.num_grad_points() <= kMaxLeafSize) continue;
       split[i] = 1;
-      divide_domain(g, d, lefts[i], rights[i]);
+      (few && d.num_grad_points() == 0 && d.num_points() >= g_par_split_min ? big : small).push_back(i);
     }
+    // Huge domains one at a time, each split data-parallel; the rest one per thread.
+    for (Index i : big) divide_domain(g, current[i], lefts[i], rights[i], true);
+    const Index ns = static_cast<Index>(small.size());
+#pragma omp parallel for schedule(dynamic, 1)
+    for (Index k = 0; k < ns; ++k)
+      divide_domain(g, current[small[k]], lefts[small[k]], rights[small[k]], false);
     std::vector<Domain> next;
     for (Index i = 0; i < n; ++i) {
       if (!split[i]) {
@@ -340,14 +562,19 @@ std::pair<std::vector<Index>, std::vector<Index>> DomainDivider::choose_coarse_p
   cur[0].e = static_cast<Index>(pts.size());
   std::vector<Segment> finals;
   if (pts.empty()) return {std::move(idcs), std::move(grad_idcs)};
-  init_segment(g, pts, cur[0]);
+  init_segment(g, pts, cur[0], nullptr, static_cast<Index>(pts.size()) >= g_par_split_min);
   Index count = cur[0].center.mult();
 
   while (count < n_coarse && !cur.empty()) {
     const Index ns = static_cast<Index>(cur.size());
     std::vector<Segment> left(ns), right(ns);
+    if (ns < omp_get_max_threads()) {
+      // Few clusters: split them one at a time, each data-parallel when huge.
+      for (Index s = 0; s < ns; ++s) split_segment(g, pts, cur[s], left[s], right[s], true);
+    } else {
 #pragma omp parallel for schedule(dynamic, 1)
-    for (Index s = 0; s < ns; ++s) split_segment(g, pts, cur[s], left[s], right[s]);
+      for (Index s = 0; s < ns; ++s) split_segment(g, pts, cur[s], left[s], right[s]);
+    }
     // Accept the splits in the reference's order.
     std::vector<Index> order(ns);
     for (Index s = 0; s < ns; ++s) order[s] = s;

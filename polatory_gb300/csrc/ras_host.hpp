@@ -24,6 +24,10 @@ struct Domain {
 // domain_divider.hpp:18-321): recursive splits along the widest axes with an overlap quota of
 // 0.5 down to at most 1024 points (gradient points count three times); coarse points chosen by
 // priority-queue bisection. points/grad_points: host xyz rows of the full point sets.
+// Point sets of at least n points are split data-parallel (same results as the sequential
+// selection); the tests lower it to cover that path on small inputs.
+void set_parallel_split_min(Index n);
+
 class DomainDivider {
  public:
   DomainDivider(const double* points, const double* grad_points,

@@ -165,7 +165,35 @@ static void check_coarse_equivalence(Index n, Index n_coarse, unsigned seed) {
   CHECK(got.size() == want.size());
 }
 
+// The data-parallel split of large point sets gives the same domains and coarse points as the
+// sequential selection.
+static void check_parallel_splits(Index n_points, unsigned seed) {
+  std::mt19937 gen(seed);
+  std::uniform_real_distribution<double> u(-1.0, 1.0);
+  std::vector<double> pts(3 * n_points);
+  for (auto& v : pts) v = u(gen);
+  std::vector<Index> idx(n_points), none;
+  std::iota(idx.begin(), idx.end(), 0);
+  std::vector<Index> poly{0, 1, 2, 3};
+  pgpu::set_parallel_split_min(Index{1} << 40);
+  pgpu::DomainDivider seq(pts.data(), nullptr, idx, none, poly);
+  auto cseq = seq.choose_coarse_points(n_points / 10).first;
+  pgpu::set_parallel_split_min(2000);
+  pgpu::DomainDivider par(pts.data(), nullptr, idx, none, poly);
+  auto cpar = par.choose_coarse_points(n_points / 10).first;
+  pgpu::set_parallel_split_min(262144);
+  CHECK(seq.domains().size() == par.domains().size());
+  for (size_t k = 0; k < std::min(seq.domains().size(), par.domains().size()); ++k) {
+    CHECK(seq.domains()[k].point_indices == par.domains()[k].point_indices);
+    CHECK(seq.domains()[k].inner_point == par.domains()[k].inner_point);
+  }
+  std::sort(cseq.begin(), cseq.end());
+  std::sort(cpar.begin(), cpar.end());
+  CHECK(cseq == cpar);
+}
+
 int main() {
+  check_parallel_splits(30000, 7);
   check_divider(10000, 10000, 10, 1);
   check_divider(20000, 0, 4, 2);
   check_divider(5000, 3000, 1, 3);
