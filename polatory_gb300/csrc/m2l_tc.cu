@@ -293,7 +293,9 @@ __global__ void __launch_bounds__(256, 1)
   auto b_hi = [&](int s) { return stage_f + s * kStageFloats + 2 * kAFloats; };
   auto b_lo = [&](int s) { return stage_f + s * kStageFloats + 2 * kAFloats + kBFloats; };
 
-  // Issues the loads of iteration i into stage i % kStages.
+  // Issues the loads of iteration i into stage i % kStages. Loads are issued in iteration
+  // order, so the source cell of the row is looked up once per offset (at its first chunk).
+  int src = -1;
   auto load = [&](int i) {
     const int s = i % kStages;
     const int o = olist[q_beg + i / kChunks];
@@ -304,7 +306,7 @@ __global__ void __launch_bounds__(256, 1)
       bulk_g2s(smem_u32(b_hi(s)), kb_hi + blk, kBBytes, load_bar(s));
       bulk_g2s(smem_u32(b_lo(s)), kb_lo + blk, kBBytes, load_bar(s));
     }
-    const int src = g_valid ? table[g_cell * kNOffsets + o] : -1;
+    if (c == 0) src = g_valid ? table[g_cell * kNOffsets + o] : -1;
     float* dst = a_hi(s);
 #pragma unroll
     for (int jj = 0; jj < 2; ++jj) {
@@ -377,8 +379,8 @@ __global__ void __launch_bounds__(256, 1)
     if (!ok) atomicExch(reinterpret_cast<int*>(&misc[1]), 1);
   }
   // Drain every MMA still in flight before TMEM is freed.
-  if (tid == 0) mma_commit(smem_u32(&bars[kBars - 1]));
-  const bool drained = mbar_wait(smem_u32(&bars[kBars - 1]), 0);
+  if (tid == 0) mma_commit(smem_u32(&bars[2 * kStages + 2]));
+  const bool drained = mbar_wait(smem_u32(&bars[2 * kStages + 2]), 0);
   __syncthreads();
   aborted = misc[1] != 0 || !drained;
   if (tid == 0 && aborted) atomicExch(err, 1);
