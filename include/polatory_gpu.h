@@ -204,6 +204,11 @@ int pgpu_interpolant_num_centers(const pgpu_interpolant* it, int64_t* mu, int64_
 int pgpu_interpolant_centers(const pgpu_interpolant* it, double* centers, double* grad_centers);
 int pgpu_interpolant_bbox(const pgpu_interpolant* it, double bbox[6]);
 int pgpu_interpolant_fit_stats(const pgpu_interpolant* it, pgpu_fit_stats* out);
+/* Interpolant::save / Interpolant::load (interpolant.hpp:218, POLATORY_IMPLEMENT_LOAD_SAVE,
+ * with Write/Read<Interpolant> at interpolant.hpp:345-367): the reference's binary file format,
+ * so models move between the two implementations. Errors: "cannot open file '<name>'". */
+int pgpu_interpolant_save(const pgpu_interpolant* it, const char* filename);
+int pgpu_interpolant_load(const char* filename, pgpu_interpolant** out);
 
 /* ---- batched fits (no single reference counterpart: Interpolant::fit over many problems) --- */
 /* One independent fit (+ optional evaluation). Inputs are host or device pointers; outputs are

@@ -217,6 +217,20 @@ class Interpolant:
     def set_precision(self, precision: int):
         check(lib.pgpu_interpolant_set_precision(self._h, precision))
 
+    def save(self, filename: str) -> None:
+        """Interpolant::save: the reference's binary format."""
+        check(lib.pgpu_interpolant_save(self._h, str(filename).encode()))
+
+    @classmethod
+    def load(cls, filename: str, precision: int = PLAIN) -> "Interpolant":
+        """Interpolant::load: reads the reference's binary format (model, centers, weights)."""
+        obj = cls.__new__(cls)
+        obj.model = None
+        obj._h = C.c_void_p()
+        check(lib.pgpu_interpolant_load(str(filename).encode(), C.byref(obj._h)))
+        check(lib.pgpu_interpolant_set_precision(obj._h, precision))
+        return obj
+
     def fit(self, points, values, tolerance, max_iter=100, accuracy=INF, initial=None, *,
             grad_points=None, grad_tolerance=INF, grad_accuracy=INF):
         pts = as_points(points)

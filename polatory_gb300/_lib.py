@@ -129,6 +129,8 @@ def _load():
         "pgpu_interpolant_centers": ([P, P, P], C.c_int),
         "pgpu_interpolant_bbox": ([P, P], C.c_int),
         "pgpu_interpolant_fit_stats": ([P, C.POINTER(PgpuFitStats)], C.c_int),
+        "pgpu_interpolant_save": ([P, C.c_char_p], C.c_int),
+        "pgpu_interpolant_load": ([C.c_char_p, C.POINTER(P)], C.c_int),
         "pgpu_fit_batch": ([C.POINTER(PgpuModel), C.c_int, C.POINTER(PgpuFitProblem), I64,
                             C.c_int], C.c_int),
         "pgpu_server_create": ([C.c_int, I64, C.POINTER(P)], C.c_int),

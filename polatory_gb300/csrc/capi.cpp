@@ -1,5 +1,6 @@
 // The C ABI (include/polatory_gpu.h): status codes, thread-local error messages, handles.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -804,4 +805,166 @@ int pgpu_server_stats_get(pgpu_server* s, pgpu_server_stats* out) {
 int64_t pgpu_server_estimate_bytes(const pgpu_request* req) {
   if (!req) return -1;
   return server_estimate(*req);
+}
+
+// ---- save / load (the reference's binary format) -------------------------------------------
+// common/io.hpp:31-187 with Write<Interpolant> (interpolant.hpp:345-367), Write<Model>
+// (model.hpp:304-320), Write<Rbf> (rbf/rbf_io.hpp), Write<Bbox> (geometry/bbox3d.hpp:82-96):
+// trivially copyable values as their bytes; std::string and std::vector as a size_t count and
+// the elements; dynamic Eigen matrices as their Index row count (fixed columns are not written)
+// and the data in storage order (points row-major); fixed-size matrices as their data
+// (anisotropy row-major). Little-endian, as on both hosts.
+
+namespace {
+
+const char* const kShortNames[PGPU_RBF_COUNT] = {"bh2", "bh3", "cub", "exp", "gau", "gc3",
+                                                 "gc5", "gc7", "gc9", "sph", "sp3", "sp5",
+                                                 "sp7", "sp9", "th2", "th3"};
+
+struct Out {
+  std::vector<char> b;
+  template <class V>
+  void put(const V& v) {
+    const char* p = reinterpret_cast<const char*>(&v);
+    b.insert(b.end(), p, p + sizeof(V));
+  }
+  void put_doubles(const double* p, size_t n) {
+    const char* c = reinterpret_cast<const char*>(p);
+    b.insert(b.end(), c, c + n * sizeof(double));
+  }
+};
+
+struct In {
+  const std::vector<char>& b;
+  size_t pos = 0;
+  template <class V>
+  V get() {
+    if (pos + sizeof(V) > b.size()) throw_runtime("unexpected end of the interpolant file");
+    V v;
+    std::memcpy(&v, b.data() + pos, sizeof(V));
+    pos += sizeof(V);
+    return v;
+  }
+  void get_doubles(double* p, size_t n) {
+    if (pos + n * sizeof(double) > b.size()) throw_runtime("unexpected end of the interpolant file");
+    std::memcpy(p, b.data() + pos, n * sizeof(double));
+    pos += n * sizeof(double);
+  }
+};
+
+std::vector<char> serialize(const pgpu_interpolant* it) {
+  Out o;
+  o.put(static_cast<uint64_t>(it->model.rbfs.size()));
+  for (const auto& r : it->model.rbfs) {
+    const std::string name = kShortNames[r.kind];
+    o.put(static_cast<uint64_t>(name.size()));
+    o.b.insert(o.b.end(), name.begin(), name.end());
+    o.put(static_cast<uint64_t>(2));
+    o.put_doubles(r.p, 2);
+    o.put_doubles(r.a, 9);
+  }
+  o.put(static_cast<int32_t>(it->model.poly_degree));
+  o.put(it->model.nugget);
+  o.put(static_cast<uint8_t>(it->fitted ? 1 : 0));
+  o.put(static_cast<int64_t>(it->mu));
+  o.put_doubles(it->centers_host.data(), 3 * static_cast<size_t>(it->mu));
+  std::vector<double> g(3 * static_cast<size_t>(it->sigma));
+  if (it->sigma > 0) copy_out(g.data(), it->grad_centers.data(), g.size());
+  o.put(static_cast<int64_t>(it->sigma));
+  o.put_doubles(g.data(), g.size());
+  o.put_doubles(it->bbox.min, 3);
+  o.put_doubles(it->bbox.max, 3);
+  std::vector<double> w(it->fitted ? it->weights.size() : 0);
+  if (!w.empty()) copy_out(w.data(), it->weights.data(), w.size());
+  o.put(static_cast<int64_t>(w.size()));
+  o.put_doubles(w.data(), w.size());
+  return std::move(o.b);
+}
+
+std::unique_ptr<pgpu_interpolant> deserialize(const std::vector<char>& bytes) {
+  In in{bytes};
+  pgpu_model m{};
+  const uint64_t n_rbfs = in.get<uint64_t>();
+  if (n_rbfs < 1 || n_rbfs > 4) throw_runtime("unsupported number of RBFs in the interpolant file");
+  m.n_rbfs = static_cast<int32_t>(n_rbfs);
+  for (uint64_t k = 0; k < n_rbfs; ++k) {
+    const uint64_t len = in.get<uint64_t>();
+    if (len > 16) throw_runtime("bad RBF name in the interpolant file");
+    std::string name(len, '\0');
+    for (auto& ch : name) ch = in.get<char>();
+    int kind = -1;
+    for (int q = 0; q < PGPU_RBF_COUNT; ++q)
+      if (name == kShortNames[q]) kind = q;
+    if (kind < 0) throw_runtime("unknown RBF '" + name + "' in the interpolant file");
+    const uint64_t np = in.get<uint64_t>();
+    if (np > 2) throw_runtime("bad RBF parameters in the interpolant file");
+    m.rbfs[k].kind = kind;
+    m.rbfs[k].params[0] = 1.0;
+    m.rbfs[k].params[1] = 0.0;
+    in.get_doubles(m.rbfs[k].params, np);
+    in.get_doubles(m.rbfs[k].aniso, 9);
+  }
+  m.poly_degree = in.get<int32_t>();
+  m.nugget = in.get<double>();
+  auto it = std::make_unique<pgpu_interpolant>();
+  it->model = model_from_c(&m);
+  const bool fitted = in.get<uint8_t>() != 0;
+  const int64_t mu = in.get<int64_t>();
+  if (mu < 0) throw_runtime("bad point count in the interpolant file");
+  std::vector<double> pts(3 * static_cast<size_t>(mu));
+  in.get_doubles(pts.data(), pts.size());
+  const int64_t sigma = in.get<int64_t>();
+  if (sigma < 0) throw_runtime("bad point count in the interpolant file");
+  std::vector<double> gpts(3 * static_cast<size_t>(sigma));
+  in.get_doubles(gpts.data(), gpts.size());
+  in.get_doubles(it->bbox.min, 3);
+  in.get_doubles(it->bbox.max, 3);
+  const int64_t nw = in.get<int64_t>();
+  if (nw < 0) throw_runtime("bad weight count in the interpolant file");
+  std::vector<double> w(static_cast<size_t>(nw));
+  in.get_doubles(w.data(), w.size());
+  if (fitted) {
+    if (nw != mu + 3 * sigma + it->model.l())
+      throw_runtime("the weights of the interpolant file do not match its centers");
+    it->weights.upload(w);
+    it->centers.upload(pts);
+    it->grad_centers.upload(gpts);
+    pgpu::sync();
+  }
+  it->centers_host = std::move(pts);
+  it->mu = mu;
+  it->sigma = sigma;
+  it->fitted = fitted;
+  return it;
+}
+
+}  // namespace
+
+int pgpu_interpolant_save(const pgpu_interpolant* it, const char* filename) {
+  return guarded([&] {
+    check_ptr(it, "interpolant");
+    check_ptr(filename, "filename");
+    const std::vector<char> bytes = serialize(it);
+    std::FILE* f = std::fopen(filename, "wb");
+    if (!f) throw_runtime(std::string("cannot open file '") + filename + "'");
+    const size_t wrote = std::fwrite(bytes.data(), 1, bytes.size(), f);
+    const int closed = std::fclose(f);
+    if (wrote != bytes.size() || closed != 0)
+      throw_runtime(std::string("cannot write file '") + filename + "'");
+  });
+}
+
+int pgpu_interpolant_load(const char* filename, pgpu_interpolant** out) {
+  return guarded([&] {
+    check_ptr(filename, "filename");
+    check_ptr(out, "out");
+    std::FILE* f = std::fopen(filename, "rb");
+    if (!f) throw_runtime(std::string("cannot open file '") + filename + "'");
+    std::vector<char> bytes;
+    char buf[1 << 16];
+    size_t got;
+    while ((got = std::fread(buf, 1, sizeof(buf), f)) > 0) bytes.insert(bytes.end(), buf, buf + got);
+    std::fclose(f);
+    *out = deserialize(bytes).release();
+  });
 }
