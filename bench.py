@@ -347,6 +347,20 @@ def cpu_baseline(pts, vals, q, budget_n_fit=3000, n_eval=2000):
                       f"evaluation at {sq.shape[0]} sampled queries ({dt:.2f} s)"}
 
 
+def combine_ranks(dist, ms, world, n_units, steps, device):
+    """Replicas: every rank ran the same workload; the job's time is the slowest rank's
+    (max over ranks, after a barrier) and its value the units of all ranks over that time."""
+    import torch
+
+    t_max = ms
+    if dist is not None:
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+        dist.barrier()
+    return t_max, world * n_units * steps / (t_max * 1e-3)
+
+
 def dist_setup(args):
     if args.gpus <= 1 or "RANK" not in os.environ:
         return 0, 1, 0, None
@@ -445,13 +459,7 @@ def main():
     launches = pg.launch_count() - launches0
     report = pg.profile_report()
     pg.profile_enable(False)
-    t_max = ms
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-        dist.barrier()
-    value = world * n_units * args.steps / (t_max * 1e-3)
+    t_max, value = combine_ranks(dist, ms, world, n_units, args.steps, dev)
     mixed_out = out_d.cpu().numpy()
     stats = interp.fit_stats
 
