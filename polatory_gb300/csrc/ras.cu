@@ -395,14 +395,14 @@ __device__ void chol_solve_inplace(double* x, const T* __restrict__ m, int ld) {
   for (int kb = 0; kb < nb; ++kb) {
     const int base = kb * NB;
     if (warp == 0) {
-      double a[NB];
-#pragma unroll
-      for (int jj = 0; jj < NB; ++jj)
-        a[jj] = jj <= lane ? static_cast<double>(m[(base + lane) + static_cast<Index>(base + jj) * ld]) : 0.0;
+      // y_blk = L_kk^{-1} b_blk (the inverted diagonal block, lower triangular).
       const double bi = x[base + lane];
       double yi = 0;
-#pragma unroll
-      for (int jj = 0; jj < NB; ++jj) yi += a[jj] * __shfl_sync(0xffffffffu, bi, jj);
+#pragma unroll 8
+      for (int jj = 0; jj < NB; ++jj) {
+        const double a = jj <= lane ? static_cast<double>(m[(base + lane) + static_cast<Index>(base + jj) * ld]) : 0.0;
+        yi += a * __shfl_sync(0xffffffffu, bi, jj);
+      }
       x[base + lane] = yi;
     }
     __syncthreads();
@@ -428,14 +428,13 @@ __device__ void chol_solve_inplace(double* x, const T* __restrict__ m, int ld) {
     __syncthreads();
     if (warp == 0) {
       // x_blk = L_kk^{-T} y_blk: lane i sums inv[j][i] y_j over j >= i (column i of the block).
-      double a[NB];
-#pragma unroll
-      for (int jj = 0; jj < NB; ++jj)
-        a[jj] = jj >= lane ? static_cast<double>(m[(base + jj) + static_cast<Index>(base + lane) * ld]) : 0.0;
       const double yi = x[base + lane];
       double zi = 0;
-#pragma unroll
-      for (int jj = 0; jj < NB; ++jj) zi += a[jj] * __shfl_sync(0xffffffffu, yi, jj);
+#pragma unroll 8
+      for (int jj = 0; jj < NB; ++jj) {
+        const double a = jj >= lane ? static_cast<double>(m[(base + jj) + static_cast<Index>(base + lane) * ld]) : 0.0;
+        zi += a * __shfl_sync(0xffffffffu, yi, jj);
+      }
       x[base + lane] = zi;
     }
     __syncthreads();
@@ -526,7 +525,7 @@ __global__ void coarse_finish_kernel(const Index* __restrict__ dp, int n, int l,
 // Cholesky factor, expand lambda = Q gamma and scatter the owned entries
 // (fine_grid.hpp:97-156, coarse_grid.hpp:91-131).
 template <class T>
-__global__ void ras_solve_kernel(const int* __restrict__ nsz, const int* __restrict__ lds,
+__global__ void __launch_bounds__(256, 4) ras_solve_kernel(const int* __restrict__ nsz, const int* __restrict__ lds,
                                  const Index* __restrict__ mat_off, const T* __restrict__ mats,
                                  const Index* __restrict__ pt_off, const Index* __restrict__ pts,
                                  const char* __restrict__ inner, int l,
