@@ -347,6 +347,28 @@ def cpu_baseline(pts, vals, q, budget_n_fit=3000, n_eval=2000):
                       f"evaluation at {sq.shape[0]} sampled queries ({dt:.2f} s)"}
 
 
+def exact_residual_sample(pg, model, pts, vals, w, n_sample=10000, seed=11):
+    """The mixed fit's residual recomputed with exact FP64 direct sums at n_sample data points
+    drawn at random (outside the timed region): max |value - (sum_j w_j phi + polynomial)|."""
+    g = np.random.Generator(np.random.PCG64(seed))
+    idx = np.sort(g.choice(pts.shape[0], min(n_sample, pts.shape[0]), replace=False))
+    n = pts.shape[0]
+    lo, hi = pts.min(0), pts.max(0)
+    ev = pg.FmmEvaluator(model.rbfs[0], np.concatenate([lo, hi]), precision=pg.PLAIN)
+    ev.configure(backend=1)
+    ev.set_source_points(pts)
+    ev.set_target_points(pts[idx])
+    ev.set_weights(w[:n])
+    fit = ev.evaluate()
+    c = w[n:]
+    q = pts[idx]
+    if c.shape[0] >= 1:
+        fit = fit + c[0]
+    if c.shape[0] >= 4:
+        fit = fit + c[1] * q[:, 0] + c[2] * q[:, 1] + c[3] * q[:, 2]
+    return {"points": int(idx.shape[0]), "max_abs": float(np.max(np.abs(fit - vals[idx])))}
+
+
 def combine_ranks(dist, ms, world, n_units, steps, device):
     """Replicas: every rank ran the same workload; the job's time is the slowest rank's
     (max over ranks, after a barrier) and its value the units of all ranks over that time."""
@@ -462,6 +484,7 @@ def main():
     t_max, value = combine_ranks(dist, ms, world, n_units, args.steps, dev)
     mixed_out = out_d.cpu().numpy()
     stats = interp.fit_stats
+    exact_res = exact_residual_sample(pg, model, pts, vals, interp.weights) if rank == 0 else None
 
     # End to end through the C ABI with host buffers (copies inside the timed region).
     e2e_interp = pg.Interpolant(model, pg.MIXED)
@@ -507,6 +530,7 @@ def main():
         "regions": regions,
         "cpu_baseline": cpu, "clocks": clk.summary(), "plain_fp64": plain,
         "fit": {"iterations": iters, "levels": stats["levels"], "residual": stats["residual"],
+                "fp64_residual_sample": exact_res,
                 "setup_s": stats["setup_seconds"], "solve_s": stats["solve_seconds"],
                 "n_domains": stats["n_domains"]},
         "profile_ms": {k: round(v["ms"], 3) for k, v in sorted(report.items(), key=lambda kv: -kv[1]["ms"])},

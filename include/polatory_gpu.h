@@ -204,6 +204,15 @@ int pgpu_interpolant_num_centers(const pgpu_interpolant* it, int64_t* mu, int64_
 int pgpu_interpolant_centers(const pgpu_interpolant* it, double* centers, double* grad_centers);
 int pgpu_interpolant_bbox(const pgpu_interpolant* it, double bbox[6]);
 int pgpu_interpolant_fit_stats(const pgpu_interpolant* it, pgpu_fit_stats* out);
+/* Interpolant::fit_incrementally (interpolant.hpp:115-150, interpolation/incremental_fitter.hpp:
+ * 46-183): fits a growing subset of the points (largest residuals first, thinned by the
+ * reference's distance filter) until every point is within the tolerance; the interpolant's
+ * centres are that subset. Gradient points: PGPU_NOT_IMPLEMENTED. */
+int pgpu_interpolant_fit_incrementally(pgpu_interpolant* it, const double* points, int64_t mu,
+                                       const double* grad_points, int64_t sigma,
+                                       const double* values, double tolerance,
+                                       double grad_tolerance, int max_iter, double accuracy,
+                                       double grad_accuracy);
 /* Interpolant::save / Interpolant::load (interpolant.hpp:218, POLATORY_IMPLEMENT_LOAD_SAVE,
  * with Write/Read<Interpolant> at interpolant.hpp:345-367): the reference's binary file format,
  * so models move between the two implementations. Errors: "cannot open file '<name>'". */

@@ -217,6 +217,15 @@ class Interpolant:
     def set_precision(self, precision: int):
         check(lib.pgpu_interpolant_set_precision(self._h, precision))
 
+    def fit_incrementally(self, points, values, tolerance, max_iter=100, accuracy=INF):
+        """Interpolant::fit_incrementally: the centres become the subset of the points the
+        incremental fitter needed (incremental_fitter.hpp:46-183)."""
+        pts = as_points(points)
+        vals = np.ascontiguousarray(np.asarray(values, dtype=np.float64).reshape(-1))
+        check(lib.pgpu_interpolant_fit_incrementally(
+            self._h, ptr(pts), pts.shape[0], None, 0, ptr(vals), float(tolerance), INF,
+            int(max_iter), float(accuracy), INF))
+
     def save(self, filename: str) -> None:
         """Interpolant::save: the reference's binary format."""
         check(lib.pgpu_interpolant_save(self._h, str(filename).encode()))

@@ -3,6 +3,8 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <numeric>
+#include <algorithm>
 #include <string>
 #include <unordered_map>
 
@@ -966,5 +968,186 @@ int pgpu_interpolant_load(const char* filename, pgpu_interpolant** out) {
     while ((got = std::fread(buf, 1, sizeof(buf), f)) > 0) bytes.insert(bytes.end(), buf, buf + got);
     std::fclose(f);
     *out = deserialize(bytes).release();
+  });
+}
+
+// ---- incremental fit (interpolation/incremental_fitter.hpp:46-183) --------------------------
+
+namespace {
+
+// DistanceFilter::filter (point_cloud/distance_filter.hpp:31-65): walking the indices in order,
+// a point not yet removed removes every other point of the full set within the distance. A
+// uniform grid with the distance as its cell size stands in for the kd-tree radius search.
+std::vector<char> distance_filter_keep(const std::vector<double>& pts, double distance,
+                                       const std::vector<Index>& indices) {
+  const Index n = static_cast<Index>(pts.size() / 3);
+  std::vector<char> removed(n, 0), keep(n, 0);
+  if (n == 0) return keep;
+  double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (Index i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) {
+      mn[k] = std::min(mn[k], pts[3 * i + k]);
+      mx[k] = std::max(mx[k], pts[3 * i + k]);
+    }
+  int64_t dims[3];
+  for (int k = 0; k < 3; ++k)
+    dims[k] = std::max<int64_t>(1, std::min<int64_t>(1 << 10, static_cast<int64_t>((mx[k] - mn[k]) / distance) + 1));
+  auto cell_of = [&](Index i, int k) {
+    return std::min<int64_t>(dims[k] - 1, static_cast<int64_t>((pts[3 * i + k] - mn[k]) / distance));
+  };
+  std::unordered_map<int64_t, std::vector<Index>> grid;
+  auto key = [&](int64_t x, int64_t y, int64_t z) { return (x * dims[1] + y) * dims[2] + z; };
+  for (Index i = 0; i < n; ++i) grid[key(cell_of(i, 0), cell_of(i, 1), cell_of(i, 2))].push_back(i);
+  const double d2max = distance * distance;
+  for (Index i : indices) {
+    if (removed[i]) continue;
+    const int64_t cx = cell_of(i, 0), cy = cell_of(i, 1), cz = cell_of(i, 2);
+    for (int64_t x = std::max<int64_t>(0, cx - 1); x <= std::min(dims[0] - 1, cx + 1); ++x)
+      for (int64_t y = std::max<int64_t>(0, cy - 1); y <= std::min(dims[1] - 1, cy + 1); ++y)
+        for (int64_t z = std::max<int64_t>(0, cz - 1); z <= std::min(dims[2] - 1, cz + 1); ++z) {
+          auto f = grid.find(key(x, y, z));
+          if (f == grid.end()) continue;
+          for (Index j : f->second) {
+            if (j == i) continue;
+            double d2 = 0;
+            for (int k = 0; k < 3; ++k) {
+              const double d = pts[3 * i + k] - pts[3 * j + k];
+              d2 += d * d;
+            }
+            if (d2 <= d2max) removed[j] = 1;
+          }
+        }
+  }
+  for (Index i : indices)
+    if (!removed[i]) keep[i] = 1;
+  return keep;
+}
+
+}  // namespace
+
+int pgpu_interpolant_fit_incrementally(pgpu_interpolant* it, const double* points, int64_t mu_full,
+                                       const double* grad_points, int64_t sigma_full,
+                                       const double* values, double tolerance,
+                                       double grad_tolerance, int max_iter, double accuracy,
+                                       double grad_accuracy) {
+  return guarded([&] {
+    check_ptr(it, "interpolant");
+    check_fit_args(it->model, mu_full, sigma_full, tolerance, grad_tolerance, max_iter, accuracy,
+                   grad_accuracy);
+    if (sigma_full > 0) throw Error(PGPU_NOT_IMPLEMENTED, "gradient data points are not supported yet");
+    if (mu_full > 0) check_ptr(points, "points");
+    check_ptr(values, "values");
+    const int l = it->model.l();
+    const auto pts = host_copy(points, 3 * mu_full);
+    const auto vals = host_copy(values, mu_full);
+    const Bbox3 bbox = Bbox3::from_host_points(pts.data(), mu_full);
+    const bool verbose_out = std::getenv("PGPU_VERBOSE") != nullptr;
+    constexpr double kMinDistance = 1.0842021724855044e-19;  // DistanceFilter::kMinDistance
+    double diag = 0;
+    for (int k = 0; k < 3; ++k) diag += (bbox.max[k] - bbox.min[k]) * (bbox.max[k] - bbox.min[k]);
+    double filtering_distance = std::max(std::sqrt(diag), kMinDistance);
+
+    std::vector<Index> centers;
+    std::vector<double> weights(l, 0.0);
+    std::vector<char> is_center(mu_full, 0);
+    it->fitted = false;
+    while (true) {
+      const Index mu = static_cast<Index>(centers.size());
+      std::vector<double> cp(3 * mu), cv(mu);
+      for (Index i = 0; i < mu; ++i) {
+        for (int k = 0; k < 3; ++k) cp[3 * i + k] = pts[3 * centers[i] + k];
+        cv[i] = vals[centers[i]];
+      }
+      if (verbose_out) std::printf("Number of RBF centers: %ld / %ld\n", static_cast<long>(mu), static_cast<long>(mu_full));
+      if (mu >= l && mu > 0) {
+        FitRequest req;
+        req.model = &it->model;
+        req.points_host = cp.data();
+        req.mu = mu;
+        req.values_host = cv.data();
+        req.tolerance = tolerance;
+        req.grad_tolerance = grad_tolerance;
+        req.max_iter = max_iter;
+        req.accuracy = accuracy;
+        req.grad_accuracy = grad_accuracy;
+        req.initial_weights = weights.data();
+        req.precision = it->precision;
+        req.verbose = verbose_out;
+        weights = fit(req).weights;
+      }
+      if (mu == mu_full) break;
+
+      // Residuals at the remaining points, sorted ascending (stable in index order).
+      std::vector<Index> rest;
+      for (Index i = 0; i < mu_full; ++i)
+        if (!is_center[i]) rest.push_back(i);
+      const Index m = static_cast<Index>(rest.size());
+      std::vector<double> rp(3 * m), fitv(m, 0.0);
+      for (Index i = 0; i < m; ++i)
+        for (int k = 0; k < 3; ++k) rp[3 * i + k] = pts[3 * rest[i] + k];
+      if (mu > 0) {
+        DevBuf<double> dc, dw, dq, dout;
+        dc.upload(cp);
+        dw.upload(weights);
+        dq.upload(rp);
+        dout.resize(m);
+        EvaluateRequest er;
+        er.model = &it->model;
+        er.centers_dev = dc.data();
+        er.mu = mu;
+        er.weights_dev = dw.data();
+        er.bbox = bbox;
+        er.points_dev = dq.data();
+        er.m = m;
+        er.accuracy = accuracy;
+        er.precision = it->precision;
+        er.out_dev = dout.data();
+        evaluate(er);
+        fitv = dout.to_host();
+      }
+      std::vector<double> res(m);
+      for (Index i = 0; i < m; ++i) res[i] = std::fabs(vals[rest[i]] - fitv[i]);
+      std::vector<Index> order(m);
+      std::iota(order.begin(), order.end(), Index{0});
+      std::stable_sort(order.begin(), order.end(), [&](Index a, Index b) { return res[a] < res[b]; });
+      Index n_need = 0;
+      for (Index i = 0; i < m; ++i)
+        if (res[i] >= tolerance) ++n_need;
+      if (verbose_out) std::printf("Number of points to fit: %ld\n", static_cast<long>(n_need));
+      if (n_need == 0) break;
+
+      // Append the points with the largest residuals that survive the distance filter.
+      std::vector<Index> indices(centers);
+      for (Index k = m - 1; k >= 0; --k) indices.push_back(rest[order[k]]);
+      const auto keep = distance_filter_keep(pts, filtering_distance, indices);
+      for (Index k = m - 1; k >= m - n_need; --k) {
+        const Index i = rest[order[k]];
+        if (keep[i]) {
+          centers.push_back(i);
+          is_center[i] = 1;
+        }
+      }
+      // Warm start: the old weights, zeros for the new centres, the polynomial part kept.
+      const Index mu_new = static_cast<Index>(centers.size());
+      std::vector<double> w(mu_new + l, 0.0);
+      for (Index i = 0; i < mu; ++i) w[i] = weights[i];
+      for (int k = 0; k < l; ++k) w[mu_new + k] = weights[weights.size() - l + k];
+      weights = std::move(w);
+      filtering_distance = std::max(0.5 * filtering_distance, kMinDistance);
+    }
+
+    const Index mu = static_cast<Index>(centers.size());
+    std::vector<double> cp(3 * mu);
+    for (Index i = 0; i < mu; ++i)
+      for (int k = 0; k < 3; ++k) cp[3 * i + k] = pts[3 * centers[i] + k];
+    it->weights.upload(weights);
+    it->centers.upload(cp);
+    it->grad_centers.resize(0);
+    it->centers_host = std::move(cp);
+    it->mu = mu;
+    it->sigma = 0;
+    it->bbox = Bbox3::from_host_points(it->centers_host.data(), mu);
+    it->fitted = true;
+    it->eval_ready = false;
   });
 }

@@ -165,3 +165,22 @@ def test_fit_mixed_fmm_hybrid_residual(kind):
     idx = g.choice(n, 4000, replace=False)
     fit_vals = oracle.direct_evaluate(model, pts, w, pts[idx]) + model.nugget * w[idx]
     assert np.max(np.abs(fit_vals - vals[idx])) <= tol
+
+
+def test_fit_incrementally():
+    # interpolation/incremental_fitter.hpp:46-183: the centres are a subset of the points and
+    # every point (centre or not) is within the tolerance, recomputed by the oracle.
+    g = np.random.Generator(np.random.PCG64(26))
+    pts = g.random((6000, 3))
+    vals = 0.2 * workloads.f_c1(pts)
+    model = pg.Model(pg.Biharmonic3D([1.0]), 1)
+    it = pg.Interpolant(model)
+    tol = 1e-3
+    it.fit_incrementally(pts, vals, tol)
+    c = it.centers
+    assert 0 < c.shape[0] <= pts.shape[0]
+    rows = {tuple(p) for p in pts}
+    assert all(tuple(p) in rows for p in c)
+    w = it.weights
+    fit_vals = oracle.direct_evaluate(model, c, w, pts)
+    assert np.max(np.abs(fit_vals - vals)) <= tol
