@@ -213,6 +213,13 @@ int pgpu_interpolant_fit_incrementally(pgpu_interpolant* it, const double* point
                                        const double* values, double tolerance,
                                        double grad_tolerance, int max_iter, double accuracy,
                                        double grad_accuracy);
+/* Interpolant::fit_inequality (interpolant.hpp:151-191, interpolation/inequality_fitter.hpp:
+ * 43-187): values, values_lb, values_ub of n entries each, NaN where absent; the centres become
+ * the equality points plus the active bounds. */
+int pgpu_interpolant_fit_inequality(pgpu_interpolant* it, const double* points, int64_t n,
+                                    const double* values, const double* values_lb,
+                                    const double* values_ub, double tolerance, int max_iter,
+                                    double accuracy);
 /* Interpolant::save / Interpolant::load (interpolant.hpp:218, POLATORY_IMPLEMENT_LOAD_SAVE,
  * with Write/Read<Interpolant> at interpolant.hpp:345-367): the reference's binary file format,
  * so models move between the two implementations. Errors: "cannot open file '<name>'". */

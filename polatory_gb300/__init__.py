@@ -226,6 +226,17 @@ class Interpolant:
             self._h, ptr(pts), pts.shape[0], None, 0, ptr(vals), float(tolerance), INF,
             int(max_iter), float(accuracy), INF))
 
+    def fit_inequality(self, points, values, values_lb, values_ub, tolerance, max_iter=100,
+                       accuracy=INF):
+        """Interpolant::fit_inequality: NaN marks an absent value or bound
+        (inequality_fitter.hpp:43-187)."""
+        pts = as_points(points)
+        arrs = [np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1))
+                for a in (values, values_lb, values_ub)]
+        check(lib.pgpu_interpolant_fit_inequality(
+            self._h, ptr(pts), pts.shape[0], ptr(arrs[0]), ptr(arrs[1]), ptr(arrs[2]),
+            float(tolerance), int(max_iter), float(accuracy)))
+
     def save(self, filename: str) -> None:
         """Interpolant::save: the reference's binary format."""
         check(lib.pgpu_interpolant_save(self._h, str(filename).encode()))

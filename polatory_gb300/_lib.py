@@ -131,6 +131,8 @@ def _load():
         "pgpu_interpolant_fit_stats": ([P, C.POINTER(PgpuFitStats)], C.c_int),
         "pgpu_interpolant_fit_incrementally": ([P, P, I64, P, I64, P, C.c_double, C.c_double,
                                                 C.c_int, C.c_double, C.c_double], C.c_int),
+        "pgpu_interpolant_fit_inequality": ([P, P, I64, P, P, P, C.c_double, C.c_int,
+                                             C.c_double], C.c_int),
         "pgpu_interpolant_save": ([P, C.c_char_p], C.c_int),
         "pgpu_interpolant_load": ([C.c_char_p, C.POINTER(P)], C.c_int),
         "pgpu_fit_batch": ([C.POINTER(PgpuModel), C.c_int, C.POINTER(PgpuFitProblem), I64,

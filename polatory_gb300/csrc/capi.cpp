@@ -5,6 +5,7 @@
 #include <memory>
 #include <numeric>
 #include <algorithm>
+#include <set>
 #include <string>
 #include <unordered_map>
 
@@ -1147,6 +1148,179 @@ int pgpu_interpolant_fit_incrementally(pgpu_interpolant* it, const double* point
     it->mu = mu;
     it->sigma = 0;
     it->bbox = Bbox3::from_host_points(it->centers_host.data(), mu);
+    it->fitted = true;
+    it->eval_ready = false;
+  });
+}
+
+// ---- inequality fit (interpolation/inequality_fitter.hpp:43-187) ---------------------------
+// values / values_lb / values_ub are NaN where absent. The active-set loop of the reference:
+// centres are the equality points plus the active bounds; each round fits them (warm start),
+// evaluates at the inequality points, activates violated bounds that survive the distance
+// filter (points ordered by their violation, largest first), and deactivates bounds whose
+// weight has the wrong sign; it stops when the active set no longer changes.
+
+int pgpu_interpolant_fit_inequality(pgpu_interpolant* it, const double* points, int64_t n,
+                                    const double* values, const double* values_lb,
+                                    const double* values_ub, double tolerance, int max_iter,
+                                    double accuracy) {
+  return guarded([&] {
+    check_ptr(it, "interpolant");
+    check_fit_args(it->model, n, 0, tolerance, INFINITY, max_iter, accuracy, INFINITY);
+    check_ptr(points, "points");
+    check_ptr(values, "values");
+    check_ptr(values_lb, "values_lb");
+    check_ptr(values_ub, "values_ub");
+    const int l = it->model.l();
+    const auto pts = host_copy(points, 3 * n);
+    const auto vals = host_copy(values, n);
+    const auto lb = host_copy(values_lb, n);
+    const auto ub = host_copy(values_ub, n);
+    const Bbox3 bbox = Bbox3::from_host_points(pts.data(), n);
+    const bool verbose_out = std::getenv("PGPU_VERBOSE") != nullptr;
+    constexpr double kMinDistance = 1.0842021724855044e-19;
+    double diag = 0;
+    for (int k = 0; k < 3; ++k) diag += (bbox.max[k] - bbox.min[k]) * (bbox.max[k] - bbox.min[k]);
+    double filtering_distance = std::max(std::sqrt(diag), kMinDistance);
+
+    std::vector<Index> eq, ineq;
+    for (Index i = 0; i < n; ++i) {
+      if (!std::isnan(vals[i])) eq.push_back(i);
+      if (!std::isnan(lb[i]) || !std::isnan(ub[i])) ineq.push_back(i);
+    }
+    const Index n_ineq = static_cast<Index>(ineq.size());
+    std::vector<double> ineq_pts(3 * n_ineq);
+    for (Index i = 0; i < n_ineq; ++i)
+      for (int k = 0; k < 3; ++k) ineq_pts[3 * i + k] = pts[3 * ineq[i] + k];
+
+    std::vector<double> weights(n + l, 0.0);
+    std::set<Index> active_lb, active_ub;
+    std::vector<Index> centers;
+    std::vector<double> center_weights;
+    it->fitted = false;
+    while (true) {
+      if (verbose_out)
+        std::printf("Active lower bounds: %zu, active upper bounds: %zu\n", active_lb.size(),
+                    active_ub.size());
+      centers = eq;
+      std::set_union(active_lb.begin(), active_lb.end(), active_ub.begin(), active_ub.end(),
+                     std::back_inserter(centers));
+      const Index nc = static_cast<Index>(centers.size());
+      std::vector<double> fitv(n_ineq, 0.0);
+      if (nc >= l && nc > 0) {
+        std::vector<double> cp(3 * nc), cv(nc);
+        for (Index i = 0; i < nc; ++i) {
+          const Index idx = centers[i];
+          for (int k = 0; k < 3; ++k) cp[3 * i + k] = pts[3 * idx + k];
+          cv[i] = i < static_cast<Index>(eq.size()) ? vals[idx]
+                                                    : (active_lb.count(idx) ? lb[idx] : ub[idx]);
+        }
+        center_weights.assign(nc + l, 0.0);
+        for (Index i = 0; i < nc; ++i) center_weights[i] = weights[centers[i]];
+        for (int k = 0; k < l; ++k) center_weights[nc + k] = weights[n + k];
+        FitRequest req;
+        req.model = &it->model;
+        req.points_host = cp.data();
+        req.mu = nc;
+        req.values_host = cv.data();
+        req.tolerance = tolerance;
+        req.grad_tolerance = INFINITY;
+        req.max_iter = max_iter;
+        req.accuracy = accuracy;
+        req.grad_accuracy = INFINITY;
+        req.initial_weights = center_weights.data();
+        req.precision = it->precision;
+        req.verbose = verbose_out;
+        center_weights = fit(req).weights;
+        for (Index i = 0; i < nc; ++i) weights[centers[i]] = center_weights[i];
+        for (int k = 0; k < l; ++k) weights[n + k] = center_weights[nc + k];
+        if (n_ineq > 0) {
+          DevBuf<double> dc, dw, dq, dout;
+          dc.upload(cp);
+          dw.upload(center_weights);
+          dq.upload(ineq_pts);
+          dout.resize(n_ineq);
+          EvaluateRequest er;
+          er.model = &it->model;
+          er.centers_dev = dc.data();
+          er.mu = nc;
+          er.weights_dev = dw.data();
+          er.bbox = bbox;
+          er.points_dev = dq.data();
+          er.m = n_ineq;
+          er.accuracy = accuracy;
+          er.precision = it->precision;
+          er.out_dev = dout.data();
+          evaluate(er);
+          fitv = dout.to_host();
+        }
+      } else {
+        center_weights.assign(l, 0.0);
+      }
+
+      // Violations at the points that are not centres, largest first, through the filter.
+      std::vector<char> is_center(n, 0);
+      for (Index c : centers) is_center[c] = 1;
+      std::vector<double> viol(n, 0.0);
+      for (Index i = 0; i < n_ineq; ++i) {
+        const Index idx = ineq[i];
+        const double lr = std::isnan(lb[idx]) ? 0.0 : std::max(lb[idx] - fitv[i], 0.0);
+        const double ur = std::isnan(ub[idx]) ? 0.0 : std::max(fitv[i] - ub[idx], 0.0);
+        viol[idx] = std::max(lr, ur);
+      }
+      std::vector<Index> order;
+      for (Index i = 0; i < n; ++i)
+        if (!is_center[i]) order.push_back(i);
+      std::stable_sort(order.begin(), order.end(), [&](Index a, Index b) { return viol[a] > viol[b]; });
+      const auto keep = distance_filter_keep(pts, filtering_distance, order);
+
+      bool changed = false;
+      for (Index i = 0; i < n_ineq; ++i) {
+        const Index idx = ineq[i];
+        if (!std::isnan(lb[idx])) {
+          if (active_lb.count(idx)) {
+            if (weights[idx] <= 0.0) {
+              active_lb.erase(idx);
+              changed = true;
+            }
+          } else if (fitv[i] < lb[idx] - tolerance) {
+            if (keep[idx]) {
+              active_lb.insert(idx);
+              weights[idx] = 0.0;
+            }
+            changed = true;
+          }
+        }
+        if (!std::isnan(ub[idx])) {
+          if (active_ub.count(idx)) {
+            if (weights[idx] >= 0.0) {
+              active_ub.erase(idx);
+              changed = true;
+            }
+          } else if (fitv[i] > ub[idx] + tolerance) {
+            if (keep[idx]) {
+              active_ub.insert(idx);
+              weights[idx] = 0.0;
+            }
+            changed = true;
+          }
+        }
+      }
+      if (!changed) break;
+      filtering_distance = std::max(0.5 * filtering_distance, kMinDistance);
+    }
+
+    const Index nc = static_cast<Index>(centers.size());
+    std::vector<double> cp(3 * nc);
+    for (Index i = 0; i < nc; ++i)
+      for (int k = 0; k < 3; ++k) cp[3 * i + k] = pts[3 * centers[i] + k];
+    it->weights.upload(center_weights);
+    it->centers.upload(cp);
+    it->grad_centers.resize(0);
+    it->centers_host = std::move(cp);
+    it->mu = nc;
+    it->sigma = 0;
+    it->bbox = Bbox3::from_host_points(it->centers_host.data(), nc);
     it->fitted = true;
     it->eval_ready = false;
   });

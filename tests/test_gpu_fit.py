@@ -184,3 +184,30 @@ def test_fit_incrementally():
     w = it.weights
     fit_vals = oracle.direct_evaluate(model, c, w, pts)
     assert np.max(np.abs(fit_vals - vals)) <= tol
+
+
+def test_fit_inequality():
+    # interpolation/inequality_fitter.hpp:43-187: equality points are interpolated, bounds hold
+    # within the tolerance at every bounded point (recomputed by the oracle).
+    g = np.random.Generator(np.random.PCG64(27))
+    n = 3000
+    pts = g.random((n, 3))
+    f = 0.2 * workloads.f_c1(pts)
+    nan = np.full(n, np.nan)
+    values, lb, ub = nan.copy(), nan.copy(), nan.copy()
+    eq = np.arange(0, n, 10)
+    values[eq] = f[eq]
+    low = np.arange(1, n, 3)
+    lb[low] = f[low] - 0.02
+    high = np.arange(2, n, 3)
+    ub[high] = f[high] + 0.02
+    model = pg.Model(pg.Biharmonic3D([1.0]), 1)
+    it = pg.Interpolant(model)
+    tol = 1e-4
+    it.fit_inequality(pts, values, lb, ub, tol)
+    c = it.centers
+    w = it.weights
+    fit = oracle.direct_evaluate(model, c, w, pts)
+    assert np.max(np.abs(fit[eq] - values[eq])) <= tol
+    assert np.all(fit[low] >= lb[low] - 2 * tol)
+    assert np.all(fit[high] <= ub[high] + 2 * tol)
