@@ -26,6 +26,7 @@ namespace pgpu {
 namespace {
 
 constexpr int NB = 32;
+constexpr int kMaxL = 10;  // polynomial basis size at degree 2
 
 template <class T>
 __device__ __forceinline__ T rbf_value_rt(int kind, T r2, const KParams<T>& kp) {
@@ -119,29 +120,55 @@ __global__ void assemble_kernel(KParams<T> kp, const P4<T>* __restrict__ frame,
   if (bi * NB >= ld) return;
   T* m = mats + mat_off[d];
   const Index* dp = pts + pt_off[d] + l;  // non-polynomial points
-  const int r = bi * NB + (threadIdx.x & 31);  // lanes walk down a column (coalesced)
-  for (int cc = threadIdx.x >> 5; cc < NB; cc += blockDim.x >> 5) {
+  // The tile's 32 rows and 32 columns (positions, Lagrange values, u, v) staged once.
+  __shared__ P4<T> s_xr[NB], s_xc[NB];
+  __shared__ double s_lr[NB][kMaxL], s_ur[NB][kMaxL], s_lc[NB][kMaxL], s_uc[NB][kMaxL],
+      s_vc[NB][kMaxL];
+  const int t = threadIdx.x;
+  if (t < NB) {
+    const int r = bi * NB + t;
+    if (r < n) {
+      const Index g = dp[r];
+      s_xr[t] = frame[g];
+      if (last)
+        for (int k = 0; k < l; ++k) {
+          s_lr[t][k] = lag[g * l + k];
+          s_ur[t][k] = u[g * l + k];
+        }
+    }
+  } else if (t < 2 * NB) {
+    const int c = bj * NB + (t - NB);
+    if (c < n) {
+      const Index g = dp[c];
+      s_xc[t - NB] = frame[g];
+      if (last)
+        for (int k = 0; k < l; ++k) {
+          s_lc[t - NB][k] = lag[g * l + k];
+          s_uc[t - NB][k] = u[g * l + k];
+          s_vc[t - NB][k] = v[g * l + k];
+        }
+    }
+  }
+  __syncthreads();
+  const int rr = t & 31;
+  const int r = bi * NB + rr;  // lanes walk down a column (coalesced)
+  for (int cc = t >> 5; cc < NB; cc += blockDim.x >> 5) {
     const int c = bj * NB + cc;
     T* dst = m + r + static_cast<Index>(c) * ld;
     if (r >= n || c >= n) {
       *dst = (r == c) ? T(1) : T(0);
       continue;
     }
-    const Index gr = dp[r], gc = dp[c];
-    P4<T> xr = frame[gr], xc = frame[gc];
+    const P4<T> xr = s_xr[rr], xc = s_xc[cc];
     T dx = xr.x - xc.x, dy = xr.y - xc.y, dz = xr.z - xc.z;
     T val = rbf_value<KIND>(dx * dx + dy * dy + dz * dz, kp);
     double acc = first ? 0.0 : static_cast<double>(*dst);
     acc += static_cast<double>(val);
     if (last) {
       if (r == c) acc += nugget;
-      const double* lr = lag + gr * l;
-      const double* lc = lag + gc * l;
-      const double* ur = u + gr * l;
-      const double* uc = u + gc * l;
-      const double* vc = v + gc * l;
       double corr = 0;
-      for (int k = 0; k < l; ++k) corr += -ur[k] * lc[k] - lr[k] * uc[k] + lr[k] * vc[k];
+      for (int k = 0; k < l; ++k)
+        corr += -s_ur[rr][k] * s_lc[cc][k] - s_lr[rr][k] * s_uc[cc][k] + s_lr[rr][k] * s_vc[cc][k];
       acc += corr;
     }
     *dst = static_cast<T>(acc);
