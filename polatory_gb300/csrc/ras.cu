@@ -121,8 +121,10 @@ __global__ void assemble_kernel(KParams<T> kp, const P4<T>* __restrict__ frame,
   T* m = mats + mat_off[d];
   const Index* dp = pts + pt_off[d] + l;  // non-polynomial points
   // The tile's 32 rows and 32 columns (positions, Lagrange values, u, v) staged once.
+  // The polynomial correction runs in the matrix's type: FP32 matrices hold an FP32 kernel
+  // value, so FP64 correction terms (at 1/64 of the FP32 rate) would add cost, not accuracy.
   __shared__ P4<T> s_xr[NB], s_xc[NB];
-  __shared__ double s_lr[NB][kMaxL], s_ur[NB][kMaxL], s_lc[NB][kMaxL], s_uc[NB][kMaxL],
+  __shared__ T s_lr[NB][kMaxL], s_ur[NB][kMaxL], s_lc[NB][kMaxL], s_uc[NB][kMaxL],
       s_vc[NB][kMaxL];
   const int t = threadIdx.x;
   if (t < NB) {
@@ -132,8 +134,8 @@ __global__ void assemble_kernel(KParams<T> kp, const P4<T>* __restrict__ frame,
       s_xr[t] = frame[g];
       if (last)
         for (int k = 0; k < l; ++k) {
-          s_lr[t][k] = lag[g * l + k];
-          s_ur[t][k] = u[g * l + k];
+          s_lr[t][k] = static_cast<T>(lag[g * l + k]);
+          s_ur[t][k] = static_cast<T>(u[g * l + k]);
         }
     }
   } else if (t < 2 * NB) {
@@ -143,9 +145,9 @@ __global__ void assemble_kernel(KParams<T> kp, const P4<T>* __restrict__ frame,
       s_xc[t - NB] = frame[g];
       if (last)
         for (int k = 0; k < l; ++k) {
-          s_lc[t - NB][k] = lag[g * l + k];
-          s_uc[t - NB][k] = u[g * l + k];
-          s_vc[t - NB][k] = v[g * l + k];
+          s_lc[t - NB][k] = static_cast<T>(lag[g * l + k]);
+          s_uc[t - NB][k] = static_cast<T>(u[g * l + k]);
+          s_vc[t - NB][k] = static_cast<T>(v[g * l + k]);
         }
     }
   }
@@ -162,16 +164,16 @@ __global__ void assemble_kernel(KParams<T> kp, const P4<T>* __restrict__ frame,
     const P4<T> xr = s_xr[rr], xc = s_xc[cc];
     T dx = xr.x - xc.x, dy = xr.y - xc.y, dz = xr.z - xc.z;
     T val = rbf_value<KIND>(dx * dx + dy * dy + dz * dz, kp);
-    double acc = first ? 0.0 : static_cast<double>(*dst);
-    acc += static_cast<double>(val);
+    T acc = first ? T(0) : *dst;
+    acc += val;
     if (last) {
-      if (r == c) acc += nugget;
-      double corr = 0;
+      if (r == c) acc += static_cast<T>(nugget);
+      T corr = 0;
       for (int k = 0; k < l; ++k)
         corr += -s_ur[rr][k] * s_lc[cc][k] - s_lr[rr][k] * s_uc[cc][k] + s_lr[rr][k] * s_vc[cc][k];
       acc += corr;
     }
-    *dst = static_cast<T>(acc);
+    *dst = acc;
   }
 }
 
