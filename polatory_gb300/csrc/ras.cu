@@ -707,23 +707,45 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
       for (int level = n_levels_ - 1; level >= 1; --level) {
         std::vector<Index> no_grad;
         const double t0 = wall_seconds();
-        DomainDivider divider(div_points, nullptr, point_idcs_[level], no_grad, poly_idcs_);
-        const double t1 = wall_seconds();
-        {
-          std::lock_guard<std::mutex> lk(div_mu);
-          level_domains[level] = std::move(divider.domains());
-          published = level;
-        }
-        div_cv.notify_all();
         double finest = std::log(static_cast<double>(mu_)) / std::log(kFineToCoarseRatio);
         double coarsest = std::log(static_cast<double>(kNCoarsestPoints)) / std::log(kFineToCoarseRatio);
         Index n_coarse = static_cast<Index>(std::pow(
             kFineToCoarseRatio, coarsest + (level - 1) * (finest - coarsest) / (n_levels_ - 1)));
-        auto coarse = divider.choose_coarse_points(n_coarse).first;
+        // The coarse points of this level (the next level's point set) are chosen on a second
+        // thread while this one divides the level; each takes half of the host threads.
+        std::vector<Index> coarse;
+        std::exception_ptr coarse_error;
+        const int half = std::max(1, omp_threads / 2);
+        std::thread coarse_thread([&] {
+          omp_set_num_threads(half);
+          try {
+            coarse = DomainDivider::choose_coarse_points(div_points, nullptr, point_idcs_[level],
+                                                         no_grad, poly_idcs_, n_coarse)
+                         .first;
+          } catch (...) {
+            coarse_error = std::current_exception();
+          }
+        });
+        omp_set_num_threads(std::max(1, omp_threads - half));
+        double t1 = 0;
+        try {
+          DomainDivider divider(div_points, nullptr, point_idcs_[level], no_grad, poly_idcs_);
+          t1 = wall_seconds();
+          std::lock_guard<std::mutex> lk(div_mu);
+          level_domains[level] = std::move(divider.domains());
+          published = level;
+        } catch (...) {
+          coarse_thread.join();
+          throw;
+        }
+        div_cv.notify_all();
+        coarse_thread.join();
+        omp_set_num_threads(omp_threads);
+        if (coarse_error) std::rethrow_exception(coarse_error);
         if (verbose())
-          std::printf("ras level %d: %zu points, %zu domains, divide %.3f s, coarse points %.3f s\n",
+          std::printf("ras level %d: %zu points, %zu domains, divide %.3f s, divide + coarse points %.3f s\n",
                       level, point_idcs_[level].size(), level_domains[level].size(), t1 - t0,
-                      wall_seconds() - t1);
+                      wall_seconds() - t0);
         std::lock_guard<std::mutex> lk(div_mu);
         point_idcs_[level - 1] = std::move(coarse);
       }

@@ -533,6 +533,14 @@ DomainDivider::DomainDivider(const double* points, const double* grad_points,
 
 std::pair<std::vector<Index>, std::vector<Index>> DomainDivider::choose_coarse_points(
     Index n_coarse) const {
+  return choose_coarse_points(points_, grad_points_, point_idcs_, grad_point_idcs_,
+                              poly_point_idcs_, n_coarse);
+}
+
+std::pair<std::vector<Index>, std::vector<Index>> DomainDivider::choose_coarse_points(
+    const double* points_, const double* grad_points_, const std::vector<Index>& point_idcs_,
+    const std::vector<Index>& grad_point_idcs_, const std::vector<Index>& poly_point_idcs_,
+    Index n_coarse) {
   // The reference pops clusters from a priority queue ordered by (level ascending, bbox volume
   // descending), splits each at its median and keeps the centres (domain_divider.hpp:54-125).
   // That order visits the clusters level by level, so here every level is split at once, in

@@ -37,6 +37,13 @@ class DomainDivider {
 
   std::pair<std::vector<Index>, std::vector<Index>> choose_coarse_points(Index n_coarse) const;
 
+  // The coarse-point selection alone: it reads only the point sets, so it can run while the
+  // division of the same sets runs elsewhere.
+  static std::pair<std::vector<Index>, std::vector<Index>> choose_coarse_points(
+      const double* points, const double* grad_points, const std::vector<Index>& point_indices,
+      const std::vector<Index>& grad_point_indices,
+      const std::vector<Index>& poly_point_indices, Index n_coarse);
+
   std::vector<Domain>& domains() { return domains_; }
 
   static constexpr double kOverlapQuota = 0.5;
