@@ -498,9 +498,12 @@ int pgpu_interpolant_fit(pgpu_interpolant* it, const double* points, int64_t mu,
     if (sigma > 0) check_ptr(grad_points, "grad_points");
     check_ptr(values, "values");
     const int l = it->model.l();
+    const double t_in = wall_seconds();
     auto pts = host_copy(points, 3 * mu);
     auto gpts = host_copy(grad_points, 3 * sigma);
     auto vals = host_copy(values, mu + 3 * sigma);
+    if (std::getenv("PGPU_VERBOSE"))
+      std::printf("fit: inputs to host %.3f s\n", wall_seconds() - t_in);
 
     std::vector<double> init;
     if (initial != nullptr && initial->fitted) {

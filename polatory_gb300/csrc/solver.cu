@@ -337,7 +337,12 @@ FitResult fit_impl(const FitRequest& req) {
 
   DevBuf<double> pts;
   pts.upload(req.points_host, 3 * mu);
+  if (req.verbose) {
+    sync();
+    std::printf("fit: upload %.3f s\n", wall_seconds() - t0);
+  }
   const Bbox3 bbox = Bbox3::from_host_points(req.points_host, mu);
+  if (req.verbose) std::printf("fit: bbox %.3f s\n", wall_seconds() - t0);
 
   DevBuf<double> P, Q;
   if (l > 0) {
