@@ -42,16 +42,17 @@ def _headers_digest() -> str:
 
 def _compile(src: Path, obj: Path, cuda: Path, flags_key: str) -> str:
     stamp = obj.with_suffix(".stamp")
-    digest = hashlib.sha256(src.read_bytes()).hexdigest()[:16] + flags_key
-    if obj.exists() and stamp.exists() and stamp.read_text() == digest:
-        return f"cached {src.name}"
     common = ["-std=c++20", "-O3", f"-I{INCLUDE}", f"-I{CSRC}"]
     if src.suffix == ".cu":
         cmd = [str(cuda / "bin" / "nvcc"), *common, *ARCH, "-lineinfo", "--expt-relaxed-constexpr",
-               "-Xcompiler", "-fPIC,-fopenmp", "-c", str(src), "-o", str(obj)]
+               "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off", "-c", str(src), "-o", str(obj)]
     else:
-        cmd = ["g++", *common, "-fPIC", "-fopenmp", f"-I{cuda / 'include'}", "-c", str(src), "-o",
-               str(obj)]
+        cmd = ["g++", *common, "-fPIC", "-fopenmp", "-ffp-contract=off", f"-I{cuda / 'include'}",
+               "-c", str(src), "-o", str(obj)]
+    digest = (hashlib.sha256(src.read_bytes()).hexdigest()[:16] + flags_key +
+              hashlib.sha256(" ".join(cmd).encode()).hexdigest()[:8])
+    if obj.exists() and stamp.exists() and stamp.read_text() == digest:
+        return f"cached {src.name}"
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

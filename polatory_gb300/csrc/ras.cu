@@ -12,6 +12,7 @@
 #include <cmath>
 #include <condition_variable>
 #include <cstdio>
+#include <cstdlib>
 #include <exception>
 #include <mutex>
 #include <thread>
@@ -20,6 +21,7 @@
 #include "linalg.hpp"
 #include "profile.hpp"
 #include "ras.hpp"
+#include "ras_divide.hpp"
 
 namespace pgpu {
 
@@ -83,6 +85,18 @@ __global__ void lagrange_kernel(int degree, int l, const double* __restrict__ pt
     for (int r = 0; r < l; ++r) s += m[r] * coeffs[r * l + c];
     lag[i * l + c] = s;
   }
+}
+
+// A p for the division of an anisotropic model, rounded like the host restatement:
+// (a0 p0 + a1 p1) + a2 p2 per row.
+__global__ void transform_points_kernel(const double* __restrict__ pts, Index n, Mat3 a,
+                                        double* __restrict__ out) {
+  const Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double p0 = pts[3 * i], p1 = pts[3 * i + 1], p2 = pts[3 * i + 2];
+  for (int r = 0; r < 3; ++r)
+    out[3 * i + r] = __dadd_rn(__dadd_rn(__dmul_rn(a.a[3 * r], p0), __dmul_rn(a.a[3 * r + 1], p1)),
+                               __dmul_rn(a.a[3 * r + 2], p2));
 }
 
 template <class T>
@@ -679,9 +693,22 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
 
   // Points used for the geometric division: A-transformed when the model has one
   // anisotropic RBF (ras_preconditioner.hpp:108-119).
+  const bool aniso = model_.rbfs.size() == 1 && !model_.rbfs[0].aniso_is_identity();
+  auto n_coarse_of = [&](int level) {
+    const double finest = std::log(static_cast<double>(mu_)) / std::log(kFineToCoarseRatio);
+    const double coarsest = std::log(static_cast<double>(kNCoarsestPoints)) / std::log(kFineToCoarseRatio);
+    return static_cast<Index>(
+        std::pow(kFineToCoarseRatio, coarsest + (level - 1) * (finest - coarsest) / (n_levels_ - 1)));
+  };
+
+  // The levels are divided on the device (ras_divide.cu) unless PGPU_RAS_HOST_DIVIDE is set:
+  // then the host divides them (ras_host.cpp, finest first) on a helper thread and publishes
+  // each level's domains as soon as they exist, while this thread runs the device set-up of
+  // the levels already published.
+  const bool host_division = std::getenv("PGPU_RAS_HOST_DIVIDE") != nullptr;
   std::vector<double> a_points;
   const double* div_points = points_host;
-  if (model_.rbfs.size() == 1 && !model_.rbfs[0].aniso_is_identity()) {
+  if (host_division && aniso) {
     const double* a = model_.rbfs[0].a;
     a_points.resize(3 * mu_);
     for (Index i = 0; i < mu_; ++i) {
@@ -690,27 +717,20 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
     }
     div_points = a_points.data();
   }
-
-  // The host divides the levels (finest first) on a helper thread and publishes each level's
-  // domains as soon as they exist; meanwhile this thread runs the device set-up of the levels
-  // already published, so the GPU assembles and factors the finest level while the host picks
-  // its coarse points and divides the coarser levels.
   std::vector<std::vector<Domain>> level_domains(n_levels_);
   std::mutex div_mu;
   std::condition_variable div_cv;
   int published = n_levels_;  // levels >= published are available
   std::exception_ptr div_error;
   const int omp_threads = omp_get_max_threads();
-  std::thread divide_thread([&] {
+  std::thread divide_thread;
+  if (host_division) divide_thread = std::thread([&] {
     omp_set_num_threads(omp_threads);
     try {
       for (int level = n_levels_ - 1; level >= 1; --level) {
         std::vector<Index> no_grad;
         const double t0 = wall_seconds();
-        double finest = std::log(static_cast<double>(mu_)) / std::log(kFineToCoarseRatio);
-        double coarsest = std::log(static_cast<double>(kNCoarsestPoints)) / std::log(kFineToCoarseRatio);
-        Index n_coarse = static_cast<Index>(std::pow(
-            kFineToCoarseRatio, coarsest + (level - 1) * (finest - coarsest) / (n_levels_ - 1)));
+        const Index n_coarse = n_coarse_of(level);
         // The coarse points of this level (the next level's point set) are chosen on a second
         // thread while this one divides the level; each takes half of the host threads.
         std::vector<Index> coarse;
@@ -813,13 +833,39 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
     sync();
   }
 
-  for (int level = n_levels_ - 1; level >= 1; --level) {
-    wait_level(level);
-    fine_[level] = std::make_unique<DomainBatch<T>>();
-    build_batch(*fine_[level], level_domains[level]);
+  if (host_division) {
+    for (int level = n_levels_ - 1; level >= 1; --level) {
+      wait_level(level);
+      fine_[level] = std::make_unique<DomainBatch<T>>();
+      build_batch(*fine_[level], level_domains[level]);
+    }
+    divide_thread.join();
+    if (div_error) std::rethrow_exception(div_error);
+  } else if (n_levels_ > 1) {
+    DevBuf<double> a_dev;
+    const double* coords = points_dev;
+    if (aniso) {
+      Mat3 a;
+      for (int k = 0; k < 9; ++k) a.a[k] = model_.rbfs[0].a[k];
+      a_dev.resize(3 * mu_);
+      transform_points_kernel<<<blocks_for(mu_, 256), 256, 0, stream()>>>(points_dev, mu_, a, a_dev.data());
+      PGPU_LAUNCH_CHECK();
+      coords = a_dev.data();
+    }
+    DeviceDivider divider(coords, mu_, poly_idcs_);
+    for (int level = n_levels_ - 1; level >= 1; --level) {
+      const double t0 = verbose() ? (sync(), wall_seconds()) : 0.0;
+      divider.set_level(point_idcs_[level]);
+      LevelDomains ld;
+      divider.divide(ld);
+      point_idcs_[level - 1] = divider.choose_coarse_points(n_coarse_of(level));
+      if (verbose())
+        std::printf("ras level %d: %zu points, %zu domains, device divide + coarse points %.3f s\n",
+                    level, point_idcs_[level].size(), ld.sizes.size(), wall_seconds() - t0);
+      fine_[level] = std::make_unique<DomainBatch<T>>();
+      build_batch(*fine_[level], ld.sizes, std::move(ld.pts), std::move(ld.inner));
+    }
   }
-  divide_thread.join();
-  if (div_error) std::rethrow_exception(div_error);
   {
     Domain cd;
     cd.point_indices = point_idcs_[0];
@@ -908,17 +954,32 @@ Index RasPreconditioner<T>::n_domains() const {
 template <class T>
 template <class U>
 void RasPreconditioner<T>::build_batch(DomainBatch<U>& b, const std::vector<Domain>& domains) {
+  std::vector<Index> sizes, pts;
+  std::vector<char> inner;
+  for (const auto& dom : domains) {
+    sizes.push_back(dom.num_points());
+    pts.insert(pts.end(), dom.point_indices.begin(), dom.point_indices.end());
+    inner.insert(inner.end(), dom.inner_point.begin(), dom.inner_point.end());
+  }
+  DevBuf<Index> dpts;
+  DevBuf<char> dinner;
+  dpts.upload(pts);
+  dinner.upload(inner);
+  build_batch(b, sizes, std::move(dpts), std::move(dinner));
+}
+
+template <class T>
+template <class U>
+void RasPreconditioner<T>::build_batch(DomainBatch<U>& b, const std::vector<Index>& sizes,
+                                       DevBuf<Index>&& pts, DevBuf<char>&& inner) {
   const int l = l_;
-  b.n_dom = static_cast<Index>(domains.size());
+  b.n_dom = static_cast<Index>(sizes.size());
   std::vector<int> n(b.n_dom), ld(b.n_dom);
   std::vector<Index> mat_off(b.n_dom + 1), pt_off(b.n_dom + 1);
-  std::vector<Index> pts;
-  std::vector<char> inner;
   Index moff = 0, poff = 0;
   b.max_n = 0;
   for (Index d = 0; d < b.n_dom; ++d) {
-    const auto& dom = domains[d];
-    const int m = static_cast<int>(dom.point_indices.size());
+    const int m = static_cast<int>(sizes[d]);
     n[d] = std::max(m - l, 0);
     ld[d] = std::max(NB, ((n[d] + NB - 1) / NB) * NB);
     b.max_n = std::max(b.max_n, ld[d]);
@@ -928,9 +989,9 @@ void RasPreconditioner<T>::build_batch(DomainBatch<U>& b, const std::vector<Doma
     b.solve_bytes += static_cast<double>(n[d]) * n[d] * sizeof(U);  // two triangle sweeps
     pt_off[d] = poff;
     poff += m;
-    pts.insert(pts.end(), dom.point_indices.begin(), dom.point_indices.end());
-    inner.insert(inner.end(), dom.inner_point.begin(), dom.inner_point.end());
   }
+  if (static_cast<Index>(pts.size()) != poff || static_cast<Index>(inner.size()) != poff)
+    throw_runtime("domain point lists do not match the domain sizes");
   mat_off[b.n_dom] = moff;
   pt_off[b.n_dom] = poff;
   b.total_points = poff;
@@ -938,11 +999,8 @@ void RasPreconditioner<T>::build_batch(DomainBatch<U>& b, const std::vector<Doma
   b.ld.upload(ld);
   b.mat_off.upload(mat_off);
   b.pt_off.upload(pt_off);
-  b.pts.upload(pts);
-  b.inner.resize(inner.size());
-  if (!inner.empty())
-    PGPU_CUDA(cudaMemcpyAsync(b.inner.data(), inner.data(), inner.size(), cudaMemcpyHostToDevice,
-                              stream()));
+  b.pts = std::move(pts);
+  b.inner = std::move(inner);
   b.mats.resize(moff);
   b.info.resize(b.n_dom);
   b.info.zero();

@@ -55,6 +55,10 @@ class RasPreconditioner {
   void orthogonalize(double* weights, double* residuals);
   template <class U>
   void build_batch(DomainBatch<U>& b, const std::vector<Domain>& domains);
+  // The same from flattened device lists: sizes per domain, point indices and inner flags.
+  template <class U>
+  void build_batch(DomainBatch<U>& b, const std::vector<Index>& sizes, DevBuf<Index>&& pts,
+                   DevBuf<char>&& inner);
   Evaluator<T>& evaluator(int src_level, int trg_level);
 
   ModelDesc model_;

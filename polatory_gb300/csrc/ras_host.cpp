@@ -228,12 +228,8 @@ void divide_domain(const Geo& g, const Domain& d, Domain& left, Domain& right, b
 
   const Index n_points = mu + sigma;
   const Index n_mult = mu + 3 * sigma;
-  const double q = DomainDivider::kOverlapQuota * 1024.0 / static_cast<double>(n_mult);
-  const Index n_sub = static_cast<Index>(round_half_to_even((1.0 + q) / 2.0 * static_cast<double>(n_mult)));
-  const Index left_mult = n_mult - n_sub;
-  const Index right_mult = n_sub;
-  const Index mid_mult =
-      static_cast<Index>(round_half_to_even(static_cast<double>(left_mult + right_mult) / 2.0));
+  Index left_mult, mid_mult, right_mult;
+  overlap_split_sizes(n_mult, left_mult, mid_mult, right_mult);
 
   Index left_part, right_part, mid;
   if (sigma == 0) {
@@ -445,14 +441,7 @@ void split_segment(const Geo& g, std::vector<MixedPoint>& pts, const Segment& s,
       }
     }
   } else {
-    Index bestd = n;
-    for (Index i = 1; i < n; ++i) {
-      Index di = std::llabs(2 * i - n);
-      if (di < bestd || (di == bestd && i % 2 == 0)) {
-        mid = i;
-        bestd = di;
-      }
-    }
+    mid = cluster_split(n);
     if (mid > 0 && mid < n) {
       if (par)
         par_multi_select(g, pts.data() + s.b, n, less, {mid});
@@ -471,6 +460,23 @@ void split_segment(const Geo& g, std::vector<MixedPoint>& pts, const Segment& s,
 }  // namespace
 
 void set_parallel_split_min(Index n) { g_par_split_min = n; }
+
+void overlap_split_sizes(Index n, Index& left_part, Index& mid, Index& right_part) {
+  const double q = DomainDivider::kOverlapQuota * 1024.0 / static_cast<double>(n);
+  const Index n_sub = static_cast<Index>(round_half_to_even((1.0 + q) / 2.0 * static_cast<double>(n)));
+  left_part = n - n_sub;
+  right_part = n_sub;
+  mid = static_cast<Index>(round_half_to_even(static_cast<double>(left_part + right_part) / 2.0));
+}
+
+// The first i in [1, n) minimising |2 i - n|, a tie going to the even i (std::min_element over
+// domain_divider.hpp:82-88's comparator); 0 for n < 2. For odd n both neighbours of n / 2 tie.
+Index cluster_split(Index n) {
+  if (n < 2) return 0;
+  if (n % 2 == 0) return n / 2;
+  const Index a = (n - 1) / 2;
+  return a % 2 == 0 ? a : a + 1;
+}
 
 DomainDivider::DomainDivider(const double* points, const double* grad_points,
                              const std::vector<Index>& point_indices,
@@ -575,6 +581,8 @@ std::pair<std::vector<Index>, std::vector<Index>> DomainDivider::choose_coarse_p
 
   while (count < n_coarse && !cur.empty()) {
     const Index ns = static_cast<Index>(cur.size());
+    // Single-point clusters split into themselves: stop when no cluster can grow the count.
+    if (std::none_of(cur.begin(), cur.end(), [](const Segment& c) { return c.e - c.b >= 2; })) break;
     std::vector<Segment> left(ns), right(ns);
     if (ns < omp_get_max_threads()) {
       // Few clusters: split them one at a time, each data-parallel when huge.
@@ -583,11 +591,14 @@ std::pair<std::vector<Index>, std::vector<Index>> DomainDivider::choose_coarse_p
 #pragma omp parallel for schedule(dynamic, 1)
       for (Index s = 0; s < ns; ++s) split_segment(g, pts, cur[s], left[s], right[s]);
     }
-    // Accept the splits in the reference's order.
+    // Accept the splits in the reference's order (volume descending); clusters of equal volume
+    // in the order of their segments.
     std::vector<Index> order(ns);
     for (Index s = 0; s < ns; ++s) order[s] = s;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](Index a, Index b) { return cur[a].volume > cur[b].volume; });
+    std::sort(order.begin(), order.end(), [&](Index a, Index b) {
+      if (cur[a].volume != cur[b].volume) return cur[a].volume > cur[b].volume;
+      return cur[a].b < cur[b].b;
+    });
     std::vector<Segment> next;
     next.reserve(2 * ns);
     Index k = 0;
@@ -604,8 +615,14 @@ std::pair<std::vector<Index>, std::vector<Index>> DomainDivider::choose_coarse_p
     for (; k < ns; ++k) finals.push_back(cur[order[k]]);
     cur = std::move(next);
   }
+  // The centres in ascending index order after the polynomial points: a canonical order that
+  // does not depend on how the clusters were visited.
+  std::vector<Index> centers;
   for (const auto* v : {&finals, &cur})
-    for (const auto& s : *v) (s.center.grad ? grad_idcs : idcs).push_back(s.center.index);
+    for (const auto& s : *v) (s.center.grad ? grad_idcs : centers).push_back(s.center.index);
+  std::sort(centers.begin(), centers.end());
+  std::sort(grad_idcs.begin(), grad_idcs.end());
+  idcs.insert(idcs.end(), centers.begin(), centers.end());
   return {std::move(idcs), std::move(grad_idcs)};
 }
 

@@ -28,6 +28,14 @@ struct Domain {
 // selection); the tests lower it to cover that path on small inputs.
 void set_parallel_split_min(Index n);
 
+// Sizes of the two overlapping halves of a domain of n value points (domain_divider.hpp:
+// 199-213): in the domain's sorted order the left half takes positions [0, right_part), the
+// right half [left_part, n); positions below mid stay inner on the left, the rest on the right.
+void overlap_split_sizes(Index n, Index& left_part, Index& mid, Index& right_part);
+
+// Split position of a coarse-point cluster of n value points (domain_divider.hpp:82-88).
+Index cluster_split(Index n);
+
 class DomainDivider {
  public:
   DomainDivider(const double* points, const double* grad_points,
@@ -35,6 +43,7 @@ class DomainDivider {
                 const std::vector<Index>& grad_point_indices,
                 const std::vector<Index>& poly_point_indices);
 
+  // Coarse points: the polynomial points, then the cluster centres in ascending index order.
   std::pair<std::vector<Index>, std::vector<Index>> choose_coarse_points(Index n_coarse) const;
 
   // The coarse-point selection alone: it reads only the point sets, so it can run while the

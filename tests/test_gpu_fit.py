@@ -211,3 +211,36 @@ def test_fit_inequality():
     assert np.max(np.abs(fit[eq] - values[eq])) <= tol
     assert np.all(fit[low] >= lb[low] - 2 * tol)
     assert np.all(fit[high] <= ub[high] + 2 * tol)
+
+
+@pytest.mark.parametrize("kind", ["bh3_plain", "bh3_mixed", "cov_aniso"])
+def test_device_division_equals_host_division(monkeypatch, kind):
+    # The RAS levels divided on the device (domains, inner flags, coarse points) equal the host
+    # restatement's, so the fits agree bit for bit. 60k points: three levels.
+    g = np.random.Generator(np.random.PCG64(41))
+    pts = g.random((60000, 3))
+    vals = workloads.f_c1(pts)
+    if kind == "cov_aniso":
+        rbf = pg.CovExponential([1.0, 0.3])
+        rbf.anisotropy = np.array([[1.0, 0.2, 0.0], [0.0, 1.0, 0.0], [0.1, 0.0, 0.5]])
+        model = pg.Model(rbf, 0)
+        model.nugget = 1e-3
+    else:
+        model = pg.Model(pg.Biharmonic3D([1.0]), 1)
+    precision = pg.MIXED if kind == "bh3_mixed" else pg.PLAIN
+
+    def fit():
+        it = pg.Interpolant(model, precision)
+        it.fit(pts, vals, 1e-4)
+        return it.weights, it.fit_stats
+
+    monkeypatch.delenv("PGPU_RAS_HOST_DIVIDE", raising=False)
+    w_dev, s_dev = fit()
+    w_again, _ = fit()
+    monkeypatch.setenv("PGPU_RAS_HOST_DIVIDE", "1")
+    w_host, s_host = fit()
+    np.testing.assert_array_equal(w_dev, w_again)  # the fit itself is deterministic
+    assert s_dev["levels"] == s_host["levels"] >= 3
+    assert s_dev["n_domains"] == s_host["n_domains"]
+    assert s_dev["iterations"] == s_host["iterations"]
+    np.testing.assert_array_equal(w_dev, w_host)
