@@ -16,6 +16,7 @@
 #include <exception>
 #include <mutex>
 #include <thread>
+#include <type_traits>
 
 #include "kernels.cuh"
 #include "linalg.hpp"
@@ -484,6 +485,99 @@ __device__ void chol_solve_inplace(double* x, const T* __restrict__ m, int ld) {
   }
 }
 
+// The same solve for an FP32 factor, in FP32 (the factor's own precision; FP64 arithmetic runs
+// at 1/64 of the FP32 rate here and would bound the sweep). Each 32-column panel is streamed
+// once per sweep with float4 loads: rows below the diagonal block in the forward sweep,
+// columns in the backward sweep (four columns per warp, a dot product each).
+__device__ void chol_solve_f32(float* x, const float* __restrict__ m, int ld) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int nb = ld / NB;
+  // Forward: L y = b.
+  for (int kb = 0; kb < nb; ++kb) {
+    const int base = kb * NB;
+    if (warp == 0) {
+      // y_blk = L_kk^{-1} b_blk; lane i holds row i of the inverted (lower) diagonal block.
+      const float bi = x[base + lane];
+      const float* row = m + base + lane + static_cast<Index>(base) * ld;
+      float yi = 0.0f;
+#pragma unroll 1
+      for (int j0 = 0; j0 < NB; j0 += 8) {
+        float a[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) a[q] = j0 + q <= lane ? row[static_cast<Index>(j0 + q) * ld] : 0.0f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) yi = fmaf(a[q], __shfl_sync(0xffffffffu, bi, j0 + q), yi);
+      }
+      x[base + lane] = yi;
+    }
+    __syncthreads();
+    const float* panel = m + static_cast<Index>(base) * ld;
+#pragma unroll 1
+    for (int r = base + NB + 4 * tid; r < ld; r += 4 * blockDim.x) {
+      float4 s = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll 4
+      for (int c = 0; c < NB; ++c) {
+        const float4 v = *reinterpret_cast<const float4*>(panel + r + static_cast<Index>(c) * ld);
+        const float xc = x[base + c];
+        s.x = fmaf(v.x, xc, s.x);
+        s.y = fmaf(v.y, xc, s.y);
+        s.z = fmaf(v.z, xc, s.z);
+        s.w = fmaf(v.w, xc, s.w);
+      }
+      float4* xr = reinterpret_cast<float4*>(x + r);
+      float4 t = *xr;
+      t.x -= s.x;
+      t.y -= s.y;
+      t.z -= s.z;
+      t.w -= s.w;
+      *xr = t;
+    }
+    __syncthreads();
+  }
+  // Backward: L^T x = y.
+  for (int kb = nb - 1; kb >= 0; --kb) {
+    const int base = kb * NB, below = base + NB;
+    for (int c0 = 4 * warp; c0 < NB; c0 += 4 * nw) {
+      float s[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll 2
+      for (int r = below + 4 * lane; r < ld; r += 128) {
+        const float4 xr = *reinterpret_cast<const float4*>(x + r);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float4 v =
+              *reinterpret_cast<const float4*>(m + r + static_cast<Index>(base + c0 + q) * ld);
+          s[q] = fmaf(v.x, xr.x, fmaf(v.y, xr.y, fmaf(v.z, xr.z, fmaf(v.w, xr.w, s[q]))));
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        for (int o = 16; o > 0; o >>= 1) s[q] += __shfl_xor_sync(0xffffffffu, s[q], o);
+        if (lane == 0) x[base + c0 + q] -= s[q];
+      }
+    }
+    __syncthreads();
+    if (warp == 0) {
+      // x_blk = L_kk^{-T} y_blk; lane i holds column i of the inverted diagonal block.
+      const float yi = x[base + lane];
+      const float* col = m + base + static_cast<Index>(base + lane) * ld;
+      float zi = 0.0f;
+#pragma unroll 1
+      for (int j0 = 0; j0 < NB; j0 += 8) {
+        const float4 v0 = *reinterpret_cast<const float4*>(col + j0);
+        const float4 v1 = *reinterpret_cast<const float4*>(col + j0 + 4);
+        const float a[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const float yj = __shfl_sync(0xffffffffu, yi, j0 + q);
+          if (j0 + q >= lane) zi = fmaf(a[q], yj, zi);
+        }
+      }
+      x[base + lane] = zi;
+    }
+    __syncthreads();
+  }
+}
+
 // Column j of (L L^T)^{-1} for every j (grid = ld blocks): the coarse grid keeps the explicit
 // inverse so that each coarse solve is one matrix-vector product spread over the GPU.
 template <class T>
@@ -581,9 +675,9 @@ __global__ void __launch_bounds__(256, 4) ras_solve_kernel(const int* __restrict
   const Index* dp = pts + pt_off[d];
   const char* din = inner + pt_off[d];
   const T* m = mats + mat_off[d];
-  double* x = sh;            // ld
-  double* dh = sh + ld;      // l (polynomial-point residuals)
-  double* red = dh + 16;     // 32 * 16 reduction scratch
+  double* dh = sh;                           // l (polynomial-point residuals)
+  double* red = sh + 16;                     // 2 x 32 reduction scratch
+  T* x = reinterpret_cast<T*>(sh + 80);      // ld, in the factor's precision
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
 
   for (int k = tid; k < l; k += blockDim.x) dh[k] = resid[dp[k]];
@@ -595,10 +689,13 @@ __global__ void __launch_bounds__(256, 4) ras_solve_kernel(const int* __restrict
       s = resid[g];
       for (int k = 0; k < l; ++k) s -= lag[g * l + k] * dh[k];
     }
-    x[i] = s;
+    x[i] = static_cast<T>(s);
   }
   __syncthreads();
-  chol_solve_inplace(x, m, ld);
+  if constexpr (std::is_same_v<T, float>)
+    chol_solve_f32(x, m, ld);
+  else
+    chol_solve_inplace(x, m, ld);
   // lambda_head_k = -sum_i L_ik gamma_i ; for the coarse grid also s_k = sum_i u_ik gamma_i.
   for (int k = 0; k < l; ++k) {
     double s1 = 0, s2 = 0;
