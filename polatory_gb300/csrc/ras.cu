@@ -392,6 +392,119 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, unsigned src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(
+                   static_cast<unsigned>(__cvta_generic_to_shared(dst))),
+               "l"(src), "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// FP32 trailing update of a panel group over 128 x 128 tiles: C(i, j) -= sum over the group's
+// columns of L(i, k) L(j, k) for the lower tiles of the trailing matrix (rows and columns from
+// (kb0 + np) * 32). 256 threads, 8 x 8 outputs each; the group's columns stream through a
+// three-stage cp.async pipeline in chunks of 16 (rows contiguous, as in the factor). The grid
+// is (tile, domain), tiles fastest, so the blocks running together share one domain's panels in
+// L2. Rows past the domain load zeros; a diagonal tile writes its 32-blocks on and below the
+// diagonal only.
+constexpr int kTile = 128, kChunk = 16, kStages = 3;
+constexpr size_t kSyrk128Smem = 2ull * kStages * kChunk * kTile * sizeof(float);
+
+__global__ void __launch_bounds__(256, 2)
+    syrk128_update_kernel(int kb0, int np, const int* __restrict__ lds,
+                          const Index* __restrict__ mat_off, float* __restrict__ mats) {
+  const Index d = blockIdx.y;
+  const int ld = lds[d];
+  const int first = (kb0 + np) * NB;
+  if (first >= ld) return;
+  const int nt = (ld - first + kTile - 1) / kTile;
+  if (static_cast<Index>(blockIdx.x) >= static_cast<Index>(nt) * (nt + 1) / 2) return;
+  int ti, tj;
+  tile_of(blockIdx.x, ti, tj);
+  const int r0 = first + ti * kTile, c0 = first + tj * kTile;
+  float* mat = mats + mat_off[d];
+  const float* panel = mat + static_cast<Index>(kb0 * NB) * ld;
+  extern __shared__ float4 syrk_smem[];
+  float* sa = reinterpret_cast<float*>(syrk_smem);  // [stage][k][row]
+  float* sb = sa + kStages * kChunk * kTile;        // [stage][k][col]
+  const int tid = threadIdx.x;
+  const int nk = np * NB / kChunk;
+
+  auto load_chunk = [&](int stage, int kc) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int idx = tid + 256 * e;
+      const int which = idx >> 9, w = idx & 511, k = w >> 5, r4 = (w & 31) * 4;
+      const int row = (which ? c0 : r0) + r4;
+      const bool have = row < ld;
+      const float* src = have ? panel + static_cast<Index>(kc + k) * ld + row : panel;
+      float* dst = (which ? sb : sa) + (stage * kChunk + k) * kTile + r4;
+      cp_async16(dst, src, have ? 16u : 0u);
+    }
+  };
+
+  float acc[8][8];
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+#pragma unroll
+    for (int b = 0; b < 8; ++b) acc[a][b] = 0.0f;
+  const int tr = tid & 15, tc = tid >> 4;  // rows 8 tr .., columns 8 tc ..
+
+#pragma unroll
+  for (int st = 0; st < kStages - 1; ++st) {
+    if (st < nk) load_chunk(st, st * kChunk);
+    cp_async_commit();
+  }
+  for (int kk = 0; kk < nk; ++kk) {
+    cp_async_wait<kStages - 2>();
+    __syncthreads();
+    const int nxt = kk + kStages - 1;
+    if (nxt < nk) load_chunk(nxt % kStages, nxt * kChunk);
+    cp_async_commit();
+    const int st = kk % kStages;
+    const float* a_s = sa + st * kChunk * kTile + 8 * tr;
+    const float* b_s = sb + st * kChunk * kTile + 8 * tc;
+#pragma unroll
+    for (int k = 0; k < kChunk; ++k) {
+      const float4 a0 = *reinterpret_cast<const float4*>(a_s + k * kTile);
+      const float4 a1 = *reinterpret_cast<const float4*>(a_s + k * kTile + 4);
+      const float4 b0 = *reinterpret_cast<const float4*>(b_s + k * kTile);
+      const float4 b1 = *reinterpret_cast<const float4*>(b_s + k * kTile + 4);
+      const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(av[a], bv[b], acc[a][b]);
+    }
+  }
+  cp_async_wait<0>();
+
+  const int r = r0 + 8 * tr;  // eight rows inside one 32-block
+  if (r >= ld) return;
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const int c = c0 + 8 * tc + b;
+    if (c >= ld || c / NB > r / NB) continue;
+    float4* dst = reinterpret_cast<float4*>(mat + r + static_cast<Index>(c) * ld);
+    float4 x0 = dst[0], x1 = dst[1];
+    x0.x -= acc[0][b];
+    x0.y -= acc[1][b];
+    x0.z -= acc[2][b];
+    x0.w -= acc[3][b];
+    x1.x -= acc[4][b];
+    x1.y -= acc[5][b];
+    x1.z -= acc[6][b];
+    x1.w -= acc[7][b];
+    dst[0] = x0;
+    dst[1] = x1;
+  }
+}
+
 // Replaces every 32x32 diagonal block of the Cholesky factor by its inverse (lower triangular),
 // so that the triangular solves apply the diagonal blocks as small matrix-vector products
 // instead of 32-step dependent substitutions.
@@ -1166,10 +1279,17 @@ void RasPreconditioner<T>::build_batch(DomainBatch<U>& b, const std::vector<Inde
     }
     const int rem = nbmax - g0 - np;
     if (rem <= 0) continue;
-    const int rem2 = (rem + 1) / 2;
-    dim3 gs(nd, static_cast<unsigned>(static_cast<Index>(rem2) * (rem2 + 1) / 2));
-    syrk64_update_kernel<U><<<gs, 256, 0, stream()>>>(g0, np, b.ld.data(), b.mat_off.data(),
-                                                      b.mats.data());
+    if (std::is_same_v<U, float> && nd <= 65535) {
+      const int nt = (rem * NB + kTile - 1) / kTile;
+      dim3 gs(static_cast<unsigned>(nt * (nt + 1) / 2), nd);
+      syrk128_update_kernel<<<gs, 256, kSyrk128Smem, stream()>>>(
+          g0, np, b.ld.data(), b.mat_off.data(), reinterpret_cast<float*>(b.mats.data()));
+    } else {
+      const int rem2 = (rem + 1) / 2;
+      dim3 gs(nd, static_cast<unsigned>(static_cast<Index>(rem2) * (rem2 + 1) / 2));
+      syrk64_update_kernel<U><<<gs, 256, 0, stream()>>>(g0, np, b.ld.data(), b.mat_off.data(),
+                                                        b.mats.data());
+    }
     PGPU_LAUNCH_CHECK();
   }
   invert_diag_kernel<U><<<dim3(static_cast<unsigned>(b.n_dom), nbmax), 32, 0, stream()>>>(
