@@ -505,6 +505,93 @@ __global__ void __launch_bounds__(256, 2)
   }
 }
 
+// FP32 left-looking update of one block column inside a panel group: C(i, j) -= sum over the
+// group's panels [kb0, kb0 + np) of L(i, k) L(j, k) for the 32 columns of block column
+// kb0 + np and every row from that block down. 128-row tiles, 256 threads with 4 x 4 outputs
+// each, the trailing update's cp.async pipeline; grid (row tile, domain).
+constexpr size_t kPanelSmem = static_cast<size_t>(kStages) * kChunk * (kTile + NB) * sizeof(float);
+
+__global__ void __launch_bounds__(256, 4)
+    panel_update_kernel(int kb0, int np, const int* __restrict__ lds,
+                        const Index* __restrict__ mat_off, float* __restrict__ mats) {
+  const Index d = blockIdx.y;
+  const int ld = lds[d];
+  const int c0 = (kb0 + np) * NB;
+  const int r0 = c0 + static_cast<int>(blockIdx.x) * kTile;
+  if (r0 >= ld) return;
+  float* mat = mats + mat_off[d];
+  const float* panel = mat + static_cast<Index>(kb0 * NB) * ld;
+  extern __shared__ float4 panel_smem[];
+  float* sa = reinterpret_cast<float*>(panel_smem);  // [stage][k][row]
+  float* sb = sa + kStages * kChunk * kTile;         // [stage][k][column]
+  const int tid = threadIdx.x;
+  const int nk = np * NB / kChunk;
+
+  auto load_chunk = [&](int stage, int kc) {
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int idx = tid + 256 * e;
+      const int k = idx >> 5, r4 = (idx & 31) * 4;
+      const int row = r0 + r4;
+      const bool have = row < ld;
+      const float* src = have ? panel + static_cast<Index>(kc + k) * ld + row : panel;
+      cp_async16(sa + (stage * kChunk + k) * kTile + r4, src, have ? 16u : 0u);
+    }
+    if (tid < 128) {  // the block column's own 32 rows: c0 + 32 <= ld
+      const int k = tid >> 3, c4 = (tid & 7) * 4;
+      cp_async16(sb + (stage * kChunk + k) * NB + c4, panel + static_cast<Index>(kc + k) * ld + c0 + c4, 16u);
+    }
+  };
+
+  float acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0f;
+  const int tr = tid & 31, tc = tid >> 5;  // rows 4 tr .., columns 4 tc ..
+
+#pragma unroll
+  for (int st = 0; st < kStages - 1; ++st) {
+    if (st < nk) load_chunk(st, st * kChunk);
+    cp_async_commit();
+  }
+  for (int kk = 0; kk < nk; ++kk) {
+    cp_async_wait<kStages - 2>();
+    __syncthreads();
+    const int nxt = kk + kStages - 1;
+    if (nxt < nk) load_chunk(nxt % kStages, nxt * kChunk);
+    cp_async_commit();
+    const int st = kk % kStages;
+    const float* a_s = sa + st * kChunk * kTile + 4 * tr;
+    const float* b_s = sb + st * kChunk * NB + 4 * tc;
+#pragma unroll
+    for (int k = 0; k < kChunk; ++k) {
+      const float4 av = *reinterpret_cast<const float4*>(a_s + k * kTile);
+      const float4 bv = *reinterpret_cast<const float4*>(b_s + k * NB);
+      const float a4[4] = {av.x, av.y, av.z, av.w};
+      const float b4[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = fmaf(a4[a], b4[b], acc[a][b]);
+    }
+  }
+  cp_async_wait<0>();
+
+  const int r = r0 + 4 * tr;
+  if (r >= ld) return;
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    float4* dst = reinterpret_cast<float4*>(mat + r + static_cast<Index>(c0 + 4 * tc + b) * ld);
+    float4 x = *dst;
+    x.x -= acc[0][b];
+    x.y -= acc[1][b];
+    x.z -= acc[2][b];
+    x.w -= acc[3][b];
+    *dst = x;
+  }
+}
+
 // Replaces every 32x32 diagonal block of the Cholesky factor by its inverse (lower triangular),
 // so that the triangular solves apply the diagonal blocks as small matrix-vector products
 // instead of 32-step dependent substitutions.
@@ -1264,8 +1351,14 @@ void RasPreconditioner<T>::build_batch(DomainBatch<U>& b, const std::vector<Inde
     for (int p = 0; p < np; ++p) {
       const int kb = g0 + p;
       if (p > 0) {
-        syrk_update_kernel<U><<<dim3(nd, static_cast<unsigned>(nbmax - kb)), 256, 0, stream()>>>(
-            g0, p, 1, b.ld.data(), b.mat_off.data(), b.mats.data());
+        if (std::is_same_v<U, float> && nd <= 65535) {
+          const int gx = (b.max_n - kb * NB + kTile - 1) / kTile;
+          panel_update_kernel<<<dim3(static_cast<unsigned>(gx), nd), 256, kPanelSmem, stream()>>>(
+              g0, p, b.ld.data(), b.mat_off.data(), reinterpret_cast<float*>(b.mats.data()));
+        } else {
+          syrk_update_kernel<U><<<dim3(nd, static_cast<unsigned>(nbmax - kb)), 256, 0, stream()>>>(
+              g0, p, 1, b.ld.data(), b.mat_off.data(), b.mats.data());
+        }
         PGPU_LAUNCH_CHECK();
       }
       potrf_diag_kernel<U><<<nd, 32, 0, stream()>>>(kb, b.ld.data(), b.mat_off.data(),
