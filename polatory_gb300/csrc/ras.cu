@@ -127,11 +127,13 @@ __global__ void assemble_kernel(KParams<T> kp, const P4<T>* __restrict__ frame,
                                 const Index* __restrict__ pt_off, const Index* __restrict__ pts,
                                 int l, int first, int last, double nugget,
                                 const double* __restrict__ lag, const double* __restrict__ u,
-                                const double* __restrict__ v) {
-  const Index d = blockIdx.x;
+                                const double* __restrict__ v, int tiles_in_x) {
+  // tiles_in_x: grid (tile, domain), so that the blocks running together are the tiles of a
+  // few domains and their gathered point data stays in L2; otherwise grid (domain, tile).
+  const Index d = tiles_in_x ? blockIdx.y : blockIdx.x;
   const int n = nsz[d], ld = lds[d];
   int bi, bj;
-  tile_of(blockIdx.y, bi, bj);
+  tile_of(tiles_in_x ? blockIdx.x : blockIdx.y, bi, bj);
   if (bi * NB >= ld) return;
   T* m = mats + mat_off[d];
   const Index* dp = pts + pt_off[d] + l;  // non-polynomial points
@@ -1329,13 +1331,15 @@ void RasPreconditioner<T>::build_batch(DomainBatch<U>& b, const std::vector<Inde
     PGPU_LAUNCH_CHECK();
     KParams<U> kp{static_cast<U>(rb.p[0]), static_cast<U>(rb.p[1])};
     const int first = r == 0, last = r + 1 == model_.rbfs.size();
-    if (ntiles > 65535) throw_runtime("domain too large for the batched assembly");
-    dim3 grid(static_cast<unsigned>(b.n_dom), static_cast<unsigned>(ntiles));
+    const int tiles_in_x = b.n_dom <= 65535 ? 1 : 0;
+    if (!tiles_in_x && ntiles > 65535) throw_runtime("domain too large for the batched assembly");
+    const dim3 grid = tiles_in_x ? dim3(static_cast<unsigned>(ntiles), static_cast<unsigned>(b.n_dom))
+                                 : dim3(static_cast<unsigned>(b.n_dom), static_cast<unsigned>(ntiles));
     dispatch_kind(rb.kind, [&]<int K>() {
       assemble_kernel<U, K><<<grid, 256, 0, stream()>>>(
           kp, frame.data(), b.n.data(), b.ld.data(), b.mat_off.data(), b.mats.data(),
           b.pt_off.data(), b.pts.data(), l, first, last, model_.nugget, lagrange_.data(),
-          u_.data(), v_.data());
+          u_.data(), v_.data(), tiles_in_x);
       return 0;
     });
     PGPU_LAUNCH_CHECK();
