@@ -4,7 +4,9 @@
 //     coarse-point count within [n + l, n + l + 3));
 //  2. domain sizes (points + 3 x gradient points) at most 1024;
 //  3. the level-parallel coarse-point selection returns the same set as a direct sequential
-//     restatement of the priority-queue rule (domain_divider.hpp:54-125) on value points.
+//     restatement of the priority-queue rule (domain_divider.hpp:54-125) on value points, in
+//     the canonical order (polynomial points, then ascending index);
+//  4. asking for more coarse points than there are points returns every point once.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -163,6 +165,48 @@ static void check_coarse_equivalence(Index n, Index n_coarse, unsigned seed) {
   std::set<Index> a(got.begin(), got.end()), b(want.begin(), want.end());
   CHECK(a == b);
   CHECK(got.size() == want.size());
+  CHECK(std::equal(poly.begin(), poly.end(), got.begin()));
+  CHECK(std::is_sorted(got.begin() + static_cast<std::ptrdiff_t>(poly.size()), got.end()));
+}
+
+// Single-point clusters split into themselves, so the selection stops when every cluster is a
+// single point, with every point a centre.
+static void check_coarse_saturation(Index n, unsigned seed) {
+  std::mt19937 gen(seed);
+  std::uniform_real_distribution<double> u(0.0, 1.0);
+  std::vector<double> p(3 * n);
+  for (auto& v : p) v = u(gen);
+  std::vector<Index> idx(n), none;
+  std::iota(idx.begin(), idx.end(), 0);
+  std::vector<Index> poly{0, 1, 2, 3};
+  pgpu::DomainDivider div(p.data(), nullptr, idx, none, poly);
+  auto got = div.choose_coarse_points(10 * n).first;
+  CHECK(static_cast<Index>(got.size()) == n);
+  CHECK(std::equal(poly.begin(), poly.end(), got.begin()));
+  CHECK(std::is_sorted(got.begin() + 4, got.end()));
+  CHECK(static_cast<Index>(std::set<Index>(got.begin(), got.end()).size()) == n);
+}
+
+// The split sizes shared by the host and device dividers.
+static void check_split_sizes() {
+  for (Index n = 1025; n < 200000; n = n * 3 / 2 + 7) {
+    Index lp, mid, rp;
+    pgpu::overlap_split_sizes(n, lp, mid, rp);
+    CHECK(0 < lp && lp <= mid && mid <= rp && rp < n);
+    CHECK(rp + (n - lp) >= n);  // the halves cover the domain
+  }
+  for (Index n = 0; n < 100; ++n) {
+    const Index m = pgpu::cluster_split(n);
+    Index best = 0, bestd = n;
+    for (Index i = 1; i < n; ++i) {
+      const Index di = std::llabs(2 * i - n);
+      if (di < bestd || (di == bestd && i % 2 == 0)) {
+        best = i;
+        bestd = di;
+      }
+    }
+    CHECK(m == best);
+  }
 }
 
 // The data-parallel split of large point sets gives the same domains and coarse points as the
@@ -200,6 +244,8 @@ int main() {
   check_coarse_equivalence(5000, 700, 4);
   check_coarse_equivalence(20000, 2048, 5);
   check_coarse_equivalence(3000, 1500, 6);
+  check_coarse_saturation(200, 8);
+  check_split_sizes();
   if (failures) {
     std::printf("%d failures\n", failures);
     return 1;
