@@ -88,8 +88,8 @@ __global__ void lagrange_kernel(int degree, int l, const double* __restrict__ pt
   }
 }
 
-// A p for the division of an anisotropic model, rounded like the host restatement:
-// (a0 p0 + a1 p1) + a2 p2 per row.
+// The points as the division of an anisotropic model sees them, A p, rounded like the host
+// restatement: (a0 p0 + a1 p1) + a2 p2 per row of A.
 __global__ void transform_points_kernel(const double* __restrict__ pts, Index n, Mat3 a,
                                         double* __restrict__ out) {
   const Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
