@@ -108,6 +108,16 @@ int pgpu_profile_enable(int on);
 int pgpu_profile_reset(void);
 int pgpu_profile_report(char* buf, int64_t size);
 int pgpu_launch_count(int64_t* out);
+/* Host-side fault injection for failure-detection tests (no reference counterpart); nothing
+ * here faults the GPU. what = PGPU_INJECT_ALLOC: the `after`-th next device allocation made by
+ * this thread (1 = the next one) fails as an exhausted memory pool would, so the running call
+ * returns PGPU_OUT_OF_MEMORY. what = PGPU_INJECT_M2L_STALL: in the next tensor-core M2L launch
+ * of this thread, the first CTA leaves the operator copy of its first pipeline stage unissued
+ * and polls its mbarrier at most `after` times, so that bounded wait runs out: the CTA waits
+ * for its other copies in flight and its MMAs, frees its TMEM and returns, and the call returns
+ * PGPU_TIMEOUT. after <= 0 clears the injection. */
+enum { PGPU_INJECT_ALLOC = 1, PGPU_INJECT_M2L_STALL = 2 };
+int pgpu_debug_inject(int what, int64_t after);
 /* Synchronizes the library stream of this thread. */
 int pgpu_synchronize(void);
 /* The library's CUDA stream of this thread (a cudaStream_t), for event timing by callers. */
@@ -155,11 +165,37 @@ int pgpu_evaluator_evaluate(pgpu_evaluator* ev, double* out, int64_t n);
  * (NULL = legacy default stream). All pointers must be device pointers; nothing is allocated or
  * copied. Partial sums live in a fixed 16 MiB device array compiled into the library (held by
  * every GPU that loads it until exit), which limits a call to 2,097,152 targets; larger calls
- * return PGPU_INVALID_ARGUMENT. The first call on a device looks the array up on that device.
- * Calls share the array: calls that may overlap on the GPU race and must be serialised. */
+ * return PGPU_INVALID_ARGUMENT. The entry point runs on the caller's current CUDA device (not the
+ * device chosen by pgpu_set_device), and every pointer must be memory of that device or managed
+ * memory. The first call on a device looks the array up on that device (make it before any
+ * stream capture) and keeps its address until exit: do not call the entry point again after
+ * cudaDeviceReset or another teardown of the device's primary context. Calls share the array:
+ * calls that may overlap on the GPU race and must be serialised. */
 int pgpu_direct_evaluate_noalloc(const pgpu_rbf* rbf, const double* src_points, int64_t n_src,
                                  const double* weights, const double* trg_points, int64_t n_trg,
                                  double* out, void* stream);
+
+/* ---- component tests of the solver and the preconditioner ------------------------------
+ * Device runs of the FGMRES and of one RAS domain on caller-given inputs (host buffers), so that
+ * the reference's own unit tests of these components can be restated against the device code:
+ * test/krylov/test_krylov.cpp:21-137 and test/preconditioner/test_{fine,coarse}_grid.cpp. */
+/* FGMRES (src/krylov/fgmres.cpp, gmres.cpp) on the dense row-major n x n operator op, with the
+ * optional dense right preconditioner pc and initial solution x0 (NULL: identity / zero), for
+ * iters <= n iterations: after iteration k, solutions[k * n ..] receives the solution estimate
+ * (Fgmres::solution_vector) and rel_residuals[k] the relative residual estimate
+ * (GmresBase::relative_residual). */
+int pgpu_krylov_fgmres_dense(int64_t n, const double* op, const double* pc, const double* rhs,
+                             const double* x0, int iters, double* solutions, double* rel_residuals);
+/* One RAS domain holding all n points (preconditioner/fine_grid.hpp:36-195,
+ * coarse_grid.hpp:19-159; value points only): order is a permutation of 0..n-1 whose first l
+ * entries are the polynomial points of the Lagrange basis, inner the fine-grid inner flag of each
+ * entry of order. coarse != 0 solves rhs (n values) as the coarse grid (use_inverse != 0: through
+ * the explicit inverse that a multilevel preconditioner keeps), writing all n weights and the l
+ * polynomial coefficients; coarse == 0 solves it as a fine-grid domain, writing the weights of
+ * the inner points (zeros elsewhere). precision MIXED uses FP32 factors. out: n + l values. */
+int pgpu_ras_domain_solve(const pgpu_model* model, const double* points, int64_t n,
+                          const int64_t* order, const unsigned char* inner, int coarse,
+                          int use_inverse, int precision, const double* rhs, double* out);
 
 /* ---- Interpolant (interpolant.hpp:54-218) --------------------------------------------- */
 typedef struct pgpu_interpolant pgpu_interpolant;
@@ -173,6 +209,8 @@ typedef struct pgpu_fit_stats {
   double setup_seconds;    /* tree + preconditioner setup */
   double solve_seconds;    /* FGMRES loop */
   int64_t n_domains;       /* RAS domains over all fine levels */
+  int32_t precision_used;  /* PGPU_PRECISION_* of the arithmetic that produced the weights */
+  int32_t fell_back;       /* 1: a MIXED fit met a non-finite FP32 value and reran in FP64 */
 } pgpu_fit_stats;
 
 int pgpu_interpolant_create(const pgpu_model* model, pgpu_interpolant** out);

@@ -76,6 +76,40 @@ def rbf_isotropic(kind: int, params, diff):
     return float(v[0]), g, (h.reshape(3, 3) if rc == 0 else None)
 
 
+RBF_KINDS = ["bh2", "bh3", "cub", "exp", "gau", "gc3", "gc5", "gc7", "gc9", "sph", "sp3", "sp5",
+             "sp7", "sp9", "th2", "th3"]
+
+
+class Rbf(C.Structure):
+    """pgpu_rbf of include/polatory_gpu.h (declared here so that the oracle needs no product
+    library)."""
+    _fields_ = [("kind", C.c_int32), ("reserved", C.c_int32), ("params", C.c_double * 2),
+                ("aniso", C.c_double * 9)]
+
+
+class Model(C.Structure):
+    """pgpu_model of include/polatory_gpu.h."""
+    _fields_ = [("n_rbfs", C.c_int32), ("poly_degree", C.c_int32), ("nugget", C.c_double),
+                ("rbfs", Rbf * 4)]
+
+
+def model(kind: str, params, poly_degree: int, nugget: float = 0.0, aniso=None) -> Model:
+    """A one-RBF model struct: kind is the reference's short name ("bh3", "exp", ...), params
+    the RBF's parameters (scale, or psill and range), aniso the 3x3 anisotropy (identity)."""
+    m = Model()
+    m.n_rbfs = 1
+    m.poly_degree = poly_degree
+    m.nugget = nugget
+    r = m.rbfs[0]
+    r.kind = RBF_KINDS.index(kind)
+    p = list(params) + [0.0] * (2 - len(params))
+    r.params[0], r.params[1] = p[0], p[1]
+    a = np.eye(3) if aniso is None else np.asarray(aniso, dtype=np.float64).reshape(3, 3)
+    for k in range(9):
+        r.aniso[k] = a.reshape(9)[k]
+    return m
+
+
 def _model(model):
     """Accepts a polatory_gb300.Model (uses its C struct) or a ready ctypes struct."""
     return model._c() if hasattr(model, "_c") else model

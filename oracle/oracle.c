@@ -346,48 +346,104 @@ int orc_direct_operator(const pgpu_model* model, const double* pts, int64_t mu,
 
 /* ---- exact fit: the saddle-point system [A + nugget I, P; P^T, 0] --------------------- */
 
-/* LU with partial pivoting, in place on an n x n row-major matrix; solves for b. */
+/* LU with partial pivoting, in place on an n x n row-major matrix; solves for b. Right-looking
+ * and blocked (panels of LU_NB columns): the panel is factored column by column with row
+ * swaps across the whole matrix, the block row of U is solved with the panel's unit lower
+ * triangle, and the trailing matrix takes one rank-LU_NB update, register-tiled 4 rows x 8
+ * columns and spread over the host threads by row blocks. The arithmetic is the textbook
+ * algorithm (Golub & Van Loan, Alg. 3.4.2 with the block update of section 3.2.10). */
+#define LU_NB 64
 static int lu_solve(double* a, int64_t n, double* b) {
-  int64_t* piv = (int64_t*)malloc(sizeof(int64_t) * (n > 0 ? n : 1));
-  for (int64_t k = 0; k < n; ++k) {
-    int64_t p = k;
-    double best = fabs(a[k * n + k]);
-    for (int64_t i = k + 1; i < n; ++i)
-      if (fabs(a[i * n + k]) > best) {
-        best = fabs(a[i * n + k]);
-        p = i;
+  for (int64_t k0 = 0; k0 < n; k0 += LU_NB) {
+    const int64_t kb = n - k0 < LU_NB ? n - k0 : LU_NB;
+    const int64_t k1 = k0 + kb;
+    for (int64_t k = k0; k < k1; ++k) {
+      int64_t p = k;
+      double best = fabs(a[k * n + k]);
+      for (int64_t i = k + 1; i < n; ++i)
+        if (fabs(a[i * n + k]) > best) {
+          best = fabs(a[i * n + k]);
+          p = i;
+        }
+      if (best == 0.0) return -1;
+      if (p != k) {
+        double* rk = a + k * n;
+        double* rp = a + p * n;
+        for (int64_t j = 0; j < n; ++j) {
+          double t = rk[j];
+          rk[j] = rp[j];
+          rp[j] = t;
+        }
+        double t = b[k];
+        b[k] = b[p];
+        b[p] = t;
       }
-    if (best == 0.0) {
-      free(piv);
-      return -1;
-    }
-    piv[k] = p;
-    if (p != k) {
-      for (int64_t j = 0; j < n; ++j) {
-        double t = a[k * n + j];
-        a[k * n + j] = a[p * n + j];
-        a[p * n + j] = t;
+      const double inv = 1.0 / a[k * n + k];
+      /* Column k below the pivot, and the rest of the panel (columns k+1 .. k1-1). */
+#pragma omp parallel for schedule(static) if (n - k > 4096)
+      for (int64_t i = k + 1; i < n; ++i) {
+        double* ri = a + i * n;
+        const double f = ri[k] * inv;
+        ri[k] = f;
+        if (f != 0.0)
+          for (int64_t j = k + 1; j < k1; ++j) ri[j] -= f * a[k * n + j];
       }
-      double t = b[k];
-      b[k] = b[p];
-      b[p] = t;
     }
-    const double inv = 1.0 / a[k * n + k];
+    if (k1 >= n) break;
+    /* U12 = L11^{-1} A12 (unit lower L11), by column chunks. */
 #pragma omp parallel for schedule(static)
-    for (int64_t i = k + 1; i < n; ++i) {
-      const double f = a[i * n + k] * inv;
-      a[i * n + k] = f;
-      if (f != 0.0)
-        for (int64_t j = k + 1; j < n; ++j) a[i * n + j] -= f * a[k * n + j];
+    for (int64_t j0 = k1; j0 < n; j0 += 256) {
+      const int64_t j1 = j0 + 256 < n ? j0 + 256 : n;
+      for (int64_t k = k0; k < k1; ++k)
+        for (int64_t i = k + 1; i < k1; ++i) {
+          const double f = a[i * n + k];
+          if (f != 0.0)
+            for (int64_t j = j0; j < j1; ++j) a[i * n + j] -= f * a[k * n + j];
+        }
     }
-    for (int64_t i = k + 1; i < n; ++i) b[i] -= a[i * n + k] * b[k];
+    /* A22 -= L21 U12 over 4-row blocks; 8-column register tiles. */
+    const int64_t nrb = (n - k1 + 3) / 4;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t rb = 0; rb < nrb; ++rb) {
+      const int64_t i0 = k1 + 4 * rb;
+      const int64_t ni = n - i0 < 4 ? n - i0 : 4;
+      double lrow[4][LU_NB];
+      for (int r = 0; r < 4; ++r)
+        for (int64_t k = 0; k < kb; ++k) lrow[r][k] = r < ni ? a[(i0 + r) * n + k0 + k] : 0.0;
+      int64_t j = k1;
+      for (; j + 8 <= n; j += 8) {
+        double acc[4][8];
+        for (int r = 0; r < 4; ++r)
+          for (int c = 0; c < 8; ++c) acc[r][c] = r < ni ? a[(i0 + r) * n + j + c] : 0.0;
+        for (int64_t k = 0; k < kb; ++k) {
+          const double* u = a + (k0 + k) * n + j;
+          for (int r = 0; r < 4; ++r) {
+            const double f = lrow[r][k];
+            for (int c = 0; c < 8; ++c) acc[r][c] -= f * u[c];
+          }
+        }
+        for (int r = 0; r < ni; ++r)
+          for (int c = 0; c < 8; ++c) a[(i0 + r) * n + j + c] = acc[r][c];
+      }
+      for (; j < n; ++j)
+        for (int r = 0; r < ni; ++r) {
+          double s = a[(i0 + r) * n + j];
+          for (int64_t k = 0; k < kb; ++k) s -= lrow[r][k] * a[(k0 + k) * n + j];
+          a[(i0 + r) * n + j] = s;
+        }
+    }
+  }
+  /* Forward (unit L) and backward (U) substitution. */
+  for (int64_t i = 1; i < n; ++i) {
+    double s = b[i];
+    for (int64_t j = 0; j < i; ++j) s -= a[i * n + j] * b[j];
+    b[i] = s;
   }
   for (int64_t i = n - 1; i >= 0; --i) {
     double s = b[i];
     for (int64_t j = i + 1; j < n; ++j) s -= a[i * n + j] * b[j];
     b[i] = s / a[i * n + i];
   }
-  free(piv);
   return 0;
 }
 

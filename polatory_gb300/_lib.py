@@ -1,6 +1,6 @@
 """ctypes binding of libpolatory_gpu.so (the C ABI in include/polatory_gpu.h).
 
-The shared library must be built in-tree (python -m polatory_gb300.build); importing this module
+The shared library must be built in-tree (python polatory_gb300/build.py); importing this module
 raises when it is missing. There is no CPU fallback.
 """
 from __future__ import annotations
@@ -21,6 +21,9 @@ PGPU_NOT_IMPLEMENTED = 5
 PGPU_MAX_ITER = 6
 PGPU_TIMEOUT = 7
 PGPU_REJECTED = 8
+
+INJECT_ALLOC = 1
+INJECT_M2L_STALL = 2
 
 PRECISION_PLAIN = 0
 PRECISION_MIXED = 1
@@ -50,7 +53,8 @@ class PgpuModel(C.Structure):
 class PgpuFitStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("levels", C.c_int32), ("residual", C.c_double),
                 ("grad_residual", C.c_double), ("setup_seconds", C.c_double),
-                ("solve_seconds", C.c_double), ("n_domains", C.c_int64)]
+                ("solve_seconds", C.c_double), ("n_domains", C.c_int64),
+                ("precision_used", C.c_int32), ("fell_back", C.c_int32)]
 
 
 class PgpuFitProblem(C.Structure):
@@ -82,7 +86,7 @@ class PolatoryError(RuntimeError):
 
 def _load():
     if not LIB_PATH.exists():
-        raise ImportError(f"{LIB_PATH} is missing: build it with python -m polatory_gb300.build")
+        raise ImportError(f"{LIB_PATH} is missing: build it with python polatory_gb300/build.py")
     lib = C.CDLL(str(LIB_PATH))
     P = C.c_void_p
     D = C.POINTER(C.c_double)
@@ -97,6 +101,7 @@ def _load():
         "pgpu_profile_report": ([C.c_char_p, I64], C.c_int),
         "pgpu_launch_count": ([C.POINTER(I64)], C.c_int),
         "pgpu_synchronize": ([], C.c_int),
+        "pgpu_debug_inject": ([C.c_int, I64], C.c_int),
         "pgpu_stream": ([C.POINTER(C.c_void_p)], C.c_int),
         "pgpu_rbf_evaluate": ([C.POINTER(PgpuRbf), P, I64, P, P, P], C.c_int),
         "pgpu_rbf_cpd_order": ([C.POINTER(PgpuRbf), C.POINTER(C.c_int)], C.c_int),
@@ -114,6 +119,9 @@ def _load():
         "pgpu_evaluator_configure": ([P, C.c_int, C.c_int, C.c_int], C.c_int),
         "pgpu_evaluator_evaluate": ([P, P, I64], C.c_int),
         "pgpu_direct_evaluate_noalloc": ([C.POINTER(PgpuRbf), P, I64, P, P, I64, P, P], C.c_int),
+        "pgpu_krylov_fgmres_dense": ([I64, P, P, P, P, C.c_int, P, P], C.c_int),
+        "pgpu_ras_domain_solve": ([C.POINTER(PgpuModel), P, I64, P, P, C.c_int, C.c_int,
+                                   C.c_int, P, P], C.c_int),
         "pgpu_interpolant_create": ([C.POINTER(PgpuModel), C.POINTER(P)], C.c_int),
         "pgpu_interpolant_destroy": ([P], C.c_int),
         "pgpu_interpolant_set_precision": ([P, C.c_int], C.c_int),

@@ -1,6 +1,6 @@
 """Builds libpolatory_gpu.so in-tree for sm_103a (nvcc) and the host objects (g++).
 
-Usage: python -m polatory_gb300.build   (or polatory_gb300.build.build())
+Usage: python polatory_gb300/build.py   (or __graft_entry__.build())
 """
 from __future__ import annotations
 

@@ -14,6 +14,7 @@
 #include "evaluator.hpp"
 #include "model.hpp"
 #include "profile.hpp"
+#include "ras.hpp"
 #include "rbf.cuh"
 #include "solver.hpp"
 
@@ -126,6 +127,17 @@ int pgpu_launch_count(int64_t* out) {
   return guarded([&] {
     check_ptr(out, "out");
     *out = launch_count();
+  });
+}
+
+int pgpu_debug_inject(int what, int64_t after) {
+  return guarded([&] {
+    if (what == PGPU_INJECT_ALLOC)
+      inject_alloc_failure(after);
+    else if (what == PGPU_INJECT_M2L_STALL)
+      inject_m2l_stall(after);
+    else
+      throw_invalid("unknown injection");
   });
 }
 
@@ -332,6 +344,10 @@ int pgpu_evaluator_set_source_points(pgpu_evaluator* ev, const double* points, i
     ev->e64.reset();
     ev->e32.reset();
     ev->weights_set = false;
+    if (!device_all_finite(ev->src.data(), 3 * n)) {
+      ev->n_src = 0;
+      throw_invalid("points must be finite");
+    }
   });
 }
 
@@ -344,6 +360,10 @@ int pgpu_evaluator_set_target_points(pgpu_evaluator* ev, const double* points, i
     ev->n_trg = n;
     ev->e64.reset();
     ev->e32.reset();
+    if (!device_all_finite(ev->trg.data(), 3 * n)) {
+      ev->n_trg = 0;
+      throw_invalid("points must be finite");
+    }
   });
 }
 
@@ -357,6 +377,10 @@ int pgpu_evaluator_set_points(pgpu_evaluator* ev, const double* points, int64_t 
     ev->e64.reset();
     ev->e32.reset();
     ev->weights_set = false;
+    if (!device_all_finite(ev->src.data(), 3 * n)) {
+      ev->n_src = ev->n_trg = 0;
+      throw_invalid("points must be finite");
+    }
   });
 }
 
@@ -434,6 +458,37 @@ int pgpu_fit_batch(const pgpu_model* model, int precision, pgpu_fit_problem* pro
 }
 
 // ---- interpolant ----------------------------------------------------------------------
+
+int pgpu_krylov_fgmres_dense(int64_t n, const double* op, const double* pc, const double* rhs,
+                             const double* x0, int iters, double* solutions, double* rel_residuals) {
+  return guarded([&] {
+    check_ptr(op, "op");
+    check_ptr(rhs, "rhs");
+    if (iters > 0) {
+      check_ptr(solutions, "solutions");
+      check_ptr(rel_residuals, "rel_residuals");
+    }
+    krylov_fgmres_dense(n, op, pc, rhs, x0, iters, solutions, rel_residuals);
+  });
+}
+
+int pgpu_ras_domain_solve(const pgpu_model* model, const double* points, int64_t n,
+                          const int64_t* order, const unsigned char* inner, int coarse,
+                          int use_inverse, int precision, const double* rhs, double* out) {
+  return guarded([&] {
+    ModelDesc m = model_from_c(model);
+    if (n <= 0) throw_invalid("n must be positive");
+    check_ptr(points, "points");
+    check_ptr(order, "order");
+    check_ptr(inner, "inner");
+    check_ptr(rhs, "rhs");
+    check_ptr(out, "out");
+    if (precision != PGPU_PRECISION_PLAIN && precision != PGPU_PRECISION_MIXED)
+      throw_invalid("unknown precision");
+    ras_domain_solve(m, points, n, order, inner, coarse != 0, use_inverse != 0,
+                     precision == PGPU_PRECISION_MIXED, rhs, out);
+  });
+}
 
 int pgpu_interpolant_create(const pgpu_model* model, pgpu_interpolant** out) {
   return guarded([&] {
@@ -561,6 +616,8 @@ int pgpu_interpolant_fit(pgpu_interpolant* it, const double* points, int64_t mu,
     it->stats.setup_seconds = r.setup_seconds;
     it->stats.solve_seconds = r.solve_seconds;
     it->stats.n_domains = r.n_domains;
+    it->stats.precision_used = r.precision_used;
+    it->stats.fell_back = r.fell_back ? 1 : 0;
     it->fitted = true;
     it->eval_ready = false;
   });

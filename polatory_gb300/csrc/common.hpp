@@ -50,6 +50,12 @@ struct Error : std::runtime_error {
 cudaStream_t stream();
 void set_stream(cudaStream_t s);
 
+// Host-side fault injection of this thread (pgpu_debug_inject): the after-th next dev_alloc
+// throws PGPU_OUT_OF_MEMORY; the next tensor-core M2L launch stalls one stage and polls its wait
+// at most `polls` times (take_m2l_stall returns and clears the count).
+void inject_alloc_failure(int64_t after);
+void inject_m2l_stall(int64_t polls);
+int64_t take_m2l_stall();
 // Device memory from the stream-ordered pool of the current device.
 void* dev_alloc(size_t bytes);
 void dev_free(void* p, size_t bytes);

@@ -89,6 +89,26 @@ void transformed_bbox(const Bbox3& b, const double* a, double* tmin, double* tma
 
 }  // namespace
 
+namespace {
+__global__ void nonfinite_kernel(const double* __restrict__ p, Index n, int* __restrict__ flag) {
+  bool bad = false;
+  for (Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<Index>(gridDim.x) * blockDim.x)
+    bad |= !isfinite(p[i]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(flag, 1);
+}
+}  // namespace
+
+bool device_all_finite(const double* p, Index n) {
+  if (n <= 0) return true;
+  DevBuf<int> flag(1);
+  flag.zero();
+  const int nblk = static_cast<int>(std::min<Index>(blocks_for(n, 256), 4 * num_sms()));
+  nonfinite_kernel<<<nblk, 256, 0, stream()>>>(p, n, flag.data());
+  PGPU_LAUNCH_CHECK();
+  return flag.to_host()[0] == 0;
+}
+
 Bbox3 bbox_of_device_points(const double* pts, Index n) {
   Bbox3 b;
   if (n == 0) return b;

@@ -41,6 +41,8 @@ struct Bbox3 {
 
 // Bounding box of device points (x y z rows).
 Bbox3 bbox_of_device_points(const double* pts, Index n);
+// True when every one of the n device values is finite (one reduction and a sync).
+bool device_all_finite(const double* p, Index n);
 
 // FMM / direct configuration selected from an accuracy (fmm_accuracy_estimator.hpp:74-121).
 struct FarFieldConfig {

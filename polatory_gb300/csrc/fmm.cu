@@ -1658,7 +1658,10 @@ struct Fmm<T>::Impl {
         int e = 0;
         PGPU_CUDA(cudaMemcpyAsync(&e, tc_err.data(), sizeof(int), cudaMemcpyDeviceToHost, st));
         sync();
-        if (e != 0) throw Error(PGPU_RUNTIME_ERROR, "tensor-core M2L: a wait timed out");
+        if (e != 0) {
+          tc_err.zero();  // the next evaluation starts with a clear flag
+          throw Error(PGPU_TIMEOUT, "tensor-core M2L: a bounded wait ran out");
+        }
       }
     }
     const Index ntl = tt.ncell[lf];

@@ -385,4 +385,23 @@ void poly_eval_add(int degree, const double* c_host, const double* pts, Index mu
   PGPU_LAUNCH_CHECK();
 }
 
+namespace {
+__global__ void dense_gemv_kernel(const double* __restrict__ a, Index n, const double* __restrict__ x,
+                                  double* __restrict__ y) {
+  const Index row = (static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  double s = 0;
+  for (Index j = lane; j < n; j += 32) s += a[row * n + j] * x[j];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) y[row] = s;
+}
+}  // namespace
+
+void dense_gemv(const double* A, Index n, const double* x, double* y) {
+  if (n <= 0) return;
+  dense_gemv_kernel<<<blocks_for(32 * n, 256), 256, 0, stream()>>>(A, n, x, y);
+  PGPU_LAUNCH_CHECK();
+}
+
 }  // namespace pgpu

@@ -12,6 +12,8 @@ void multi_dot(const double* V, Index ld, int k, const double* w, Index n, doubl
 double multi_axpy_sub_norm2(const double* V, Index ld, int k, const double* h, double* w, Index n);
 // x += sum_i y[i] Z_i.
 void multi_axpy(const double* Z, Index ld, int k, const double* y, double* x, Index n);
+// y = A x for a dense row-major n x n matrix (one warp per row).
+void dense_gemv(const double* A, Index n, const double* x, double* y);
 // Generic helpers.
 double dot(const double* x, const double* y, Index n);
 double norm2(const double* x, Index n);

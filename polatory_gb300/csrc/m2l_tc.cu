@@ -83,9 +83,11 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait: about two seconds at most.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (int it = 0; it < (1 << 21); ++it) {
+// Bounded wait: `limit` polls of at least 256 ns (the default limit, 2^21, is about two
+// seconds at most).
+constexpr int kWaitPolls = 1 << 21;
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int limit) {
+  for (int it = 0; it < limit; ++it) {
     if (mbar_try(bar, parity)) return true;
     __nanosleep(256);
   }
@@ -185,7 +187,8 @@ __device__ __host__ __forceinline__ int core_off(int row, int k) {
 __global__ void __launch_bounds__(256, 1)
     m2l_tc_kernel(const float* __restrict__ kb_hi, const float* __restrict__ kb_lo,
                   const int* __restrict__ table, Index nt, const float* __restrict__ Ms,
-                  float* __restrict__ L, float* __restrict__ part, int* __restrict__ err) {
+                  float* __restrict__ L, float* __restrict__ part, int* __restrict__ err,
+                  int stall_polls) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
@@ -202,6 +205,10 @@ __global__ void __launch_bounds__(256, 1)
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
+  // Fault injection (host knob): the first CTA leaves the operator copy of its first stage
+  // unissued and gives up on that wait after stall_polls polls.
+  const bool stall = stall_polls > 0 && blockIdx.x == 0 && blockIdx.y == 0;
+  const int limit = stall ? stall_polls : kWaitPolls;
   const Index t0 = static_cast<Index>(blockIdx.x) * kCells;
   // Gather role: thread tid loads row tid % 128, k-groups 2 (tid / 128) and 2 (tid / 128) + 1.
   const int g_row = tid & 127;
@@ -270,7 +277,7 @@ __global__ void __launch_bounds__(256, 1)
   // Adds the accumulator of offset q (complete once acc_bar fires) into the running sums.
   auto drain = [&](int q) {
     const int b = q & 1;
-    if (!mbar_wait(acc_bar(b), (q >> 1) & 1)) {
+    if (!mbar_wait(acc_bar(b), (q >> 1) & 1, limit)) {
       ok = false;
       return;
     }
@@ -296,11 +303,15 @@ __global__ void __launch_bounds__(256, 1)
   // Issues the loads of iteration i into stage i % kStages. Loads are issued in iteration
   // order, so the source cell of the row is looked up once per offset (at its first chunk).
   int src = -1;
+  // Thread 0's bookkeeping of the operator copies: issued up to `issued`, seen complete up to
+  // `consumed` (an aborted CTA waits for the ones in between before it exits).
+  int issued = -1, consumed = -1;
   auto load = [&](int i) {
     const int s = i % kStages;
     const int o = olist[q_beg + i / kChunks];
     const int c = i % kChunks;
-    if (tid == 0) {
+    issued = i;
+    if (tid == 0 && !(stall && i == 0)) {
       mbar_expect_tx(load_bar(s), 2 * kBBytes);
       const size_t blk = (static_cast<size_t>(o) * kChunks + c) * kBFloats;
       bulk_g2s(smem_u32(b_hi(s)), kb_hi + blk, kBBytes, load_bar(s));
@@ -327,7 +338,7 @@ __global__ void __launch_bounds__(256, 1)
     if (i + 1 < n_iter) {
       const int s1 = (i + 1) % kStages;
       // Stage s1 was last read by the MMAs of iteration i + 1 - kStages.
-      if (i + 1 >= kStages && !mbar_wait(free_bar(s1), ((i + 1) / kStages - 1) & 1)) ok = false;
+      if (i + 1 >= kStages && !mbar_wait(free_bar(s1), ((i + 1) / kStages - 1) & 1, limit)) ok = false;
       load(i + 1);
       cp_async_wait<1>();
     } else {
@@ -351,9 +362,10 @@ __global__ void __launch_bounds__(256, 1)
     __syncthreads();
     if (misc[1] != 0) break;
     if (tid == 0) {
-      if (!mbar_wait(load_bar(s), (i / kStages) & 1)) {
+      if (!mbar_wait(load_bar(s), (i / kStages) & 1, limit)) {
         atomicExch(reinterpret_cast<int*>(&misc[1]), 1);
       } else {
+        consumed = i;
         tc_fence_after();
         const uint32_t d = tmem + static_cast<uint32_t>((q & 1) * 256);
         const uint32_t ah = smem_u32(a_hi(s)), al = smem_u32(a_lo(s));
@@ -374,13 +386,19 @@ __global__ void __launch_bounds__(256, 1)
   cp_async_wait<0>();
   __syncthreads();
   bool aborted = misc[1] != 0;
+  if (aborted && tid == 0) {
+    // Operator copies still in flight land before the CTA's shared memory is released (at most
+    // three: the loads run at most two iterations ahead of the MMAs).
+    for (int j = consumed + 1; j <= issued; ++j)
+      if (!(stall && j == 0)) mbar_wait(load_bar(j % kStages), (j / kStages) & 1, kWaitPolls);
+  }
   if (!aborted) {
     drain(n_off - 1);
     if (!ok) atomicExch(reinterpret_cast<int*>(&misc[1]), 1);
   }
   // Drain every MMA still in flight before TMEM is freed.
   if (tid == 0) mma_commit(smem_u32(&bars[2 * kStages + 2]));
-  const bool drained = mbar_wait(smem_u32(&bars[2 * kStages + 2]), 0);
+  const bool drained = mbar_wait(smem_u32(&bars[2 * kStages + 2]), 0, kWaitPolls);
   __syncthreads();
   aborted = misc[1] != 0 || !drained;
   if (tid == 0 && aborted) atomicExch(err, 1);
@@ -472,8 +490,9 @@ void m2l_tc_apply(const M2LTcBlocks& b, const int* table, Index nt, const float*
       std::min<Index>(16, std::max<Index>(1, (2 * num_sms() + tiles - 1) / tiles)));
   DevBuf<float> part;
   if (groups > 1) part.resize(static_cast<size_t>(groups) * nt * kD);
+  const int stall_polls = static_cast<int>(std::min<int64_t>(take_m2l_stall(), kWaitPolls));
   m2l_tc_kernel<<<dim3(static_cast<unsigned>(tiles), groups), 256, kSmemLaunch, st>>>(
-      b.hi.data(), b.lo.data(), table, nt, Ms, L, part.data(), err);
+      b.hi.data(), b.lo.data(), table, nt, Ms, L, part.data(), err, stall_polls);
   PGPU_LAUNCH_CHECK();
   if (groups > 1) {
     const Index n = nt * kD;

@@ -15,7 +15,12 @@
 // All calls share the array and each call overwrites it, so calls whose kernels may overlap on
 // the GPU (different streams, or different host threads on one device) race: callers must
 // serialise them. The device address of the array is looked up once per device on the first
-// call made with that device current.
+// call made with that device current (make that first call before any stream capture) and kept
+// for the life of the process: after cudaDeviceReset, or any teardown of the device's primary
+// context, the kept address is stale and the entry point must not be called again.
+// The entry point works on the caller's current device (cudaGetDevice), not on the device that
+// pgpu_set_device selected for the library's other calls, and every pointer must be device memory
+// of that device (or managed memory).
 #include <mutex>
 
 #include "common.hpp"
@@ -101,13 +106,15 @@ __global__ void noalloc_reduce_kernel(const double* __restrict__ part, int npart
   out[i] = s;
 }
 
-bool device_ptr(const void* p) {
+// Device memory of device `dev`, or managed memory.
+bool device_ptr(const void* p, int dev) {
   cudaPointerAttributes attr;
   if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+  if (attr.type == cudaMemoryTypeManaged) return true;
+  return attr.type == cudaMemoryTypeDevice && attr.device == dev;
 }
 
 }  // namespace
@@ -133,8 +140,15 @@ int direct_evaluate_noalloc(const pgpu_rbf* rbf, const double* src, int64_t ns,
     *msg = "points, weights and out must not be null";
     return PGPU_INVALID_ARGUMENT;
   }
-  if (!device_ptr(out) || !device_ptr(trg) || (ns > 0 && (!device_ptr(src) || !device_ptr(weights)))) {
-    *msg = "the allocation-free entry point takes device pointers only";
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    *msg = "cudaGetDevice failed";
+    return PGPU_CUDA_ERROR;
+  }
+  if (!device_ptr(out, dev) || !device_ptr(trg, dev) ||
+      (ns > 0 && (!device_ptr(src, dev) || !device_ptr(weights, dev)))) {
+    *msg = "the allocation-free entry point takes device pointers of the current device only";
     return PGPU_INVALID_ARGUMENT;
   }
   int err = 0;
@@ -145,9 +159,12 @@ int direct_evaluate_noalloc(const pgpu_rbf* rbf, const double* src, int64_t ns,
   }
   // Source chunks: as many as the scratch holds (and the GPU needs), at most 1024.
   const int bx = blocks_for(nt, kThreads);
-  int sms = 0, dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    *msg = "cudaDeviceGetAttribute failed";
+    return PGPU_CUDA_ERROR;
+  }
   Index chunks = 1;
   if (bx < 4 * sms && ns > 0) chunks = (4 * sms + bx - 1) / bx;
   chunks = std::min<Index>(chunks, std::max<Index>(1, kNoAllocScratch / nt));

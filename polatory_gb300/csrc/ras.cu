@@ -1094,43 +1094,7 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
 
   // Device-side per-point data.
   const int l = l_;
-  if (l > 0) {
-    DevBuf<double> coeffs;
-    coeffs.upload(lagrange_coeffs_);
-    lagrange_.resize(mu_ * l);
-    lagrange_kernel<<<blocks_for(mu_, 256), 256, 0, stream()>>>(model_.poly_degree, l, points_dev,
-                                                                mu_, coeffs.data(), lagrange_.data());
-    PGPU_LAUNCH_CHECK();
-    // A11 on the host (l x l, nugget on the diagonal).
-    a11_.assign(l * l, 0.0);
-    for (int i = 0; i < l; ++i)
-      for (int j = 0; j < l; ++j) {
-        const double* x = points_host + 3 * poly_idcs_[i];
-        const double* y = points_host + 3 * poly_idcs_[j];
-        double s = (i == j) ? model_.nugget : 0.0;
-        for (const auto& rb : model_.rbfs) {
-          double dd[3] = {x[0] - y[0], x[1] - y[1], x[2] - y[2]};
-          double t[3];
-          for (int r = 0; r < 3; ++r) t[r] = rb.a[3 * r] * dd[0] + rb.a[3 * r + 1] * dd[1] + rb.a[3 * r + 2] * dd[2];
-          KParams<double> kp{rb.p[0], rb.p[1]};
-          s += dispatch_kind(rb.kind, [&]<int K>() { return rbf_value<K>(t[0] * t[0] + t[1] * t[1] + t[2] * t[2], kp); });
-        }
-        a11_[i * l + j] = s;
-      }
-    std::vector<double> pp;
-    for (auto i : poly_idcs_)
-      for (int k = 0; k < 3; ++k) pp.push_back(points_host[3 * i + k]);
-    DevBuf<double> dpp, da11;
-    dpp.upload(pp);
-    da11.upload(a11_);
-    u_.resize(mu_ * l);
-    v_.resize(mu_ * l);
-    uv_kernel<<<blocks_for(mu_, 128), 128, 0, stream()>>>(rbf_set(model_), points_dev, mu_, dpp.data(),
-                                                          l, da11.data(), lagrange_.data(), u_.data(),
-                                                          v_.data());
-    PGPU_LAUNCH_CHECK();
-    sync();
-  }
+  setup_polynomial(points_host, points_dev);
 
   if (host_division) {
     for (int level = n_levels_ - 1; level >= 1; --level) {
@@ -1237,6 +1201,102 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
   work_fit_.resize(mu_);
   work_src_w_.resize(mu_ + l);
   sync();
+}
+
+template <class T>
+void RasPreconditioner<T>::setup_polynomial(const double* points_host, const double* points_dev) {
+  const int l = l_;
+  if (l > 0) {
+    DevBuf<double> coeffs;
+    coeffs.upload(lagrange_coeffs_);
+    lagrange_.resize(mu_ * l);
+    lagrange_kernel<<<blocks_for(mu_, 256), 256, 0, stream()>>>(model_.poly_degree, l, points_dev,
+                                                                mu_, coeffs.data(), lagrange_.data());
+    PGPU_LAUNCH_CHECK();
+    // A11 on the host (l x l, nugget on the diagonal).
+    a11_.assign(l * l, 0.0);
+    for (int i = 0; i < l; ++i)
+      for (int j = 0; j < l; ++j) {
+        const double* x = points_host + 3 * poly_idcs_[i];
+        const double* y = points_host + 3 * poly_idcs_[j];
+        double s = (i == j) ? model_.nugget : 0.0;
+        for (const auto& rb : model_.rbfs) {
+          double dd[3] = {x[0] - y[0], x[1] - y[1], x[2] - y[2]};
+          double t[3];
+          for (int r = 0; r < 3; ++r) t[r] = rb.a[3 * r] * dd[0] + rb.a[3 * r + 1] * dd[1] + rb.a[3 * r + 2] * dd[2];
+          KParams<double> kp{rb.p[0], rb.p[1]};
+          s += dispatch_kind(rb.kind, [&]<int K>() { return rbf_value<K>(t[0] * t[0] + t[1] * t[1] + t[2] * t[2], kp); });
+        }
+        a11_[i * l + j] = s;
+      }
+    std::vector<double> pp;
+    for (auto i : poly_idcs_)
+      for (int k = 0; k < 3; ++k) pp.push_back(points_host[3 * i + k]);
+    DevBuf<double> dpp, da11;
+    dpp.upload(pp);
+    da11.upload(a11_);
+    u_.resize(mu_ * l);
+    v_.resize(mu_ * l);
+    uv_kernel<<<blocks_for(mu_, 128), 128, 0, stream()>>>(rbf_set(model_), points_dev, mu_, dpp.data(),
+                                                          l, da11.data(), lagrange_.data(), u_.data(),
+                                                          v_.data());
+    PGPU_LAUNCH_CHECK();
+    sync();
+  }
+}
+
+// A preconditioner over one domain holding all points (the reference's FineGrid / CoarseGrid
+// unit tests, test/preconditioner/test_fine_grid.cpp and test_coarse_grid.cpp): level 1 is that
+// domain as a fine-grid domain with the given inner flags, level 0 the same points as the coarse
+// grid. The first l entries of `order` are the polynomial points.
+template <class T>
+RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* points_host,
+                                        const double* points_dev, Index mu,
+                                        const std::vector<Index>& order,
+                                        const std::vector<char>& inner, bool coarse_inverse)
+    : model_(model), l_(model.l()), mu_(mu), n_levels_(2),
+      bbox_(Bbox3::from_host_points(points_host, mu)), points_dev_(points_dev) {
+  if (static_cast<Index>(order.size()) != mu || static_cast<Index>(inner.size()) != mu)
+    throw_invalid("order and inner must have one entry per point");
+  if (mu < l_) throw_invalid("too few points for the polynomial degree");
+  point_idcs_.resize(2);
+  fine_.resize(2);
+  poly_idcs_.assign(order.begin(), order.begin() + l_);
+  if (l_ > 0) {
+    std::vector<double> pp;
+    for (auto i : poly_idcs_)
+      for (int k = 0; k < 3; ++k) pp.push_back(points_host[3 * i + k]);
+    lagrange_coeffs_ = lagrange_coeffs(model_.poly_degree, pp.data(), l_);
+  }
+  setup_polynomial(points_host, points_dev);
+  Domain d;
+  d.point_indices = order;
+  d.inner_point = inner;
+  fine_[1] = std::make_unique<DomainBatch<T>>();
+  build_batch(*fine_[1], std::vector<Domain>{d});
+  Domain cd;
+  cd.point_indices = order;
+  cd.inner_point.assign(mu, 1);
+  build_batch(coarse_, std::vector<Domain>{cd});
+  coarse_n_ = std::max(static_cast<int>(mu) - l_, 0);
+  use_coarse_inverse_ = coarse_inverse && coarse_n_ > 0;
+  if (use_coarse_inverse_) {
+    const int cld = std::max(NB, ((coarse_n_ + NB - 1) / NB) * NB);
+    coarse_inv_.resize(static_cast<Index>(coarse_n_) * coarse_n_);
+    chol_inverse_kernel<double><<<coarse_n_, 256, cld * sizeof(double), stream()>>>(
+        coarse_.mats.data(), cld, coarse_n_, coarse_inv_.data());
+    PGPU_LAUNCH_CHECK();
+  }
+  coarse_x_.resize(std::max(coarse_n_, 1));
+  coarse_g_.resize(std::max(coarse_n_, 1));
+  coarse_out_.resize(48);
+  coarse_out_.zero();
+  sync();
+}
+
+template <class T>
+void RasPreconditioner<T>::solve_domain(bool coarse, const double* residuals, double* weights) {
+  solve_level(coarse ? 0 : 1, residuals, weights);
 }
 
 template <class T>
@@ -1529,7 +1589,37 @@ void RasPreconditioner<T>::apply(const double* v, double* out) {
   }
 }
 
+template <class T>
+static void ras_domain_solve_t(const ModelDesc& model, const double* points, Index n,
+                               const std::vector<Index>& order, const std::vector<char>& inner,
+                               bool coarse, bool use_inverse, const double* rhs, double* out) {
+  DevBuf<double> pts, r, w;
+  pts.upload(points, static_cast<size_t>(3 * n));
+  r.upload(rhs, n);
+  w.resize(n + model.l());
+  RasPreconditioner<T> ras(model, points, pts.data(), n, order, inner, use_inverse);
+  ras.solve_domain(coarse, r.data(), w.data());
+  w.download(out, n + model.l());
+  sync();
+}
+
 template class RasPreconditioner<double>;
 template class RasPreconditioner<float>;
+
+void ras_domain_solve(const ModelDesc& model, const double* points, Index n, const Index* order,
+                      const unsigned char* inner, bool coarse, bool use_inverse, bool mixed,
+                      const double* rhs, double* out) {
+  std::vector<Index> ord(order, order + n);
+  std::vector<char> seen(n, 0);
+  for (Index i : ord) {
+    if (i < 0 || i >= n || seen[i]) throw_invalid("order must be a permutation of 0 .. n-1");
+    seen[i] = 1;
+  }
+  std::vector<char> inn(inner, inner + n);
+  if (mixed)
+    ras_domain_solve_t<float>(model, points, n, ord, inn, coarse, use_inverse, rhs, out);
+  else
+    ras_domain_solve_t<double>(model, points, n, ord, inn, coarse, use_inverse, rhs, out);
+}
 
 }  // namespace pgpu

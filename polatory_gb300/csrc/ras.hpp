@@ -40,7 +40,16 @@ class RasPreconditioner {
   // points_host / points_dev: the mu data points (xyz rows). Value points only.
   RasPreconditioner(const ModelDesc& model, const double* points_host, const double* points_dev,
                     Index mu, const Bbox3& bbox);
+  // One domain holding all points, for the component tests of the fine and coarse grids:
+  // `order` lists the points (the first l are the polynomial points), `inner` the fine-grid
+  // inner flags per entry of `order`; coarse_inverse keeps the coarse grid as an explicit inverse.
+  RasPreconditioner(const ModelDesc& model, const double* points_host, const double* points_dev,
+                    Index mu, const std::vector<Index>& order, const std::vector<char>& inner,
+                    bool coarse_inverse);
   ~RasPreconditioner();
+  // Solves the test domain as the coarse grid (weights of every point and the polynomial
+  // coefficients) or as a fine-grid domain (weights of the inner points).
+  void solve_domain(bool coarse, const double* residuals, double* weights);
 
   // out (M) = RAS(v (M)), M = mu + l (ras_preconditioner.hpp:191-250).
   void apply(const double* v, double* out);
@@ -50,6 +59,7 @@ class RasPreconditioner {
   Index size() const { return mu_ + l_; }
 
  private:
+  void setup_polynomial(const double* points_host, const double* points_dev);
   void solve_level(int level, const double* residuals, double* weights);
   void update_residuals(int src_level, int trg_level, const double* weights, double* residuals);
   void orthogonalize(double* weights, double* residuals);
@@ -88,5 +98,13 @@ class RasPreconditioner {
   std::map<std::pair<int, int>, std::unique_ptr<Evaluator<T>>> evaluators_;
   DevBuf<double> work_res_, work_w_, work_tot_, work_src_w_, work_fit_;
 };
+
+// Component test of one RAS domain holding all n points (host buffers): `order` lists the
+// points with the l polynomial points first, `inner` the fine-grid inner flags; solves rhs as the
+// coarse grid (coarse, optionally through the explicit inverse) or as a fine-grid domain and
+// writes the n + l weights. FP64 factors, or FP32 factors when mixed.
+void ras_domain_solve(const ModelDesc& model, const double* points, Index n, const Index* order,
+                      const unsigned char* inner, bool coarse, bool use_inverse, bool mixed,
+                      const double* rhs, double* out);
 
 }  // namespace pgpu

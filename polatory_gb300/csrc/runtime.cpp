@@ -64,11 +64,24 @@ void set_device(int device) {
 namespace {
 thread_local int64_t g_thread_bytes = 0;
 thread_local int64_t g_thread_peak = 0;
+// Host-side fault injection (pgpu_debug_inject): countdowns, 0 = off.
+thread_local int64_t g_fail_alloc_in = 0;
+thread_local int64_t g_m2l_stall_polls = 0;
 }  // namespace
+
+void inject_alloc_failure(int64_t after) { g_fail_alloc_in = after > 0 ? after : 0; }
+void inject_m2l_stall(int64_t polls) { g_m2l_stall_polls = polls > 0 ? polls : 0; }
+int64_t take_m2l_stall() {
+  const int64_t p = g_m2l_stall_polls;
+  g_m2l_stall_polls = 0;
+  return p;
+}
 
 void* dev_alloc(size_t bytes) {
   void* p = nullptr;
   if (bytes == 0) return nullptr;
+  if (g_fail_alloc_in > 0 && --g_fail_alloc_in == 0)
+    throw Error(PGPU_OUT_OF_MEMORY, "out of device memory (injected allocation failure)");
   PGPU_CUDA(cudaMallocAsync(&p, bytes, stream()));
   g_thread_bytes += static_cast<int64_t>(bytes);
   if (g_thread_bytes > g_thread_peak) g_thread_peak = g_thread_bytes;

@@ -631,37 +631,93 @@ void evaluate_impl(const EvaluateRequest& req) {
 
 }  // namespace
 
+namespace {
+// Inputs must be finite: a NaN or infinite coordinate would poison the bounding box, the octree
+// keys and the domain division (the reference does not check; here they are rejected).
+void check_finite_host(const double* p, Index n, const char* what) {
+  for (Index i = 0; i < n; ++i)
+    if (!std::isfinite(p[i])) throw_invalid(std::string(what) + " must be finite");
+}
+}  // namespace
+
 FitResult fit(const FitRequest& req) {
   if (req.sigma > 0) throw Error(PGPU_NOT_IMPLEMENTED, "gradient data points are not supported yet");
+  check_finite_host(req.points_host, 3 * req.mu, "points");
+  check_finite_host(req.values_host, req.mu + 3 * req.sigma, "values");
   const double mu = static_cast<double>(req.mu);
   FitRequest plain = req;
   plain.precision = PGPU_PRECISION_PLAIN;
   if (req.precision == PGPU_PRECISION_PLAIN) return fit_impl<double>(plain);
+  auto mixed = [](FitResult r) {
+    r.precision_used = PGPU_PRECISION_MIXED;
+    return r;
+  };
   // Kernels of conditional positive definiteness order 2 and above (triharmonic, thin-plate)
   // give domain matrices too ill-conditioned for an FP32 Cholesky factor: their small fits keep
   // the FP64 preconditioner.
   FitRequest small = req;
   small.plain_loop = true;
-  if (!mixed_pays(mu, mu) && req.model->cpd_order() >= 2) return fit_impl<double>(small);
+  if (!mixed_pays(mu, mu) && req.model->cpd_order() >= 2) return mixed(fit_impl<double>(small));
   try {
     if (!mixed_pays(mu, mu)) {
       // Small systems: FP64-class operator and residuals (direct sums), FP32 preconditioner.
-      return fit_impl<float>(small);
+      return mixed(fit_impl<float>(small));
     }
-    return fit_impl<float>(req);
+    return mixed(fit_impl<float>(req));
   } catch (const NonFinite&) {
     if (req.verbose) std::printf("fit: non-finite value in FP32, running the FP64 path\n");
-    return fit_impl<double>(plain);
+    FitResult r = fit_impl<double>(plain);
+    r.fell_back = true;
+    return r;
   }
 }
 
 void evaluate(const EvaluateRequest& req) {
+  if (!device_all_finite(req.points_dev, 3 * req.m) ||
+      !device_all_finite(req.grad_points_dev, 3 * req.mg))
+    throw_invalid("points must be finite");
   const double pairs_src = static_cast<double>(req.mu + req.sigma);
   const double pairs_trg = static_cast<double>(req.m + req.mg);
   if (req.precision == PGPU_PRECISION_PLAIN || !mixed_pays(pairs_src, pairs_trg))
     evaluate_impl<double>(req);
   else
     evaluate_impl<float>(req);
+}
+
+namespace {
+struct DenseOperator {
+  const double* a;
+  Index n;
+  void apply(const double* x, double* y) { dense_gemv(a, n, x, y); }
+};
+struct IdentityOperator {
+  Index n;
+  void apply(const double* x, double* y) { copy(y, x, n); }
+};
+}  // namespace
+
+void krylov_fgmres_dense(Index n, const double* op, const double* pc, const double* rhs,
+                         const double* x0, int iters, double* solutions, double* rel_residuals) {
+  if (n <= 0 || iters < 0 || iters > n) throw_invalid("need n > 0 and 0 <= iters <= n");
+  DevBuf<double> a, p, b, x0d, x(n);
+  a.upload(op, static_cast<size_t>(n * n));
+  b.upload(rhs, n);
+  if (pc) p.upload(pc, static_cast<size_t>(n * n));
+  if (x0) x0d.upload(x0, n);
+  DenseOperator A{a.data(), n}, P{p.data(), n};
+  IdentityOperator I{n};
+  Fgmres g(n, iters);
+  g.setup(b.data(), x0 ? x0d.data() : nullptr, x0 == nullptr, A);
+  for (int k = 0; k < iters; ++k) {
+    if (pc)
+      g.iterate(A, P);
+    else
+      g.iterate(A, I);
+    g.solution(x.data());
+    x.download(solutions + static_cast<Index>(k) * n, n);
+    sync();
+    rel_residuals[k] = g.relative_residual();
+  }
 }
 
 }  // namespace pgpu

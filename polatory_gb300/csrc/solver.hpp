@@ -21,6 +21,8 @@ struct FitResult {
   double setup_seconds = 0;
   double solve_seconds = 0;
   Index n_domains = 0;
+  int precision_used = PGPU_PRECISION_PLAIN;  // arithmetic of the solve that produced the weights
+  bool fell_back = false;                     // a mixed solve met a non-finite FP32 value
 };
 
 struct FitRequest {
@@ -64,5 +66,12 @@ struct EvaluateRequest {
 };
 
 void evaluate(const EvaluateRequest& req);
+
+// Component test of the device FGMRES on a dense n x n operator (host buffers, row-major), with
+// an optional dense right preconditioner and initial solution (null: identity / zero): after
+// iteration k the solution estimate goes to solutions[k n ..] and the relative residual
+// estimate to rel_residuals[k].
+void krylov_fgmres_dense(Index n, const double* op, const double* pc, const double* rhs,
+                         const double* x0, int iters, double* solutions, double* rel_residuals);
 
 }  // namespace pgpu

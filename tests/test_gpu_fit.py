@@ -244,3 +244,44 @@ def test_device_division_equals_host_division(monkeypatch, kind):
     assert s_dev["n_domains"] == s_host["n_domains"]
     assert s_dev["iterations"] == s_host["iterations"]
     np.testing.assert_array_equal(w_dev, w_host)
+
+
+def test_c3_kriging_tenth_scale_mixed_vs_plain():
+    # The kriging configuration at a tenth of its size: 50,000 Gaussian-mixture points,
+    # cov_exponential (range 0.2, anisotropy 1:1:0.5, nugget 1e-3), degree 0, tol 1e-4, 1M
+    # uniform queries. The mixed interpolant is within 1e-4 of the plain FP64 one at every query,
+    # and the mixed weights meet the tolerance at sampled data points, recomputed by the oracle.
+    pts, vals, q, aniso = workloads.c3(n=50_000, n_eval=1_000_000)
+    rbf = pg.CovExponential([1.0, 0.2])
+    rbf.anisotropy = aniso
+    model = pg.Model(rbf, 0)
+    model.nugget = 1e-3
+    tol = 1e-4
+    mixed = pg.Interpolant(model, pg.MIXED)
+    mixed.fit(pts, vals, tol)
+    assert mixed.fit_stats["precision_used"] == pg.MIXED and mixed.fit_stats["fell_back"] == 0
+    plain = pg.Interpolant(model, pg.PLAIN)
+    plain.fit(pts, vals, tol)
+    assert np.max(np.abs(mixed.evaluate(q) - plain.evaluate(q))) <= 1e-4
+    g = np.random.Generator(np.random.PCG64(51))
+    idx = g.choice(pts.shape[0], 3000, replace=False)
+    w = mixed.weights
+    fit_vals = oracle.direct_evaluate(model, pts, w, pts[idx]) + model.nugget * w[idx]
+    assert np.max(np.abs(fit_vals - vals[idx])) <= tol
+
+
+def test_c4_size_batched_fits_against_oracle():
+    # 64 fits drawn like the batched configuration (N log-uniform in [200, 20000], triharmonic,
+    # degree 1, tol 1e-5, 4,096 queries each): every residual at every data point and every
+    # evaluation, recomputed by the oracle.
+    fits = workloads.c4(n_fits=64)
+    model = pg.Model(pg.Triharmonic3D([1.0]), 1)
+    tol = 1e-5
+    res = pg.fit_batch(model, fits, tol, precision=pg.MIXED)
+    assert max(p.shape[0] for p, _, _ in fits) > 10_000
+    for (p, v, q), r in zip(fits, res):
+        assert r["status"] == 0
+        w = r["weights"]
+        assert np.max(np.abs(oracle.direct_evaluate(model, p, w, p) - v)) <= tol
+        want = oracle.direct_evaluate(model, p, w, q)
+        assert np.max(np.abs(r["values"] - want)) <= 1e-8 * max(1.0, np.max(np.abs(want)))

@@ -61,6 +61,22 @@ def test_noalloc_matches_regular_entry_point_twice(cls, params):
         assert np.max(np.abs(got - want)) <= 1e-12 * scale, call
 
 
+def test_noalloc_ragged_and_edge_sizes():
+    """Target counts that split unevenly over the source chunks, a call at the 2,097,152-target
+    limit (one chunk, the whole array in use) and a call without sources (all zeros)."""
+    rbf = pg.Biharmonic3D([1.0])
+    src, w, trg = _inputs(7, 100_003, 1_001)
+    want = _regular(rbf, src, w, trg)
+    got = _noalloc(rbf, src, w, trg)
+    assert np.max(np.abs(got - want)) <= 1e-12 * np.abs(w).sum()
+    src, w, trg = _inputs(8, 37, 1 << 21)
+    want = _regular(rbf, src, w, trg)
+    got = _noalloc(rbf, src, w, trg)
+    assert np.max(np.abs(got - want)) <= 1e-12 * np.abs(w).sum()
+    got = _noalloc(rbf, np.zeros((0, 3)), np.zeros(0), trg[:5000])
+    assert np.all(got == 0.0)
+
+
 def test_noalloc_rejects_oversized_calls():
     import torch
 
