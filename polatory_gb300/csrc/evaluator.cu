@@ -192,8 +192,14 @@ __global__ void gather_p4_kernel(const P4<double>* __restrict__ src, const Index
 // 10,000 of the source points (a default-seeded std::mt19937 shuffle) are the sample targets;
 // their exact FP64 sums are compared with the FMM at increasing orders (4, 6, 8 here; the
 // reference's uniform interpolation tries 8 to 20), and the first order whose inf-norm error is
-// within the accuracy is kept. None: "failed to construct an evaluator that meets the desired
-// accuracy".
+// within the accuracy is kept. Where no order here meets it (an accuracy the reference reaches
+// at orders 10-20), the evaluator falls back to exact direct sums (returns -1) as long as they
+// stay below kExactFallbackPairs source-target pairs; beyond that the reference's error is
+// raised: "failed to construct an evaluator that meets the desired accuracy".
+// Exact sums as the fallback of a finite accuracy: up to 2^42 pairs (about a minute of FP64
+// sums on this GPU).
+constexpr double kExactFallbackPairs = 4398046511104.0;
+
 template <class T>
 int Evaluator<T>::estimate_order(Term& t, double accuracy) {
   const Index ns = std::min<Index>(mu_, 10000);
@@ -229,6 +235,8 @@ int Evaluator<T>::estimate_order(Term& t, double accuracy) {
     if (verbose()) std::printf("fmm accuracy estimate: order %d error %.3e (target %.3e)\n", p, err, accuracy);
     if (err <= accuracy) return p;
   }
+  const double pairs = static_cast<double>(mu_ + sigma_) * static_cast<double>(m_ + mg_);
+  if (pairs <= kExactFallbackPairs) return -1;
   throw Error(PGPU_RUNTIME_ERROR, "failed to construct an evaluator that meets the desired accuracy");
 }
 
@@ -340,7 +348,17 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
     const bool fmm_ok = Fmm<T>::supported(t.rbf.kind) && sigma_ == 0 && mg_ == 0;
     bool use_fmm = fmm_ok && (backend_ == kBackendFmm ||
                               (backend_ == kBackendAuto && pairs > direct_pair_limit<T>()));
-    const bool fp64_near = sizeof(T) == 4 && near64_ && sigma_ == 0 && mg_ == 0;
+    // A finite accuracy picks the far-field order (or exact sums, order -1) from the estimate.
+    const double acc = std::min(accuracy_, grad_accuracy_);
+    const double term_acc = acc / static_cast<double>(terms_.size());
+    const bool order_free = !ff_set_ || ff_.order == 0;
+    if (use_fmm && order_free && std::isfinite(acc) && acc > 0.0 && t.order == 0) {
+      t.order = estimate_order(t, term_acc);
+      t.fmm.reset();
+    }
+    const bool exact = use_fmm && order_free && t.order < 0;
+    if (exact) use_fmm = false;
+    const bool fp64_near = sizeof(T) == 4 && (near64_ || exact) && sigma_ == 0 && mg_ == 0;
     const bool values_only = sigma_ == 0 && mg_ == 0;
     if (!use_fmm && fp64_near) {
       if (!direct_evaluate_ff(t.rbf.kind, t.kp64, t.spos_d.data(), w_, mu_, t.tpos_d.data(), m_,
@@ -350,7 +368,7 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
         direct_evaluate<double>(t.rbf.kind, t.kp64, t.a, src, trg, stream());
       }
       stats_.direct_pairs += static_cast<Index>(pairs);
-    } else if (!use_fmm && sizeof(T) == 8 && ff_direct_ && values_only &&
+    } else if (!use_fmm && sizeof(T) == 8 && (ff_direct_ || exact) && values_only &&
                direct_evaluate_ff(t.rbf.kind, t.kp64, t.spos_d.data(), w_, mu_, t.tpos_d.data(),
                                   m_, out_v, stream())) {
       stats_.direct_pairs += static_cast<Index>(pairs);
@@ -360,14 +378,7 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
       direct_evaluate<T>(t.rbf.kind, t.kp, t.a, src, trg, stream());
       stats_.direct_pairs += static_cast<Index>(pairs);
     } else {
-      double acc = std::min(accuracy_, grad_accuracy_);
-      // Accuracy split over the RBFs (interpolation/operator.hpp:88-90).
-      const double term_acc = acc / static_cast<double>(terms_.size());
-      const bool order_free = !ff_set_ || ff_.order == 0;
-      if (order_free && std::isfinite(acc) && acc > 0.0 && t.order == 0) {
-        t.order = estimate_order(t, term_acc);
-        t.fmm.reset();
-      }
+      // Accuracy split over the RBFs (interpolation/operator.hpp:88-90): term_acc above.
       if (!t.fmm) {
         double rel_min[3];
         for (int k = 0; k < 3; ++k) rel_min[k] = t.box_min[k] - t.origin[k];

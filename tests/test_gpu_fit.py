@@ -249,8 +249,11 @@ def test_device_division_equals_host_division(monkeypatch, kind):
 def test_c3_kriging_tenth_scale_mixed_vs_plain():
     # The kriging configuration at a tenth of its size: 50,000 Gaussian-mixture points,
     # cov_exponential (range 0.2, anisotropy 1:1:0.5, nugget 1e-3), degree 0, tol 1e-4, 1M
-    # uniform queries. The mixed interpolant is within 1e-4 of the plain FP64 one at every query,
-    # and the mixed weights meet the tolerance at sampled data points, recomputed by the oracle.
+    # uniform queries. At the default evaluation accuracy (infinity: order 6) the far field of
+    # either arithmetic is off the exact sums by ~1e-3 for these weights, so the interpolants are
+    # compared with evaluations at accuracy 1e-6 (the estimator's order, or exact sums): the
+    # mixed interpolant is within 1e-4 of the plain FP64 one at every query, and the mixed
+    # weights meet the tolerance at sampled data points, recomputed by the oracle.
     pts, vals, q, aniso = workloads.c3(n=50_000, n_eval=1_000_000)
     rbf = pg.CovExponential([1.0, 0.2])
     rbf.anisotropy = aniso
@@ -262,12 +265,36 @@ def test_c3_kriging_tenth_scale_mixed_vs_plain():
     assert mixed.fit_stats["precision_used"] == pg.MIXED and mixed.fit_stats["fell_back"] == 0
     plain = pg.Interpolant(model, pg.PLAIN)
     plain.fit(pts, vals, tol)
-    assert np.max(np.abs(mixed.evaluate(q) - plain.evaluate(q))) <= 1e-4
+    got = mixed.evaluate(q, accuracy=1e-6)
+    want = plain.evaluate(q, accuracy=1e-6)
+    assert np.max(np.abs(got - want)) <= 1e-4
     g = np.random.Generator(np.random.PCG64(51))
     idx = g.choice(pts.shape[0], 3000, replace=False)
     w = mixed.weights
     fit_vals = oracle.direct_evaluate(model, pts, w, pts[idx]) + model.nugget * w[idx]
     assert np.max(np.abs(fit_vals - vals[idx])) <= tol
+    sub = q[g.choice(q.shape[0], 2000, replace=False)]
+    exact = oracle.direct_evaluate(model, pts, w, sub)
+    assert np.max(np.abs(mixed.evaluate(sub, accuracy=1e-6) - exact)) <= 1e-6
+
+
+def test_evaluation_at_tight_accuracy_bh3():
+    # A finite accuracy below what the far-field orders here reach falls back to exact sums
+    # instead of failing (the reference reaches it with orders up to 20): accuracy 1e-8 on a
+    # 30,000-point biharmonic interpolant at 400,000 queries, checked against the oracle.
+    g = np.random.Generator(np.random.PCG64(52))
+    pts = g.random((30_000, 3))
+    vals = workloads.f_c1(pts)
+    model = pg.Model(pg.Biharmonic3D([1.0]), 1)
+    it = pg.Interpolant(model)
+    it.fit(pts, vals, 1e-6)
+    q = g.random((400_000, 3))
+    got = it.evaluate(q, accuracy=1e-8)
+    sub = g.choice(q.shape[0], 2000, replace=False)
+    want = oracle.direct_evaluate(model, pts, it.weights, q[sub])
+    assert np.max(np.abs(got[sub] - want)) <= 1e-8
+    # The same at the default accuracy (order 6) is allowed a larger error.
+    assert np.max(np.abs(it.evaluate(q[sub]) - want)) <= 1e-4
 
 
 def test_c4_size_batched_fits_against_oracle():
