@@ -637,7 +637,7 @@ __global__ void chunk_fill_kernel(const int* __restrict__ cnt, const int* __rest
   }
 }
 template <int KIND, class T>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 12)
     p2p_kernel(KParams<T> kp, const P4<T>* __restrict__ tpos, const Index* __restrict__ tperm,
                const Index* __restrict__ tleaf_start, const int* __restrict__ chunk_leaf,
                const int* __restrict__ table, const P4<T>* __restrict__ spos,
@@ -655,17 +655,24 @@ __global__ void __launch_bounds__(128)
   __syncthreads();
   const Index tb = tleaf_start[leaf] + static_cast<Index>(chunk_leaf[2 * blockIdx.x + 1]) * kP2PChunk;
   const Index te = min(tleaf_start[leaf + 1], tb + kP2PChunk);
-  // NT targets per thread (1 or 2, uniform over the block): each source read from shared memory
-  // serves NT targets.
+  // NT targets per thread (1 or 2, uniform over the block), consecutive: thread t takes targets
+  // i0 + NT t .. + NT - 1, so that the threads without targets fill whole warps, which skip the
+  // sums. Each source read from shared memory serves NT targets. Weights are staged pre-scaled
+  // by the kernel's constant factor where the kernel has one (pair_term).
+  const T wscale = pair_weight_scale<KIND>(kp);
+  const T c2 = pair_r2_offset<KIND>(kp);
   auto pass = [&]<int NT>(Index i0) {
     P4<T> t[NT];
     bool active[NT];
+    bool any = false;
 #pragma unroll
     for (int q = 0; q < NT; ++q) {
-      const Index i = i0 + threadIdx.x + q * blockDim.x;
+      const Index i = i0 + NT * threadIdx.x + q;
       active[q] = i < te;
+      any |= active[q];
       t[q] = active[q] ? tpos[i] : P4<T>{T(0), T(0), T(0), T(0)};
     }
+    const bool warp_busy = __any_sync(0xffffffffu, any);
     double tot[NT];
 #pragma unroll
     for (int q = 0; q < NT; ++q) tot[q] = 0;
@@ -688,10 +695,11 @@ __global__ void __launch_bounds__(128)
         __syncthreads();
         if (threadIdx.x < cnt) {
           P4<T> p = spos[base + threadIdx.x];
-          p.w = sw[base + threadIdx.x];
+          p.w = sw[base + threadIdx.x] * wscale;
           s_p[threadIdx.x] = p;
         }
         __syncthreads();
+        if (!warp_busy) continue;
         T acc[NT];
 #pragma unroll
         for (int q = 0; q < NT; ++q) acc[q] = T(0);
@@ -699,10 +707,8 @@ __global__ void __launch_bounds__(128)
         for (int j = 0; j < cnt; ++j) {
           const P4<T> s4 = s_p[j];
 #pragma unroll
-          for (int q = 0; q < NT; ++q) {
-            const T dx = tx[q] - s4.x, dy = ty[q] - s4.y, dz = tz[q] - s4.z;
-            acc[q] += rbf_value_fast<KIND>(dx * dx + dy * dy + dz * dz, kp) * s4.w;
-          }
+          for (int q = 0; q < NT; ++q)
+            acc[q] = pair_term<KIND>(tx[q] - s4.x, ty[q] - s4.y, tz[q] - s4.z, s4.w, c2, kp, acc[q]);
         }
 #pragma unroll
         for (int q = 0; q < NT; ++q) tot[q] += static_cast<double>(acc[q]);
@@ -710,7 +716,7 @@ __global__ void __launch_bounds__(128)
     }
 #pragma unroll
     for (int q = 0; q < NT; ++q)
-      if (active[q]) out[tperm[i0 + threadIdx.x + q * blockDim.x]] += tot[q];
+      if (active[q]) out[tperm[i0 + NT * threadIdx.x + q]] += tot[q];
   };
   for (Index i0 = tb; i0 < te;) {
     if (te - i0 > static_cast<Index>(blockDim.x)) {
@@ -748,6 +754,8 @@ __global__ void __launch_bounds__(128)
     const Index i = i0 + threadIdx.x;
     const bool active = i < te;
     const P4<double> t = active ? tpos[i] : P4<double>{0.0, 0.0, 0.0, 0.0};
+    // Warps past the leaf's last target (the tail of a leaf) only help stage the sources.
+    const bool warp_busy = __any_sync(0xffffffffu, active);
     double tot = 0.0;
     for (int nb = 0; nb < 27; ++nb) {
       const int s = s_nb[nb];
@@ -768,6 +776,7 @@ __global__ void __launch_bounds__(128)
           ff_split(sw[base + threadIdx.x], s_p[6][threadIdx.x], s_p[7][threadIdx.x]);
         }
         __syncthreads();
+        if (!warp_busy) continue;
         float ah = 0.0f, al = 0.0f;
 #pragma unroll 2
         for (int j = 0; j < cnt; ++j)
@@ -796,6 +805,8 @@ __global__ void __launch_bounds__(128)
   if (i >= nt) return;
   const P4<T> t = tpos[i];
   const int* nbs = table + static_cast<Index>(tleaf[i]) * 27;
+  const T wscale = pair_weight_scale<KIND>(kp);
+  const T c2 = pair_r2_offset<KIND>(kp);
   double tot = 0.0;
   for (int nb = 0; nb < 27; ++nb) {
     const int s = nbs[nb];
@@ -807,8 +818,7 @@ __global__ void __launch_bounds__(128)
     T acc = T(0);
     for (Index j = sb; j < se; ++j) {
       const P4<T> q = spos[j];
-      const T dx = tx - q.x, dy = ty - q.y, dz = tz - q.z;
-      acc += rbf_value_fast<KIND>(dx * dx + dy * dy + dz * dz, kp) * sw[j];
+      acc = pair_term<KIND>(tx - q.x, ty - q.y, tz - q.z, sw[j] * wscale, c2, kp, acc);
     }
     tot += static_cast<double>(acc);
   }

@@ -190,6 +190,36 @@ template <int KIND>
 __device__ __forceinline__ double rbf_value_fast(double r2, const KParams<double>& kp) {
   return rbf_value<KIND>(r2, kp);
 }
+
+// Near-field pair term acc + w' phi(d) with the kernel's constant factor folded into the staged
+// weight w' = w * pair_weight_scale and, for the odd polyharmonic kernels in FP32, the
+// regularisation p1^2 (plus 1e-30, which keeps rsqrt finite at d = 0 and is below the rounding
+// of any nonzero squared distance of leaf-sized coordinates) folded into the first FMA of r^2:
+//   bh3: -p0 rho = w' rho with w' = -p0 w;  th3: p0 rho^3 = w' rho^3 with w' = p0 w,
+// rho = rho2 * rsqrt(rho2). Other kernels: rbf_value_fast(r^2) * w.
+template <int KIND, class T>
+__device__ __forceinline__ T pair_weight_scale(const KParams<T>& kp) {
+  if constexpr (sizeof(T) == 4 && KIND == PGPU_RBF_BH3) return -kp.p0;
+  else if constexpr (sizeof(T) == 4 && KIND == PGPU_RBF_TH3) return kp.p0;
+  else return T(1);
+}
+template <int KIND, class T>
+__device__ __forceinline__ T pair_r2_offset(const KParams<T>& kp) {
+  if constexpr (sizeof(T) == 4 && (KIND == PGPU_RBF_BH3 || KIND == PGPU_RBF_TH3))
+    return kp.p1 * kp.p1 + 1e-30f;
+  else return T(0);
+}
+template <int KIND, class T>
+__device__ __forceinline__ T pair_term(T dx, T dy, T dz, T w, T c2, const KParams<T>& kp, T acc) {
+  if constexpr (sizeof(T) == 4 && (KIND == PGPU_RBF_BH3 || KIND == PGPU_RBF_TH3)) {
+    const T rho2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, c2)));
+    const T rho = rho2 * rsqrtf(rho2);
+    if constexpr (KIND == PGPU_RBF_BH3) return fmaf(w, rho, acc);
+    else return fmaf(w, rho2 * rho, acc);
+  } else {
+    return acc + rbf_value_fast<KIND>(dx * dx + dy * dy + dz * dz, kp) * w;
+  }
+}
 #endif
 
 // ---- gradient coefficient: grad = gcoef * d ---------------------------------------------
