@@ -28,6 +28,7 @@
 
 #include "common.hpp"
 #include "m2l_tc.hpp"
+#include "tcgen05.cuh"
 #include "profile.hpp"
 
 namespace pgpu {
@@ -58,131 +59,12 @@ constexpr int kSmemMask = kSmemList + 4 * kNOffsets;           // offset bitmask
 constexpr int kSmemTotal = kSmemMask + 4 * 12;
 constexpr int kSmemLaunch = kSmemTotal + 1024;                 // room to align the base
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
+using namespace tc;
 
-__device__ __forceinline__ float tf32_round(float x) {
-  uint32_t u = __float_as_uint(x);
-  u = (u + 0x1000u) & 0xFFFFE000u;
-  return __uint_as_float(u);
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait: `limit` polls of at least 256 ns (the default limit, 2^21, is about two
-// seconds at most).
-constexpr int kWaitPolls = 1 << 21;
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int limit) {
-  for (int it = 0; it < limit; ++it) {
-    if (mbar_try(bar, parity)) return true;
-    __nanosleep(256);
-  }
-  return false;
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
-                                         uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          dst),
-      "l"(src), "r"(bytes), "r"(bar)
-      : "memory");
-}
-
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src),
-               "r"(src_bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-
-__device__ __forceinline__ void tc_fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-
-// Shared-memory matrix descriptor: no swizzle, K-major, LBO 128 B, SBO 512 B.
-__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= static_cast<uint64_t>((saddr >> 4) & 0x3FFFu);
-  d |= static_cast<uint64_t>(128u >> 4) << 16;
-  d |= static_cast<uint64_t>(512u >> 4) << 32;
-  d |= static_cast<uint64_t>(1u) << 46;  // descriptor version
-  return d;                              // base offset 0, layout type 0 (no swizzle)
-}
-
-// Instruction descriptor: kind::tf32, FP32 accumulate, A and B K-major, M = 128, N = 224.
-constexpr uint32_t kIdesc = (1u << 4)             // D format F32
-                            | (2u << 7)           // A format TF32
-                            | (2u << 10)          // B format TF32
-                            | ((kN >> 3) << 17)   // N / 8
-                            | ((128u >> 4) << 24);  // M / 16
+constexpr uint32_t kIdesc = idesc_tf32(128, kN);  // M = 128, N = 224
 
 __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
-      : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-      : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
-      "%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
-}
-
-// Offset of element (row, k) of a 128-row-tile chunk in the core-matrix layout (floats).
-__device__ __host__ __forceinline__ int core_off(int row, int k) {
-  return (row >> 3) * 128 + (k >> 2) * 32 + (row & 7) * 4 + (k & 3);
+  tc::mma_tf32(tmem_d, a, b, kIdesc, acc);
 }
 
 // Warp roles (384 threads, 12 warps: three per SM sub-partition, which leaves each thread up to

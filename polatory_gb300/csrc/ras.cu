@@ -23,6 +23,7 @@
 #include "profile.hpp"
 #include "ras.hpp"
 #include "ras_divide.hpp"
+#include "tcgen05.cuh"
 
 namespace pgpu {
 
@@ -507,6 +508,182 @@ __global__ void __launch_bounds__(256, 2)
   }
 }
 
+// The same trailing update on the tensor cores (tcgen05, kind::tf32): each 128 x 128 tile of
+// the trailing matrix is one M = 128, N = 128 accumulator in TMEM, C(i, j) -= A B^T with A the
+// tile's 128 rows and B its 128 columns of the group's panels (B = A on diagonal tiles). FP32
+// accuracy from TF32 head/tail splits of both operands: A B ~ Ah Bh + Ah Bl + Al Bh.
+// Pipeline per 16-column chunk: the raw panel columns (rows contiguous) stream into shared
+// memory by cp.async one chunk ahead (two raw stages); each thread then splits its row of the
+// chunk into head and tail in the MMA's K-major core-matrix layout (two operand stages, each
+// released by the commit of its MMAs), and one thread issues the MMAs. The epilogue reads the
+// accumulator (warp w: TMEM lanes 32 w .. + 31, its rows) and subtracts it from the tile in
+// global memory (coalesced per column). Rows past the domain load zeros; a diagonal tile writes
+// its 32-blocks on and below the diagonal only. Every wait is bounded; a wait that runs out
+// sets *err and the block finishes its MMAs in flight, frees its TMEM and returns without
+// writing.
+constexpr int kTcRaw = 2;                              // raw chunk stages
+constexpr int kTcOps = 2;                              // operand (head/tail) stages
+constexpr int kTcChunkFloats = kTile * kChunk;         // 2048 floats: 8 KB
+constexpr int kTcRawFloats = 2 * kTcChunkFloats;       // A and B columns of one chunk
+constexpr int kTcOpFloats = 4 * kTcChunkFloats;        // A head, A tail, B head, B tail
+constexpr size_t kTcDataBytes =
+    (static_cast<size_t>(kTcRaw) * kTcRawFloats + static_cast<size_t>(kTcOps) * kTcOpFloats) * sizeof(float);
+constexpr size_t kSyrkTcSmem = kTcDataBytes + 64 + 1024;  // barriers, TMEM address, alignment
+constexpr uint32_t kSyrkIdesc = tc::idesc_tf32(128, 128);
+
+__global__ void __launch_bounds__(128, 2)
+    syrk_tc_kernel(int kb0, int np, const int* __restrict__ lds, const Index* __restrict__ mat_off,
+                   float* __restrict__ mats, int* __restrict__ err) {
+  const Index d = blockIdx.y;
+  const int ld = lds[d];
+  const int first = (kb0 + np) * NB;
+  if (first >= ld) return;
+  const int nt = (ld - first + kTile - 1) / kTile;
+  if (static_cast<Index>(blockIdx.x) >= static_cast<Index>(nt) * (nt + 1) / 2) return;
+  int ti, tj;
+  tile_of(blockIdx.x, ti, tj);
+  const int r0 = first + ti * kTile, c0 = first + tj * kTile;
+  const bool diag = ti == tj;
+  float* mat = mats + mat_off[d];
+  const float* panel = mat + static_cast<Index>(kb0 * NB) * ld;
+  extern __shared__ unsigned char syrk_tc_smem[];
+  unsigned char* base = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(syrk_tc_smem) + 1023) & ~static_cast<uintptr_t>(1023));
+  float* ops = reinterpret_cast<float*>(base);         // [kTcOps][4][128 x 16] core-matrix layout
+  float* raw = ops + kTcOps * kTcOpFloats;              // [kTcRaw][A|B][16 k][128 rows]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + kTcDataBytes);
+  uint32_t* misc = reinterpret_cast<uint32_t*>(bars + kTcOps + 1);
+  auto op_bar = [&](int s) { return tc::smem_u32(&bars[s]); };
+  const uint32_t final_bar = tc::smem_u32(&bars[kTcOps]);
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+
+  if (tid == 0) {
+    for (int s = 0; s <= kTcOps; ++s) tc::mbar_init(tc::smem_u32(&bars[s]), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     tc::smem_u32(&misc[0])),
+                 "r"(128)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = misc[0];
+
+  // Raw copy of chunk kk: 16 columns x 128 rows of A (and of B off the diagonal), 16 B pieces.
+  const int nk = np * NB / kChunk;
+  auto load_raw = [&](int kk) {
+    float* dst = raw + (kk % kTcRaw) * kTcRawFloats;
+    const int kc = kk * kChunk;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int idx = tid + 128 * e;  // 0 .. 1023: operand, column, four rows
+      const int which = idx >> 9, w = idx & 511, k = w >> 5, r4 = (w & 31) * 4;
+      if (which == 1 && diag) continue;
+      const int row = (which ? c0 : r0) + r4;
+      const bool have = row < ld;
+      const float* src = have ? panel + static_cast<Index>(kc + k) * ld + row : panel;
+      tc::cp_async16(tc::smem_u32(dst + which * kTcChunkFloats + k * kTile + r4), src,
+                     have ? 16u : 0u);
+    }
+    tc::cp_async_commit();
+  };
+
+  bool ok = true;
+  load_raw(0);
+  for (int kk = 0; kk < nk; ++kk) {
+    if (kk + 1 < nk) load_raw(kk + 1);
+    else tc::cp_async_commit();
+    tc::cp_async_wait<1>();  // chunk kk has landed
+    const int s = kk % kTcOps;
+    // The operand stage's previous MMAs (chunk kk - kTcOps) have read it.
+    const bool waited = kk < kTcOps ||
+                        tc::mbar_wait(op_bar(s), ((kk / kTcOps) - 1) & 1, tc::kWaitPolls);
+    if (__syncthreads_or(!waited)) {
+      ok = false;
+      break;
+    }
+    float* a_hi = ops + s * kTcOpFloats;
+    float* a_lo = a_hi + kTcChunkFloats;
+    float* b_hi = diag ? a_hi : a_lo + kTcChunkFloats;
+    float* b_lo = diag ? a_lo : b_hi + kTcChunkFloats;
+    const float* rc = raw + (kk % kTcRaw) * kTcRawFloats;
+#pragma unroll
+    for (int op = 0; op < 2; ++op) {
+      if (op == 1 && diag) break;
+      const float* col = rc + op * kTcChunkFloats + tid;
+      float* hi = op ? b_hi : a_hi;
+      float* lo = op ? b_lo : a_lo;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float x0 = col[(4 * j) * kTile], x1 = col[(4 * j + 1) * kTile];
+        const float x2 = col[(4 * j + 2) * kTile], x3 = col[(4 * j + 3) * kTile];
+        const float4 h{tc::tf32_round(x0), tc::tf32_round(x1), tc::tf32_round(x2), tc::tf32_round(x3)};
+        const int off = tc::core_off(tid, 4 * j);
+        *reinterpret_cast<float4*>(hi + off) = h;
+        *reinterpret_cast<float4*>(lo + off) = float4{x0 - h.x, x1 - h.y, x2 - h.z, x3 - h.w};
+      }
+    }
+    tc::fence_proxy_async();
+    __syncthreads();  // operands written; the raw stage of chunk kk may be refilled
+    if (tid == 0) {
+      tc::tc_fence_after();
+      const uint32_t ah = tc::smem_u32(a_hi), al = tc::smem_u32(a_lo);
+      const uint32_t bh = tc::smem_u32(b_hi), bl = tc::smem_u32(b_lo);
+#pragma unroll
+      for (int ks = 0; ks < 2; ++ks) {
+        const uint32_t ko = static_cast<uint32_t>(ks * 256);
+        tc::mma_tf32(tmem, tc::make_desc(ah + ko), tc::make_desc(bh + ko), kSyrkIdesc,
+                     (kk == 0 && ks == 0) ? 0u : 1u);
+        tc::mma_tf32(tmem, tc::make_desc(ah + ko), tc::make_desc(bl + ko), kSyrkIdesc, 1u);
+        tc::mma_tf32(tmem, tc::make_desc(al + ko), tc::make_desc(bh + ko), kSyrkIdesc, 1u);
+      }
+      tc::mma_commit(op_bar(s));
+    }
+  }
+  tc::cp_async_wait<0>();
+  // All MMAs complete before the accumulator is read or TMEM is freed.
+  if (tid == 0) tc::mma_commit(final_bar);
+  const bool done = tc::mbar_wait(final_bar, 0, tc::kWaitPolls);
+  if (__syncthreads_or(!done)) ok = false;
+  if (!ok) {
+    if (tid == 0) atomicExch(err, 1);
+  } else {
+    tc::tc_fence_after();
+    const int row = r0 + 32 * warp + lane;
+#pragma unroll 1
+    for (int u = 0; u < kTile / 32; ++u) {
+      float v[32];
+      tc::tmem_ld16(tmem + (static_cast<uint32_t>(32 * warp) << 16) + static_cast<uint32_t>(32 * u), v);
+      tc::tmem_ld16(tmem + (static_cast<uint32_t>(32 * warp) << 16) + static_cast<uint32_t>(32 * u + 16),
+                    v + 16);
+      if (row < ld) {
+        float cur[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int c = c0 + 32 * u + j;
+          cur[j] = (c < ld && c / NB <= row / NB) ? mat[row + static_cast<Index>(c) * ld] : 0.0f;
+        }
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int c = c0 + 32 * u + j;
+          if (c < ld && c / NB <= row / NB) mat[row + static_cast<Index>(c) * ld] = cur[j] - v[j];
+        }
+      }
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128)
+                 : "memory");
+  }
+}
+
 // FP32 left-looking update of one block column inside a panel group: C(i, j) -= sum over the
 // group's panels [kb0, kb0 + np) of L(i, k) L(j, k) for the 32 columns of block column
 // kb0 + np and every row from that block down. 128-row tiles, 256 threads with 4 x 4 outputs
@@ -941,6 +1118,15 @@ __global__ void __launch_bounds__(256, 4) ras_solve_kernel(const int* __restrict
     if (coarse || din[l + i]) weights[dp[l + i]] = x[i];
   for (int k = tid; k < l; k += blockDim.x)
     if (coarse || din[k]) weights[dp[k]] = dh[k];
+}
+
+// PGPU_SYRK_TC=0 in the environment keeps the FP32 trailing updates on the CUDA cores.
+bool syrk_tc_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("PGPU_SYRK_TC");
+    return e == nullptr || std::atoi(e) != 0;
+  }();
+  return on;
 }
 
 RbfSet rbf_set(const ModelDesc& m) {
@@ -1405,6 +1591,7 @@ void RasPreconditioner<T>::build_batch(DomainBatch<U>& b, const std::vector<Inde
     PGPU_LAUNCH_CHECK();
   }
 
+  DevBuf<int> tc_err;  // timeout flag of the tensor-core trailing updates
   // Blocked Cholesky over all domains, in groups of kGroup panels: inside a group each panel is
   // updated left-looking by the group's earlier panels, factored and solved below; then one
   // trailing update applies the whole group.
@@ -1436,7 +1623,22 @@ void RasPreconditioner<T>::build_batch(DomainBatch<U>& b, const std::vector<Inde
     }
     const int rem = nbmax - g0 - np;
     if (rem <= 0) continue;
-    if (std::is_same_v<U, float> && nd <= 65535) {
+    if (std::is_same_v<U, float> && nd <= 65535 && syrk_tc_enabled()) {
+      const int nt = (rem * NB + kTile - 1) / kTile;
+      dim3 gs(static_cast<unsigned>(nt * (nt + 1) / 2), nd);
+      static std::once_flag attr_flag;
+      std::call_once(attr_flag, [] {
+        PGPU_CUDA(cudaFuncSetAttribute(syrk_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(kSyrkTcSmem)));
+      });
+      if (tc_err.size() == 0) {
+        tc_err.resize(1);
+        tc_err.zero();
+      }
+      syrk_tc_kernel<<<gs, 128, kSyrkTcSmem, stream()>>>(
+          g0, np, b.ld.data(), b.mat_off.data(), reinterpret_cast<float*>(b.mats.data()),
+          tc_err.data());
+    } else if (std::is_same_v<U, float> && nd <= 65535) {
       const int nt = (rem * NB + kTile - 1) / kTile;
       dim3 gs(static_cast<unsigned>(nt * (nt + 1) / 2), nd);
       syrk128_update_kernel<<<gs, 256, kSyrk128Smem, stream()>>>(
@@ -1452,6 +1654,12 @@ void RasPreconditioner<T>::build_batch(DomainBatch<U>& b, const std::vector<Inde
   invert_diag_kernel<U><<<dim3(static_cast<unsigned>(b.n_dom), nbmax), 32, 0, stream()>>>(
       b.ld.data(), b.mat_off.data(), b.mats.data());
   PGPU_LAUNCH_CHECK();
+  if (tc_err.size() > 0) {
+    int e = 0;
+    PGPU_CUDA(cudaMemcpyAsync(&e, tc_err.data(), sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    sync();
+    if (e != 0) throw Error(PGPU_TIMEOUT, "tensor-core Cholesky update: a bounded wait ran out");
+  }
 }
 
 template <class T>
