@@ -231,6 +231,15 @@ int pgpu_interpolant_evaluate(pgpu_interpolant* it, const double* points, int64_
  * last evaluate / set_evaluation_bbox. */
 int pgpu_interpolant_evaluate_impl(pgpu_interpolant* it, const double* points, int64_t m,
                                    const double* grad_points, int64_t mg, double* out);
+/* isosurface::RbfFieldFunction::operator() (isosurface/rbf_field_function.hpp:21-23) over the
+ * nodes of a lattice (isosurface/rmt/lattice.hpp:421-447, primitive_lattice.hpp:41-43): the
+ * node positions (lc_origin + lc) * basis (row vector times the row-major 3 x 3 basis, whose rows
+ * are the lattice vectors) are formed on the device from the n integer lattice coordinates lcs
+ * (n x 3, host or device), the interpolant is evaluated there through the evaluator of the last
+ * set_evaluation_bbox / evaluate (as evaluate_impl), and out (n) receives value - isovalue. */
+int pgpu_interpolant_evaluate_lattice(pgpu_interpolant* it, const double lc_origin[3],
+                                      const double basis[9], const int32_t* lcs, int64_t n,
+                                      double isovalue, double* out);
 /* Interpolant::set_evaluation_bbox_impl (interpolant.hpp:201-210). */
 int pgpu_interpolant_set_evaluation_bbox(pgpu_interpolant* it, const double bbox[6],
                                          double accuracy, double grad_accuracy);

@@ -292,6 +292,26 @@ class Interpolant:
             ptr(out)))
         return out
 
+    def evaluate_lattice(self, lc_origin, basis, lattice_coordinates, isovalue=0.0):
+        """isosurface::RbfFieldFunction over lattice nodes: value - isovalue at the positions
+        (lc_origin + lc) @ basis of the integer lattice coordinates (n x 3), formed on the device
+        (isosurface/rmt/primitive_lattice.hpp:41-43); uses the evaluation bbox of the last
+        set_evaluation_bbox / evaluate, like evaluate_impl."""
+        o = np.ascontiguousarray(np.asarray(lc_origin, dtype=np.float64).reshape(3))
+        b = np.ascontiguousarray(np.asarray(basis, dtype=np.float64).reshape(9))
+        lcs = np.ascontiguousarray(np.asarray(lattice_coordinates, dtype=np.int32).reshape(-1, 3))
+        out = np.empty(lcs.shape[0])
+        check(lib.pgpu_interpolant_evaluate_lattice(self._h, ptr(o), ptr(b),
+                                                    C.c_void_p(lcs.ctypes.data), lcs.shape[0],
+                                                    float(isovalue), ptr(out)))
+        return out
+
+    def set_evaluation_bbox(self, bbox_min, bbox_max, accuracy=INF, grad_accuracy=INF):
+        """Interpolant::set_evaluation_bbox_impl (interpolant.hpp:201-210)."""
+        b = np.ascontiguousarray(np.concatenate([np.asarray(bbox_min, dtype=np.float64).reshape(3),
+                                                 np.asarray(bbox_max, dtype=np.float64).reshape(3)]))
+        check(lib.pgpu_interpolant_set_evaluation_bbox(self._h, ptr(b), accuracy, grad_accuracy))
+
     @property
     def weights(self) -> np.ndarray:
         n = C.c_int64()

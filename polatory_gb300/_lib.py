@@ -129,6 +129,7 @@ def _load():
                                   C.c_double, C.c_double, P], C.c_int),
         "pgpu_interpolant_evaluate": ([P, P, I64, P, I64, C.c_double, C.c_double, P], C.c_int),
         "pgpu_interpolant_evaluate_impl": ([P, P, I64, P, I64, P], C.c_int),
+        "pgpu_interpolant_evaluate_lattice": ([P, P, P, P, I64, C.c_double, P], C.c_int),
         "pgpu_interpolant_set_evaluation_bbox": ([P, P, C.c_double, C.c_double], C.c_int),
         "pgpu_interpolant_is_fitted": ([P, C.POINTER(C.c_int)], C.c_int),
         "pgpu_interpolant_num_weights": ([P, C.POINTER(I64)], C.c_int),

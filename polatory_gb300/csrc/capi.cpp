@@ -710,6 +710,34 @@ int pgpu_interpolant_evaluate_impl(pgpu_interpolant* it, const double* points, i
   });
 }
 
+int pgpu_interpolant_evaluate_lattice(pgpu_interpolant* it, const double lc_origin[3],
+                                      const double basis[9], const int32_t* lcs, int64_t n,
+                                      double isovalue, double* out) {
+  return guarded([&] {
+    throw_if_not_fitted(it);
+    check_ptr(lc_origin, "lc_origin");
+    check_ptr(basis, "basis");
+    if (n < 0) throw_invalid("n must be non-negative");
+    if (n == 0) return;
+    check_ptr(lcs, "lcs");
+    check_ptr(out, "out");
+    DevBuf<int32_t> dl(static_cast<size_t>(3 * n));
+    const bool dev = is_device_pointer(lcs);
+    PGPU_CUDA(cudaMemcpyAsync(dl.data(), lcs, 3 * n * sizeof(int32_t),
+                              dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream()));
+    if (!dev) pgpu::sync();
+    DevBuf<double> pts(static_cast<size_t>(3 * n)), vals(static_cast<size_t>(n));
+    lattice_positions(lc_origin, basis, dl.data(), n, pts.data());
+    if (!it->eval_ready) {
+      it->eval_bbox = it->bbox;
+      it->eval_ready = true;
+    }
+    run_evaluate(it, pts.data(), n, nullptr, 0, vals.data());
+    subtract_scalar(vals.data(), n, isovalue);
+    copy_out(out, vals.data(), n);
+  });
+}
+
 int pgpu_interpolant_is_fitted(const pgpu_interpolant* it, int* out) {
   return guarded([&] {
     check_ptr(it, "interpolant");

@@ -99,6 +99,41 @@ __global__ void nonfinite_kernel(const double* __restrict__ p, Index n, int* __r
 }
 }  // namespace
 
+namespace {
+struct Basis9 {
+  double o[3], b[9];
+};
+__global__ void lattice_positions_kernel(Basis9 lb, const int32_t* __restrict__ lcs, Index n,
+                                         double* __restrict__ pts) {
+  const Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double a0 = lb.o[0] + lcs[3 * i], a1 = lb.o[1] + lcs[3 * i + 1], a2 = lb.o[2] + lcs[3 * i + 2];
+  for (int j = 0; j < 3; ++j)
+    pts[3 * i + j] = __dadd_rn(__dadd_rn(__dmul_rn(a0, lb.b[j]), __dmul_rn(a1, lb.b[3 + j])),
+                               __dmul_rn(a2, lb.b[6 + j]));
+}
+__global__ void subtract_scalar_kernel(double* __restrict__ x, Index n, double c) {
+  const Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) x[i] -= c;
+}
+}  // namespace
+
+void lattice_positions(const double lc_origin[3], const double basis[9], const int32_t* lcs, Index n,
+                       double* pts) {
+  if (n <= 0) return;
+  Basis9 lb;
+  for (int k = 0; k < 3; ++k) lb.o[k] = lc_origin[k];
+  for (int k = 0; k < 9; ++k) lb.b[k] = basis[k];
+  lattice_positions_kernel<<<blocks_for(n, 256), 256, 0, stream()>>>(lb, lcs, n, pts);
+  PGPU_LAUNCH_CHECK();
+}
+
+void subtract_scalar(double* x, Index n, double c) {
+  if (n <= 0) return;
+  subtract_scalar_kernel<<<blocks_for(n, 256), 256, 0, stream()>>>(x, n, c);
+  PGPU_LAUNCH_CHECK();
+}
+
 bool device_all_finite(const double* p, Index n) {
   if (n <= 0) return true;
   DevBuf<int> flag(1);

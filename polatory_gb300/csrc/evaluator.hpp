@@ -43,6 +43,11 @@ struct Bbox3 {
 Bbox3 bbox_of_device_points(const double* pts, Index n);
 // True when every one of the n device values is finite (one reduction and a sync).
 bool device_all_finite(const double* p, Index n);
+// Lattice node positions (lc_origin + lc) * basis for n device int32 triples (lcs), into pts (n x 3).
+void lattice_positions(const double lc_origin[3], const double basis[9], const int32_t* lcs, Index n,
+                       double* pts);
+// x[i] -= c on the device.
+void subtract_scalar(double* x, Index n, double c);
 
 // FMM / direct configuration selected from an accuracy (fmm_accuracy_estimator.hpp:74-121).
 struct FarFieldConfig {
