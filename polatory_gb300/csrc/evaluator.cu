@@ -178,6 +178,14 @@ struct Evaluator<T>::Term {
   bool fmm_targets_dirty = true;
   // Far-field order chosen for a finite accuracy (0: not chosen yet).
   int order = 0;
+  // Kernels of compact support (cub, sph) run a near-field-only tree of the kernel itself; the
+  // spheroidal kernels are split (src/fmm/spheroidal_evaluator.hpp:8-62) into a compact direct
+  // part (near-field-only tree) and a smooth fast part (full FMM). near_kind < 0: no split.
+  int near_kind = -1, far_kind = -1;
+  double near_radius = 0.0;  // support of the near part in the anisotropy frame
+  std::unique_ptr<Fmm<T>> fmm_near;
+  bool near_sources_dirty = true;
+  bool near_targets_dirty = true;
 };
 
 template <class T>
@@ -206,6 +214,14 @@ Evaluator<T>::Evaluator(const ModelDesc& model, const Bbox3& bbox, double accura
     t->box_width = w;
     t->kp = KParams<T>{static_cast<T>(r.p[0]), static_cast<T>(r.p[1])};
     t->kp64 = KParams<double>{r.p[0], r.p[1]};
+    if (r.kind == PGPU_RBF_CUB || r.kind == PGPU_RBF_SPH) {
+      t->near_kind = r.kind;
+      t->near_radius = r.p[1];
+    } else if (r.kind >= PGPU_RBF_SP3 && r.kind <= PGPU_RBF_SP9) {
+      t->near_kind = kKindSpDirect + (r.kind - PGPU_RBF_SP3);
+      t->far_kind = kKindSpFast + (r.kind - PGPU_RBF_SP3);
+      t->near_radius = spheroidal_const(r.kind).rho0 * r.p[1];
+    }
     terms_.push_back(std::move(t));
   }
 }
@@ -257,14 +273,29 @@ int Evaluator<T>::estimate_order(Term& t, double accuracy) {
   }
   double rel_min[3];
   for (int k = 0; k < 3; ++k) rel_min[k] = t.box_min[k] - t.origin[k];
+  // Split kernels: the compact direct part is exact (near-field sums); its values at the
+  // samples are added to the fast part's FMM at each order.
+  DevBuf<double> near_part(ns);
+  near_part.zero();
+  if (t.near_kind >= 0) {
+    Fmm<T> fn(t.near_kind, t.kp, t.a, rel_min, t.box_width, accuracy);
+    FarFieldConfig c;
+    c.near_only = true;
+    c.near_radius = t.near_radius;
+    fn.set_config(c);
+    fn.set_sources(t.spos_d.data(), mu_);
+    fn.set_targets(samp.data(), ns);
+    fn.evaluate(t.vw.data(), nullptr, w_, near_part.data(), nullptr);
+  }
+  const int far_kind = t.far_kind >= 0 ? t.far_kind : t.rbf.kind;
   for (int p : {4, 6, 8}) {
-    Fmm<T> f(t.rbf.kind, t.kp, t.a, rel_min, t.box_width, accuracy);
+    Fmm<T> f(far_kind, t.kp, t.a, rel_min, t.box_width, accuracy);
     FarFieldConfig c;
     c.order = p;
     f.set_config(c);
     f.set_sources(t.spos_d.data(), mu_);
     f.set_targets(samp.data(), ns);
-    approx.zero();
+    copy(approx.data(), near_part.data(), ns);
     f.evaluate(t.vw.data(), nullptr, w_, approx.data(), nullptr);
     const double err = inf_norm_diff(approx.data(), exact.data(), ns);
     if (verbose()) std::printf("fmm accuracy estimate: order %d error %.3e (target %.3e)\n", p, err, accuracy);
@@ -299,6 +330,7 @@ void Evaluator<T>::set_sources(const double* pts, Index mu, const double* gpts, 
     t->vw.resize(mu);
     t->gg.resize(3 * sigma);
     t->fmm_sources_dirty = true;
+    t->near_sources_dirty = true;
     t->order = 0;  // the accuracy estimate depends on the sources (and weights)
   }
 }
@@ -324,6 +356,7 @@ void Evaluator<T>::set_targets(const double* pts, Index m, const double* gpts, I
           gpts, mg, t->a, t->origin[0], t->origin[1], t->origin[2], t->tgpos.data());
     PGPU_LAUNCH_CHECK();
     t->fmm_targets_dirty = true;
+    t->near_targets_dirty = true;
   }
 }
 
@@ -380,14 +413,18 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
   const double pairs = static_cast<double>(mu_ + sigma_) * static_cast<double>(m_ + mg_);
   for (auto& tp : terms_) {
     Term& t = *tp;
-    const bool fmm_ok = Fmm<T>::supported(t.rbf.kind) && sigma_ == 0 && mg_ == 0;
+    // Split kernels need leaves at least as wide as the support with a level-2 tree or finer.
+    const bool split = t.near_kind >= 0;
+    const bool fmm_ok = sigma_ == 0 && mg_ == 0 &&
+                        (split ? 4.0 * t.near_radius <= t.box_width : Fmm<T>::supported(t.rbf.kind));
     bool use_fmm = fmm_ok && (backend_ == kBackendFmm ||
                               (backend_ == kBackendAuto && pairs > direct_pair_limit<T>()));
+    const bool has_far = !split || t.far_kind >= 0;
     // A finite accuracy picks the far-field order (or exact sums, order -1) from the estimate.
     const double acc = std::min(accuracy_, grad_accuracy_);
     const double term_acc = acc / static_cast<double>(terms_.size());
     const bool order_free = !ff_set_ || ff_.order == 0;
-    if (use_fmm && order_free && std::isfinite(acc) && acc > 0.0 && t.order == 0) {
+    if (use_fmm && has_far && order_free && std::isfinite(acc) && acc > 0.0 && t.order == 0) {
       t.order = estimate_order(t, term_acc);
       t.fmm.reset();
     }
@@ -413,11 +450,37 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
       direct_evaluate<T>(t.rbf.kind, t.kp, t.a, src, trg, stream());
       stats_.direct_pairs += static_cast<Index>(pairs);
     } else {
+      double rel_min[3];
+      for (int k = 0; k < 3; ++k) rel_min[k] = t.box_min[k] - t.origin[k];
+      if (split) {
+        // The compact part: exact sums over the 27 neighbour leaves of a near-field-only tree.
+        if (!t.fmm_near) {
+          t.fmm_near = std::make_unique<Fmm<T>>(t.near_kind, t.kp, t.a, rel_min, t.box_width, term_acc);
+          FarFieldConfig c;
+          c.near_only = true;
+          c.near_radius = t.near_radius;
+          t.fmm_near->set_config(c);
+          t.near_sources_dirty = t.near_targets_dirty = true;
+        }
+        if (t.near_sources_dirty || t.near_targets_dirty) {
+          if (symmetric_) {
+            t.fmm_near->set_points(t.spos_d.data(), mu_);
+          } else {
+            if (t.near_sources_dirty) t.fmm_near->set_sources(t.spos_d.data(), mu_);
+            if (t.near_targets_dirty) t.fmm_near->set_targets(t.tpos_d.data(), m_);
+          }
+          t.near_sources_dirty = t.near_targets_dirty = false;
+        }
+        t.fmm_near->set_near_fp64(fp64_near, t.kp64);
+        t.fmm_near->evaluate(t.vw.data(), t.gg.data(), w_, out_v, out_g);
+        stats_.near_pairs += t.fmm_near->near_pairs();
+        stats_.backend = 1;
+        if (!has_far) continue;
+      }
       // Accuracy split over the RBFs (interpolation/operator.hpp:88-90): term_acc above.
       if (!t.fmm) {
-        double rel_min[3];
-        for (int k = 0; k < 3; ++k) rel_min[k] = t.box_min[k] - t.origin[k];
-        t.fmm = std::make_unique<Fmm<T>>(t.rbf.kind, t.kp, t.a, rel_min, t.box_width, term_acc);
+        t.fmm = std::make_unique<Fmm<T>>(split ? t.far_kind : t.rbf.kind, t.kp, t.a, rel_min,
+                                         t.box_width, term_acc);
         if (ff_set_ || t.order > 0) {
           FarFieldConfig c = ff_set_ ? ff_ : FarFieldConfig{};
           if (order_free && t.order > 0) c.order = t.order;

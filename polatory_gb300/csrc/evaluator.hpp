@@ -53,6 +53,10 @@ void subtract_scalar(double* x, Index n, double c);
 struct FarFieldConfig {
   int order = 0;          // interpolation nodes per axis (0: from the accuracy)
   int leaf_level = -1;    // -1: automatic
+  // Near field only, for kernels of compact support: leaves at least near_radius wide (in the
+  // anisotropy frame), so that the 27 neighbour leaves hold every source within the support.
+  bool near_only = false;
+  double near_radius = 0.0;
 };
 
 struct EvalStats {

@@ -1023,7 +1023,7 @@ std::shared_ptr<DevBuf<T>> m2l_matrices(int kind, const KParams<T>& kp, double r
   for (int m = 0; m < p; ++m) nodes[m] = cheb_node(p, m);
   DevBuf<double> dn;
   dn.upload(nodes);
-  dispatch_kind(kind, [&]<int K>() {
+  dispatch_fmm_kind(kind, [&]<int K>() {
     m2l_matrix_kernel<K, T><<<4 * num_sms(), 256, 0, stream()>>>(kp, p, r, dn.data(), buf->data());
     return 0;
   });
@@ -1336,6 +1336,7 @@ struct Fmm<T>::Impl {
   const P4<double>* tpos_in = nullptr;
   Index ns = 0, nt = 0;
   int lf = 2;
+  bool near_only = false;  // compact support: near field only (FarFieldConfig::near_only)
   bool built = false;
   // M2L tables per level (target cells x 343) and P2P table (target leaves x 27).
   std::vector<DevBuf<int>> m2l_table;
@@ -1395,7 +1396,15 @@ struct Fmm<T>::Impl {
     SortedPoints ss, ts;
     sort_points(ss, spos_in, ns, box);
     if (!symmetric) sort_points(ts, tpos_in, nt, box);
-    lf = choose_leaf_level(occupancy(ss));
+    near_only = cfg_set && cfg.near_only;
+    if (near_only) {
+      // The finest level whose leaves are at least the support radius wide.
+      int k = 2;
+      while (k < kSortLevel && box.width / static_cast<double>(1 << (k + 1)) >= cfg.near_radius) ++k;
+      lf = k;
+    } else {
+      lf = choose_leaf_level(occupancy(ss));
+    }
     p = cfg_set && cfg.order > 0 ? cfg.order : order_for_accuracy(accuracy);
     if (p != 4 && p != 6 && p != 8) p = 6;
     ch = make_cheb<T>(p);
@@ -1408,7 +1417,7 @@ struct Fmm<T>::Impl {
     m2l_table.resize(lf + 1);
     m2l_pairs.assign(lf + 1, 0);
     kmats.assign(lf + 1, nullptr);
-    for (int k = 2; k <= lf; ++k) {
+    for (int k = 2; k <= (near_only ? 1 : lf); ++k) {
       const Index n_t = tt.ncell[k];
       m2l_table[k].resize(std::max<Index>(n_t, 1) * kNOff);
       PGPU_CUDA(cudaMemsetAsync(m2l_table[k].data(), 0xff, m2l_table[k].size() * sizeof(int), st));
@@ -1490,7 +1499,7 @@ struct Fmm<T>::Impl {
     Lt.clear();
     Mt.resize(lf + 1);
     Lt.resize(lf + 1);
-    for (int k = 2; k <= lf; ++k) {
+    for (int k = 2; k <= (near_only ? 1 : lf); ++k) {
       M[k].resize(std::max<Index>(src.ncell[k], 1) * p3);
       L[k].resize(std::max<Index>(tt.ncell[k], 1) * p3);
       if (kmats[k]->r > 0) {
@@ -1658,7 +1667,7 @@ struct Fmm<T>::Impl {
     const bool fp64_near = sizeof(T) == 4 && near64 && w64 != nullptr;
     gather_w_kernel<T><<<blocks_for(ns, 256), 256, 0, st>>>(vw, src.perm.data(), ns, sw.data());
     PGPU_LAUNCH_CHECK();
-    if (lf >= 2) {
+    if (lf >= 2 && !near_only) {
       switch (p) {
         case 4: run_far<4>(st, out); break;
         case 8: run_far<8>(st, out); break;
@@ -1696,7 +1705,7 @@ struct Fmm<T>::Impl {
         PGPU_LAUNCH_CHECK();
       } else {
         ProfScope ps("fmm_p2p_f64", pair_flops(kind) * static_cast<double>(near_pairs));
-        dispatch_kind(kind, [&]<int K>() {
+        dispatch_fmm_kind(kind, [&]<int K>() {
           p2p_kernel<K, double><<<static_cast<unsigned>(n_chunks), 128, 0, st>>>(
               kp64, tt.pos64.data(), tt.perm.data(), tt.start[lf].data(), chunk_leaf.data(),
               p2p_table.data(), src.pos64.data(), sw64.data(), src.start[lf].data(), wl, out);
@@ -1710,14 +1719,14 @@ struct Fmm<T>::Impl {
                    pair_flops(kind) * static_cast<double>(near_pairs));
       const T wl = static_cast<T>(box.width / static_cast<double>(1 << lf));
       if (tleaf.size() > 0) {
-        dispatch_kind(kind, [&]<int K>() {
+        dispatch_fmm_kind(kind, [&]<int K>() {
           p2p_point_kernel<K, T><<<blocks_for(nt, 128), 128, 0, st>>>(
               kp, tt.pos.data(), tt.perm.data(), tleaf.data(), nt, p2p_table.data(),
               src.pos.data(), sw.data(), src.start[lf].data(), wl, out);
           return 0;
         });
       } else {
-        dispatch_kind(kind, [&]<int K>() {
+        dispatch_fmm_kind(kind, [&]<int K>() {
           p2p_kernel<K, T><<<static_cast<unsigned>(n_chunks), 128, 0, st>>>(
               kp, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), chunk_leaf.data(),
               p2p_table.data(), src.pos.data(), sw.data(), src.start[lf].data(), wl, out);
@@ -1730,10 +1739,19 @@ struct Fmm<T>::Impl {
 };
 
 template <class T>
+bool Fmm<T>::near_only_supported(int kind) {
+  return kind == PGPU_RBF_CUB || kind == PGPU_RBF_SPH ||
+         (kind >= kKindSpDirect && kind < kKindSpDirect + 4);
+}
+
+template <class T>
 bool Fmm<T>::supported(int kind) {
-  // Compactly supported and piecewise kernels are not smooth enough for interpolation; the
-  // reference splits the spheroidal family (src/fmm/spheroidal_evaluator.hpp); those stay on the
-  // exact direct backend here.
+  // Compactly supported and piecewise kernels are not smooth enough for interpolation: they run
+  // near-field-only trees (near_only_supported), and the spheroidal family is split into a
+  // compact direct part and a smooth fast part (src/fmm/spheroidal_evaluator.hpp), as the
+  // evaluator arranges.
+  if (kind >= kKindSpDirect) return false;
+  if (kind >= kKindSpFast) return true;
   switch (kind) {
     case PGPU_RBF_CUB:
     case PGPU_RBF_SPH:

@@ -10,7 +10,10 @@ namespace pgpu {
 template <class T>
 class Fmm {
  public:
+  // Kernels whose far field interpolates (the smooth ones, and the spheroidal fast parts).
   static bool supported(int kind);
+  // Kernels of compact support, evaluated by near-field-only trees (FarFieldConfig::near_only).
+  static bool near_only_supported(int kind);
   // box_min / box_width: the cube (anisotropy frame, relative to the frame origin of the
   // positions handed in later).
   Fmm(int kind, const KParams<T>& kp, const Mat3& a, const double box_min[3], double box_width,

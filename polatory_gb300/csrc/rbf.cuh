@@ -103,6 +103,16 @@ PG_HD double support_radius_isotropic(int kind, const double* p) {
   return INFINITY;
 }
 
+// Internal kinds of the split spheroidal kernels (src/fmm/spheroidal_evaluator.hpp:8-62 with
+// rbf/cov_spheroidal{3,5,7,9}.hpp direct_part / fast_part): the smooth fast part is the inverse
+// multiquadric tail over all distances, the compact direct part the linear head minus that tail
+// inside rho0 (zero beyond). They only reach the FMM's near and far fields (value kernels).
+constexpr int kKindSpFast = 16;    // 16..19: fast parts of sp3, sp5, sp7, sp9
+constexpr int kKindSpDirect = 20;  // 20..23: direct parts of sp3, sp5, sp7, sp9
+PG_HD constexpr int sp_base_kind(int k) {
+  return k >= kKindSpDirect ? PGPU_RBF_SP3 + (k - kKindSpDirect) : PGPU_RBF_SP3 + (k - kKindSpFast);
+}
+
 // Generalized Cauchy "A" constants, cov_generalized_cauchy{3,5,7}.hpp:24 (gc9 has none: 1).
 PG_HD double cauchy_a(int kind) {
   switch (kind) {
@@ -157,6 +167,18 @@ PG_HD T rbf_value(T r2, const KParams<T>& kp) {
       return p / sqrt_pow<9>(T(1) + rho * rho);
     } else if constexpr (KIND == PGPU_RBF_SPH) {
       return r < range ? p * (T(1) + rho * (T(-1.5) + T(0.5) * rho * rho)) : T(0);
+    } else if constexpr (KIND >= kKindSpFast) {  // split spheroidal parts
+      constexpr int base = sp_base_kind(KIND);
+      const SpheroidalConst s = spheroidal_const(base);
+      const T q = T(1) + T(s.c) * rho * rho;
+      T den;
+      if constexpr (base == PGPU_RBF_SP3) den = sqrt_pow<3>(q);
+      else if constexpr (base == PGPU_RBF_SP5) den = sqrt_pow<5>(q);
+      else if constexpr (base == PGPU_RBF_SP7) den = sqrt_pow<7>(q);
+      else den = sqrt_pow<9>(q);
+      const T imq = p * T(s.b) / den;
+      if constexpr (KIND < kKindSpDirect) return imq;
+      else return rho < T(s.rho0) ? p * (T(1) - T(s.a) * rho) - imq : T(0);
     } else {  // spheroidal
       const SpheroidalConst s = spheroidal_const(KIND);
       if (rho < T(s.rho0)) return p * (T(1) - T(s.a) * rho);
@@ -403,6 +425,22 @@ PG_HD auto dispatch_kind(int kind, F&& f) {
     case PGPU_RBF_SP9: return f.template operator()<PGPU_RBF_SP9>();
     case PGPU_RBF_TH2: return f.template operator()<PGPU_RBF_TH2>();
     default: return f.template operator()<PGPU_RBF_TH3>();
+  }
+}
+
+// The FMM's dispatch: the 16 public kinds and the split spheroidal parts.
+template <class F>
+PG_HD auto dispatch_fmm_kind(int kind, F&& f) {
+  switch (kind) {
+    case kKindSpFast + 0: return f.template operator()<kKindSpFast + 0>();
+    case kKindSpFast + 1: return f.template operator()<kKindSpFast + 1>();
+    case kKindSpFast + 2: return f.template operator()<kKindSpFast + 2>();
+    case kKindSpFast + 3: return f.template operator()<kKindSpFast + 3>();
+    case kKindSpDirect + 0: return f.template operator()<kKindSpDirect + 0>();
+    case kKindSpDirect + 1: return f.template operator()<kKindSpDirect + 1>();
+    case kKindSpDirect + 2: return f.template operator()<kKindSpDirect + 2>();
+    case kKindSpDirect + 3: return f.template operator()<kKindSpDirect + 3>();
+    default: return dispatch_kind(kind, f);
   }
 }
 
