@@ -80,6 +80,13 @@ def build(verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    # The command-line front end (fit / evaluate) over the C ABI.
+    cli = PKG / "polatory-gpu"
+    cmd = ["g++", "-std=c++20", "-O2", f"-I{INCLUDE}", str(PKG / "cli" / "polatory_gpu_cli.cpp"),
+           f"-L{PKG}", "-lpolatory_gpu", "-Wl,-rpath,$ORIGIN", "-o", str(cli)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"cli build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     return LIB
 
 
