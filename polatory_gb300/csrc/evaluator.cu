@@ -134,6 +134,26 @@ void subtract_scalar(double* x, Index n, double c) {
   PGPU_LAUNCH_CHECK();
 }
 
+namespace {
+// out[3 i + r] += sum_c a[3 c + r] g[3 i + c]  (A^T g: the anisotropy frame's gradient mapped back)
+__global__ void frame_gradient_add_kernel(Mat3 a, const double* __restrict__ g, Index n,
+                                          double* __restrict__ out) {
+  const Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double ox, oy, oz;
+  mat3_tvec(a.a, g[3 * i], g[3 * i + 1], g[3 * i + 2], ox, oy, oz);
+  out[3 * i] += ox;
+  out[3 * i + 1] += oy;
+  out[3 * i + 2] += oz;
+}
+}  // namespace
+
+void frame_gradient_add(const Mat3& a, const double* g, Index n, double* out) {
+  if (n <= 0) return;
+  frame_gradient_add_kernel<<<blocks_for(n, 256), 256, 0, stream()>>>(a, g, n, out);
+  PGPU_LAUNCH_CHECK();
+}
+
 bool device_all_finite(const double* p, Index n) {
   if (n <= 0) return true;
   DevBuf<int> flag(1);
@@ -186,6 +206,11 @@ struct Evaluator<T>::Term {
   std::unique_ptr<Fmm<T>> fmm_near;
   bool near_sources_dirty = true;
   bool near_targets_dirty = true;
+  // Gradient targets through the FMM (value sources): their frame positions and tree.
+  DevBuf<P4<double>> tgpos_d;
+  std::unique_ptr<Fmm<T>> fmm_g;
+  bool g_sources_dirty = true;
+  bool g_targets_dirty = true;
 };
 
 template <class T>
@@ -331,6 +356,7 @@ void Evaluator<T>::set_sources(const double* pts, Index mu, const double* gpts, 
     t->gg.resize(3 * sigma);
     t->fmm_sources_dirty = true;
     t->near_sources_dirty = true;
+    t->g_sources_dirty = true;
     t->order = 0;  // the accuracy estimate depends on the sources (and weights)
   }
 }
@@ -351,12 +377,17 @@ void Evaluator<T>::set_targets(const double* pts, Index m, const double* gpts, I
       to_frame_kernel<double><<<blocks_for(m, 256), 256, 0, stream()>>>(
           pts, m, t->a, t->origin[0], t->origin[1], t->origin[2], t->tpos_d.data());
     }
-    if (mg)
+    t->tgpos_d.resize(mg);
+    if (mg) {
       to_frame_kernel<T><<<blocks_for(mg, 256), 256, 0, stream()>>>(
           gpts, mg, t->a, t->origin[0], t->origin[1], t->origin[2], t->tgpos.data());
+      to_frame_kernel<double><<<blocks_for(mg, 256), 256, 0, stream()>>>(
+          gpts, mg, t->a, t->origin[0], t->origin[1], t->origin[2], t->tgpos_d.data());
+    }
     PGPU_LAUNCH_CHECK();
     t->fmm_targets_dirty = true;
     t->near_targets_dirty = true;
+    t->g_targets_dirty = true;
   }
 }
 
@@ -415,7 +446,15 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
     Term& t = *tp;
     // Split kernels need leaves at least as wide as the support with a level-2 tree or finer.
     const bool split = t.near_kind >= 0;
-    const bool fmm_ok = sigma_ == 0 && mg_ == 0 &&
+    // Gradient targets of value sources go through their own FMM (smooth kernels); the code
+    // below then sees value targets only (mgv = 0).
+    const bool grad_fmm = sigma_ == 0 && mg_ > 0 && !split && !symmetric_ &&
+                          Fmm<T>::supported(t.rbf.kind) &&
+                          (backend_ == kBackendFmm ||
+                           (backend_ == kBackendAuto &&
+                            static_cast<double>(mu_) * static_cast<double>(mg_) > direct_pair_limit<T>()));
+    const Index mgv = grad_fmm ? 0 : mg_;
+    const bool fmm_ok = sigma_ == 0 && mgv == 0 &&
                         (split ? 4.0 * t.near_radius <= t.box_width : Fmm<T>::supported(t.rbf.kind));
     bool use_fmm = fmm_ok && (backend_ == kBackendFmm ||
                               (backend_ == kBackendAuto && pairs > direct_pair_limit<T>()));
@@ -430,8 +469,8 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
     }
     const bool exact = use_fmm && order_free && t.order < 0;
     if (exact) use_fmm = false;
-    const bool fp64_near = sizeof(T) == 4 && (near64_ || exact) && sigma_ == 0 && mg_ == 0;
-    const bool values_only = sigma_ == 0 && mg_ == 0;
+    const bool fp64_near = sizeof(T) == 4 && (near64_ || exact) && sigma_ == 0 && mgv == 0;
+    const bool values_only = sigma_ == 0 && mgv == 0;
     if (!use_fmm && fp64_near) {
       if (!direct_evaluate_ff(t.rbf.kind, t.kp64, t.spos_d.data(), w_, mu_, t.tpos_d.data(), m_,
                               out_v, stream())) {
@@ -446,7 +485,7 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
       stats_.direct_pairs += static_cast<Index>(pairs);
     } else if (!use_fmm) {
       DirectSources<T> src{t.spos.data(), t.vw.data(), mu_, t.sgpos.data(), t.gg.data(), sigma_};
-      DirectTargets<T> trg{t.tpos.data(), m_, out_v, t.tgpos.data(), mg_, out_g};
+      DirectTargets<T> trg{t.tpos.data(), m_, out_v, t.tgpos.data(), mgv, out_g};
       direct_evaluate<T>(t.rbf.kind, t.kp, t.a, src, trg, stream());
       stats_.direct_pairs += static_cast<Index>(pairs);
     } else {
@@ -500,6 +539,35 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
       t.fmm->set_near_fp64(fp64_near, t.kp64);
       t.fmm->evaluate(t.vw.data(), t.gg.data(), w_, out_v, out_g);
       stats_.near_pairs += t.fmm->near_pairs();
+      stats_.backend = 1;
+    }
+    if (grad_fmm && t.order < 0) {
+      // The value estimate asked for exact sums: the gradients take them too.
+      DirectSources<double> src{t.spos_d.data(), w_, mu_, nullptr, nullptr, 0};
+      DirectTargets<double> trg{nullptr, 0, nullptr, t.tgpos_d.data(), mg_, out_g};
+      direct_evaluate<double>(t.rbf.kind, t.kp64, t.a, src, trg, stream());
+    } else if (grad_fmm) {
+      double rel_min[3];
+      for (int k = 0; k < 3; ++k) rel_min[k] = t.box_min[k] - t.origin[k];
+      if (!t.fmm_g) {
+        t.fmm_g = std::make_unique<Fmm<T>>(t.rbf.kind, t.kp, t.a, rel_min, t.box_width, term_acc);
+        if (ff_set_ || t.order > 0) {
+          FarFieldConfig c = ff_set_ ? ff_ : FarFieldConfig{};
+          if (order_free && t.order > 0) c.order = t.order;
+          t.fmm_g->set_config(c);
+        }
+        t.fmm_g->set_gradient_targets(true);
+        t.g_sources_dirty = t.g_targets_dirty = true;
+      }
+      if (t.g_sources_dirty) t.fmm_g->set_sources(t.spos_d.data(), mu_);
+      if (t.g_targets_dirty) t.fmm_g->set_targets(t.tgpos_d.data(), mg_);
+      t.g_sources_dirty = t.g_targets_dirty = false;
+      DevBuf<double> g3(static_cast<size_t>(3 * mg_));
+      g3.zero();
+      t.fmm_g->set_near_fp64(sizeof(T) == 4 && near64_, t.kp64);
+      t.fmm_g->evaluate(t.vw.data(), t.gg.data(), w_, g3.data(), nullptr);
+      frame_gradient_add(t.a, g3.data(), mg_, out_g);
+      stats_.near_pairs += t.fmm_g->near_pairs();
       stats_.backend = 1;
     }
   }

@@ -43,6 +43,8 @@ struct Bbox3 {
 Bbox3 bbox_of_device_points(const double* pts, Index n);
 // True when every one of the n device values is finite (one reduction and a sync).
 bool device_all_finite(const double* p, Index n);
+// out[3 i ..] += A^T g[3 i ..] for n gradients (device).
+void frame_gradient_add(const Mat3& a, const double* g, Index n, double* out);
 // Lattice node positions (lc_origin + lc) * basis for n device int32 triples (lcs), into pts (n x 3).
 void lattice_positions(const double lc_origin[3], const double basis[9], const int32_t* lcs, Index n,
                        double* pts);

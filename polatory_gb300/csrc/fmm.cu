@@ -105,6 +105,35 @@ __device__ __forceinline__ void cheb_basis(const Cheb<T>& c, T x, T* s) {
   }
 }
 
+// The basis and its derivative: dS_m/dx = 2/p sum_{k>=1} T_k(x_m) k U_{k-1}(x), with U the
+// Chebyshev polynomials of the second kind (T_k' = k U_{k-1}).
+template <int P, class T>
+__device__ __forceinline__ void cheb_basis_d(const Cheb<T>& c, T x, T* s, T* ds) {
+  T t[P], u[P];
+  t[0] = T(1);
+  u[0] = T(1);
+  if (P > 1) {
+    t[1] = x;
+    u[1] = T(2) * x;
+  }
+#pragma unroll
+  for (int k = 2; k < P; ++k) {
+    t[k] = T(2) * x * t[k - 1] - t[k - 2];
+    u[k] = T(2) * x * u[k - 1] - u[k - 2];
+  }
+#pragma unroll
+  for (int m = 0; m < P; ++m) {
+    T v = T(0), dv = T(0);
+#pragma unroll
+    for (int k = 1; k < P; ++k) {
+      v += c.tkm[m][k] * t[k];
+      dv += c.tkm[m][k] * T(k) * u[k - 1];
+    }
+    s[m] = (T(1) + T(2) * v) / T(P);
+    ds[m] = T(2) * dv / T(P);
+  }
+}
+
 // ---- Morton keys --------------------------------------------------------------------------
 __host__ __device__ __forceinline__ uint64_t spread3(uint64_t x) {
   x &= 0x1fffffULL;
@@ -611,6 +640,113 @@ __global__ void __launch_bounds__(128)
       v += vy * sx[ax];
     }
     out[perm[i]] += static_cast<double>(v);
+  }
+}
+
+// L2P for gradient targets: out3[3 perm[i] + k] += d/dx_k of the local expansion at the target
+// (the anisotropy frame's gradient; the caller maps it back with A^T).
+template <int P, class T>
+__global__ void __launch_bounds__(128)
+    l2p_grad_kernel(Cheb<T> ch, const P4<T>* __restrict__ tpos, const Index* __restrict__ perm,
+                    const Index* __restrict__ leaf_start, const int* __restrict__ chunk_leaf,
+                    Box box, int lf, const T* __restrict__ L, double* __restrict__ out3) {
+  constexpr int P3 = P * P * P;
+  __shared__ T s_l[P3];
+  const Index leaf = chunk_leaf[2 * blockIdx.x];
+  for (int e = threadIdx.x; e < P3; e += blockDim.x) s_l[e] = L[leaf * P3 + e];
+  __syncthreads();
+  const double wk = box.width / static_cast<double>(1 << lf);
+  const T inv_r = static_cast<T>(2.0 / wk);
+  const Index beg = leaf_start[leaf] + static_cast<Index>(chunk_leaf[2 * blockIdx.x + 1]) * kP2PChunk;
+  const Index end = min(leaf_start[leaf + 1], beg + kP2PChunk);
+  for (Index i = beg + threadIdx.x; i < end; i += blockDim.x) {
+    const P4<T> pt = tpos[i];
+    T sx[P], sy[P], sz[P], dx[P], dy[P], dz[P];
+    cheb_basis_d<P>(ch, pt.x * inv_r, sx, dx);
+    cheb_basis_d<P>(ch, pt.y * inv_r, sy, dy);
+    cheb_basis_d<P>(ch, pt.z * inv_r, sz, dz);
+    T gx = T(0), gy = T(0), gz = T(0);
+#pragma unroll
+    for (int ax = 0; ax < P; ++ax) {
+      T vy = T(0), vyz = T(0), vdy = T(0);
+#pragma unroll
+      for (int ay = 0; ay < P; ++ay) {
+        T vz = T(0), vdz = T(0);
+#pragma unroll
+        for (int az = 0; az < P; ++az) {
+          const T l = s_l[(ax * P + ay) * P + az];
+          vz += l * sz[az];
+          vdz += l * dz[az];
+        }
+        vy += vz * sy[ay];
+        vdy += vz * dy[ay];
+        vyz += vdz * sy[ay];
+      }
+      gx += vy * dx[ax];
+      gy += vdy * sx[ax];
+      gz += vyz * sx[ax];
+    }
+    const Index o = 3 * perm[i];
+    out3[o] += static_cast<double>(gx * inv_r);
+    out3[o + 1] += static_cast<double>(gy * inv_r);
+    out3[o + 2] += static_cast<double>(gz * inv_r);
+  }
+}
+
+// Near field for gradient targets: out3[3 tperm[i] + k] += sum_j w_j d/dx_k phi(x_i - y_j) over
+// the 27 neighbour leaves (anisotropy frame), one target per thread, source tiles in shared
+// memory.
+template <int KIND, class T>
+__global__ void __launch_bounds__(128)
+    p2p_grad_kernel(KParams<T> kp, const P4<T>* __restrict__ tpos, const Index* __restrict__ tperm,
+                    const Index* __restrict__ tleaf_start, const int* __restrict__ chunk_leaf,
+                    const int* __restrict__ table, const P4<T>* __restrict__ spos,
+                    const T* __restrict__ sw, const Index* __restrict__ sleaf_start, T wleaf,
+                    double* __restrict__ out3) {
+  __shared__ P4<T> s_p[128];
+  __shared__ int s_nb[27];
+  const int leaf = chunk_leaf[2 * blockIdx.x];
+  if (threadIdx.x < 27) s_nb[threadIdx.x] = table[static_cast<Index>(leaf) * 27 + threadIdx.x];
+  __syncthreads();
+  const Index tb = tleaf_start[leaf] + static_cast<Index>(chunk_leaf[2 * blockIdx.x + 1]) * kP2PChunk;
+  const Index te = min(tleaf_start[leaf + 1], tb + kP2PChunk);
+  for (Index i0 = tb; i0 < te; i0 += blockDim.x) {
+    const Index i = i0 + threadIdx.x;
+    const bool active = i < te;
+    const P4<T> t = active ? tpos[i] : P4<T>{T(0), T(0), T(0), T(0)};
+    double tot[3] = {0.0, 0.0, 0.0};
+    for (int nb = 0; nb < 27; ++nb) {
+      const int s = s_nb[nb];
+      if (s < 0) continue;
+      const T tx = t.x - static_cast<T>(nb / 9 - 1) * wleaf;
+      const T ty = t.y - static_cast<T>((nb / 3) % 3 - 1) * wleaf;
+      const T tz = t.z - static_cast<T>(nb % 3 - 1) * wleaf;
+      const Index sb = sleaf_start[s], se = sleaf_start[s + 1];
+      for (Index base = sb; base < se; base += 128) {
+        const int cnt = static_cast<int>(min(static_cast<Index>(128), se - base));
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+          P4<T> p = spos[base + threadIdx.x];
+          p.w = sw[base + threadIdx.x];
+          s_p[threadIdx.x] = p;
+        }
+        __syncthreads();
+        T ax = T(0), ay = T(0), az = T(0);
+        for (int j = 0; j < cnt; ++j) {
+          const P4<T> q = s_p[j];
+          acc_grad_from_value<KIND>(tx - q.x, ty - q.y, tz - q.z, q.w, kp, ax, ay, az);
+        }
+        tot[0] += ax;
+        tot[1] += ay;
+        tot[2] += az;
+      }
+    }
+    if (active) {
+      const Index o = 3 * tperm[i];
+      out3[o] += tot[0];
+      out3[o + 1] += tot[1];
+      out3[o + 2] += tot[2];
+    }
   }
 }
 
@@ -1337,6 +1473,7 @@ struct Fmm<T>::Impl {
   Index ns = 0, nt = 0;
   int lf = 2;
   bool near_only = false;  // compact support: near field only (FarFieldConfig::near_only)
+  bool grad_out = false;   // gradient targets: three outputs per target (set_gradient_targets)
   bool built = false;
   // M2L tables per level (target cells x 343) and P2P table (target leaves x 27).
   std::vector<DevBuf<int>> m2l_table;
@@ -1652,9 +1789,14 @@ struct Fmm<T>::Impl {
     if (tt.ncell[lf] > 0) {
       const double npt = static_cast<double>(symmetric ? ns : nt);
       ProfScope ps(f32 ? "fmm_l2p_f32" : "fmm_l2p_f64", npt * (2.0 * P3 + 6.0 * P * P));
-      l2p_kernel<P, T><<<static_cast<unsigned>(n_chunks), 128, 0, st>>>(
-          ch, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), chunk_leaf.data(), box, lf,
-          L[lf].data(), out);
+      if (grad_out)
+        l2p_grad_kernel<P, T><<<static_cast<unsigned>(n_chunks), 128, 0, st>>>(
+            ch, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), chunk_leaf.data(), box, lf,
+            L[lf].data(), out);
+      else
+        l2p_kernel<P, T><<<static_cast<unsigned>(n_chunks), 128, 0, st>>>(
+            ch, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), chunk_leaf.data(), box, lf,
+            L[lf].data(), out);
       PGPU_LAUNCH_CHECK();
     }
   }
@@ -1684,7 +1826,35 @@ struct Fmm<T>::Impl {
       }
     }
     const Index ntl = tt.ncell[lf];
-    if (ntl > 0 && fp64_near) {
+    if (ntl > 0 && grad_out) {
+      // Gradient targets (3 outputs per target), public smooth kinds only.
+      ProfScope ps(sizeof(T) == 4 && !fp64_near ? "fmm_p2p_grad_f32" : "fmm_p2p_grad_f64",
+                   3.0 * pair_flops(kind) * static_cast<double>(near_pairs));
+      if (fp64_near) {
+        ensure_pos64(src, spos_in);
+        if (!symmetric) ensure_pos64(trg, tpos_in);
+        DevBuf<double> sw64(ns);
+        gather_w_kernel<double><<<blocks_for(ns, 256), 256, 0, st>>>(w64, src.perm.data(), ns,
+                                                                     sw64.data());
+        PGPU_LAUNCH_CHECK();
+        const double wl = box.width / static_cast<double>(1 << lf);
+        dispatch_kind(kind, [&]<int K>() {
+          p2p_grad_kernel<K, double><<<static_cast<unsigned>(n_chunks), 128, 0, st>>>(
+              kp64, tt.pos64.data(), tt.perm.data(), tt.start[lf].data(), chunk_leaf.data(),
+              p2p_table.data(), src.pos64.data(), sw64.data(), src.start[lf].data(), wl, out);
+          return 0;
+        });
+      } else {
+        const T wl = static_cast<T>(box.width / static_cast<double>(1 << lf));
+        dispatch_kind(kind, [&]<int K>() {
+          p2p_grad_kernel<K, T><<<static_cast<unsigned>(n_chunks), 128, 0, st>>>(
+              kp, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), chunk_leaf.data(),
+              p2p_table.data(), src.pos.data(), sw.data(), src.start[lf].data(), wl, out);
+          return 0;
+        });
+      }
+      PGPU_LAUNCH_CHECK();
+    } else if (ntl > 0 && fp64_near) {
       ensure_pos64(src, spos_in);
       if (!symmetric) ensure_pos64(trg, tpos_in);
       DevBuf<double> sw64(ns);
@@ -1811,6 +1981,11 @@ void Fmm<T>::set_targets(const P4<double>* pos, Index n) {
   impl_->tpos_in = pos;
   impl_->nt = n;
   impl_->built = false;
+}
+
+template <class T>
+void Fmm<T>::set_gradient_targets(bool on) {
+  impl_->grad_out = on;
 }
 
 template <class T>

@@ -26,6 +26,10 @@ class Fmm {
   void set_points(const P4<double>* pos, Index n);
   void set_sources(const P4<double>* pos, Index n);
   void set_targets(const P4<double>* pos, Index n);
+  // Targets are gradient targets: evaluate adds, per target, the three components of the
+  // gradient in the anisotropy frame (out_v[3 i + k]; the caller maps them back with A^T).
+  // Smooth public kinds only.
+  void set_gradient_targets(bool on);
   // FP32 trees: take the near field with FP64 positions (leaf-relative), weights and sums,
   // the far field staying in T. Ignored for FP64 trees.
   void set_near_fp64(bool on, const KParams<double>& kp64);

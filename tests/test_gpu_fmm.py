@@ -8,6 +8,7 @@ import pytest
 
 import oracle
 import polatory_gb300 as pg
+from polatory_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
 
@@ -170,3 +171,46 @@ def test_fmm_accuracy_estimate(precision):
     bad.set_target_points(trg)
     bad.set_weights(w)
     assert np.max(np.abs(bad.evaluate() - want)) <= 2e-13 * scale
+
+
+@pytest.mark.parametrize("precision", [pg.PLAIN, pg.MIXED], ids=["plain", "mixed"])
+@pytest.mark.parametrize("cls,params", [(pg.Biharmonic3D, [1.0]), (pg.CovExponential, [1.0, 0.3])],
+                         ids=["bh3", "exp"])
+def test_fmm_gradient_targets(cls, params, precision):
+    # Value sources, gradient targets (fmm/gradient_transpose_kernel.hpp: grad_x of sum_j w_j
+    # phi(A (x - y_j)) = A^T grad phi): L2P of the expansion's derivative and the gradient near
+    # field, against the oracle's exact gradients (test/interpolation/test_evaluator.cpp:27-76
+    # checks gradients of the FMM evaluator against the direct sums the same way).
+    src, trg, w = sample(60000, 20000, 36)
+    rbf = cls(params)
+    rbf.anisotropy = np.array([[1.0, 0.2, 0.0], [0.0, 0.9, 0.1], [0.0, 0.0, 1.1]])
+    ev = pg.FmmEvaluator(rbf, [0, 0, 0, 1, 1, 1], kernel=_lib.KERNEL_GRADIENT_TRANSPOSE,
+                         precision=precision)
+    ev.configure(backend=2)
+    ev.set_source_points(src)
+    ev.set_target_points(trg)
+    ev.set_weights(w)
+    got = ev.evaluate().reshape(-1, 3)
+    m = pg.Model(rbf, 0)._c()
+    m.poly_degree = -1
+    want = oracle.direct_evaluate(m, src, w, np.zeros((0, 3)), gtrg=trg).reshape(-1, 3)
+    scale = np.abs(w).sum() * max(1.0, np.max(np.abs(want)) / np.abs(w).sum())
+    bound = 2e-5 if cls is pg.Biharmonic3D else 1e-4
+    assert np.max(np.abs(got - want)) <= bound * scale, (np.max(np.abs(got - want)), scale)
+
+
+def test_interpolant_gradients_through_the_fmm():
+    # Interpolant::evaluate with gradient points (evaluate(points, grad_points)): values and
+    # gradients of a 30,000-point biharmonic interpolant at 50,000 points.
+    g = np.random.Generator(np.random.PCG64(37))
+    pts = g.random((30000, 3))
+    vals = np.sin(3 * pts[:, 0]) + pts[:, 1] * pts[:, 2]
+    model = pg.Model(pg.Biharmonic3D([1.0]), 1)
+    it = pg.Interpolant(model)
+    it.fit(pts, vals, 1e-6)
+    q = g.random((50000, 3))
+    out = it.evaluate(q, grad_points=q)
+    grads = out[q.shape[0]:].reshape(-1, 3)
+    sub = g.choice(q.shape[0], 1000, replace=False)
+    want = oracle.direct_evaluate(model, pts, it.weights, np.zeros((0, 3)), gtrg=q[sub]).reshape(-1, 3)
+    assert np.max(np.abs(grads[sub] - want)) <= 1e-4 * max(1.0, np.max(np.abs(want)))
