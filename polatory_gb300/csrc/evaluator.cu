@@ -206,11 +206,14 @@ struct Evaluator<T>::Term {
   std::unique_ptr<Fmm<T>> fmm_near;
   bool near_sources_dirty = true;
   bool near_targets_dirty = true;
-  // Gradient targets through the FMM (value sources): their frame positions and tree.
-  DevBuf<P4<double>> tgpos_d;
-  std::unique_ptr<Fmm<T>> fmm_g;
-  bool g_sources_dirty = true;
-  bool g_targets_dirty = true;
+  // The gradient blocks through the FMM: frame positions of the gradient sources and targets,
+  // and the trees of value -> gradient (fmm_g), gradient -> value (fmm_d) and gradient ->
+  // gradient (fmm_dg).
+  DevBuf<P4<double>> sgpos_d, tgpos_d;
+  std::unique_ptr<Fmm<T>> fmm_g, fmm_d, fmm_dg;
+  bool g_sources_dirty = true, g_targets_dirty = true;
+  bool d_sources_dirty = true, d_targets_dirty = true;
+  bool dg_sources_dirty = true, dg_targets_dirty = true;
 };
 
 template <class T>
@@ -348,15 +351,19 @@ void Evaluator<T>::set_sources(const double* pts, Index mu, const double* gpts, 
       to_frame_kernel<double><<<blocks_for(mu, 256), 256, 0, stream()>>>(
           pts, mu, t->a, t->origin[0], t->origin[1], t->origin[2], t->spos_d.data());
     }
-    if (sigma)
+    t->sgpos_d.resize(sigma);
+    if (sigma) {
       to_frame_kernel<T><<<blocks_for(sigma, 256), 256, 0, stream()>>>(
           gpts, sigma, t->a, t->origin[0], t->origin[1], t->origin[2], t->sgpos.data());
+      to_frame_kernel<double><<<blocks_for(sigma, 256), 256, 0, stream()>>>(
+          gpts, sigma, t->a, t->origin[0], t->origin[1], t->origin[2], t->sgpos_d.data());
+    }
     PGPU_LAUNCH_CHECK();
     t->vw.resize(mu);
     t->gg.resize(3 * sigma);
     t->fmm_sources_dirty = true;
     t->near_sources_dirty = true;
-    t->g_sources_dirty = true;
+    t->g_sources_dirty = t->d_sources_dirty = t->dg_sources_dirty = true;
     t->order = 0;  // the accuracy estimate depends on the sources (and weights)
   }
 }
@@ -387,7 +394,7 @@ void Evaluator<T>::set_targets(const double* pts, Index m, const double* gpts, I
     PGPU_LAUNCH_CHECK();
     t->fmm_targets_dirty = true;
     t->near_targets_dirty = true;
-    t->g_targets_dirty = true;
+    t->g_targets_dirty = t->d_targets_dirty = t->dg_targets_dirty = true;
   }
 }
 
@@ -446,15 +453,16 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
     Term& t = *tp;
     // Split kernels need leaves at least as wide as the support with a level-2 tree or finer.
     const bool split = t.near_kind >= 0;
-    // Gradient targets of value sources go through their own FMM (smooth kernels); the code
-    // below then sees value targets only (mgv = 0).
-    const bool grad_fmm = sigma_ == 0 && mg_ > 0 && !split && !symmetric_ &&
-                          Fmm<T>::supported(t.rbf.kind) &&
-                          (backend_ == kBackendFmm ||
-                           (backend_ == kBackendAuto &&
-                            static_cast<double>(mu_) * static_cast<double>(mg_) > direct_pair_limit<T>()));
-    const Index mgv = grad_fmm ? 0 : mg_;
-    const bool fmm_ok = sigma_ == 0 && mgv == 0 &&
+    // Gradient sources or targets with a smooth kernel: each of the four blocks (value/gradient
+    // sources x value/gradient targets) runs its own FMM (fmm/kernel.hpp, gradient_kernel.hpp,
+    // gradient_transpose_kernel.hpp, hessian_kernel.hpp); the code below then sees the value
+    // block only (sigmav = mgv = 0).
+    const bool blocks_fmm = (sigma_ > 0 || mg_ > 0) && !split && Fmm<T>::supported(t.rbf.kind) &&
+                            (backend_ == kBackendFmm ||
+                             (backend_ == kBackendAuto && pairs > direct_pair_limit<T>()));
+    const Index mgv = blocks_fmm ? 0 : mg_;
+    const Index sigmav = blocks_fmm ? 0 : sigma_;
+    const bool fmm_ok = sigmav == 0 && mgv == 0 &&
                         (split ? 4.0 * t.near_radius <= t.box_width : Fmm<T>::supported(t.rbf.kind));
     bool use_fmm = fmm_ok && (backend_ == kBackendFmm ||
                               (backend_ == kBackendAuto && pairs > direct_pair_limit<T>()));
@@ -469,8 +477,8 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
     }
     const bool exact = use_fmm && order_free && t.order < 0;
     if (exact) use_fmm = false;
-    const bool fp64_near = sizeof(T) == 4 && (near64_ || exact) && sigma_ == 0 && mgv == 0;
-    const bool values_only = sigma_ == 0 && mgv == 0;
+    const bool fp64_near = sizeof(T) == 4 && (near64_ || exact) && sigmav == 0 && mgv == 0;
+    const bool values_only = sigmav == 0 && mgv == 0;
     if (!use_fmm && fp64_near) {
       if (!direct_evaluate_ff(t.rbf.kind, t.kp64, t.spos_d.data(), w_, mu_, t.tpos_d.data(), m_,
                               out_v, stream())) {
@@ -484,7 +492,7 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
                                   m_, out_v, stream())) {
       stats_.direct_pairs += static_cast<Index>(pairs);
     } else if (!use_fmm) {
-      DirectSources<T> src{t.spos.data(), t.vw.data(), mu_, t.sgpos.data(), t.gg.data(), sigma_};
+      DirectSources<T> src{t.spos.data(), t.vw.data(), mu_, t.sgpos.data(), t.gg.data(), sigmav};
       DirectTargets<T> trg{t.tpos.data(), m_, out_v, t.tgpos.data(), mgv, out_g};
       direct_evaluate<T>(t.rbf.kind, t.kp, t.a, src, trg, stream());
       stats_.direct_pairs += static_cast<Index>(pairs);
@@ -541,34 +549,53 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
       stats_.near_pairs += t.fmm->near_pairs();
       stats_.backend = 1;
     }
-    if (grad_fmm && t.order < 0) {
-      // The value estimate asked for exact sums: the gradients take them too.
-      DirectSources<double> src{t.spos_d.data(), w_, mu_, nullptr, nullptr, 0};
-      DirectTargets<double> trg{nullptr, 0, nullptr, t.tgpos_d.data(), mg_, out_g};
-      direct_evaluate<double>(t.rbf.kind, t.kp64, t.a, src, trg, stream());
-    } else if (grad_fmm) {
+    if (blocks_fmm) {
+      if (t.order == 0 && order_free && std::isfinite(acc) && acc > 0.0 && mu_ == 0) t.order = 8;
       double rel_min[3];
       for (int k = 0; k < 3; ++k) rel_min[k] = t.box_min[k] - t.origin[k];
-      if (!t.fmm_g) {
-        t.fmm_g = std::make_unique<Fmm<T>>(t.rbf.kind, t.kp, t.a, rel_min, t.box_width, term_acc);
-        if (ff_set_ || t.order > 0) {
-          FarFieldConfig c = ff_set_ ? ff_ : FarFieldConfig{};
-          if (order_free && t.order > 0) c.order = t.order;
-          t.fmm_g->set_config(c);
+      // One block: sources (value or gradient) to targets (value or gradient).
+      auto block = [&](std::unique_ptr<Fmm<T>>& f, bool& sdirty, bool& tdirty, bool gsrc, bool gtrg) {
+        const Index ns_b = gsrc ? sigma_ : mu_;
+        const Index nt_b = gtrg ? mg_ : m_;
+        if (ns_b == 0 || nt_b == 0) return;
+        if (t.order < 0) {
+          // The estimate asked for exact sums.
+          DirectSources<T> src{gsrc ? nullptr : t.spos.data(), t.vw.data(), gsrc ? 0 : mu_,
+                               gsrc ? t.sgpos.data() : nullptr, t.gg.data(), gsrc ? sigma_ : 0};
+          DirectTargets<T> trg{gtrg ? nullptr : t.tpos.data(), gtrg ? 0 : m_, out_v,
+                               gtrg ? t.tgpos.data() : nullptr, gtrg ? mg_ : 0, out_g};
+          direct_evaluate<T>(t.rbf.kind, t.kp, t.a, src, trg, stream());
+          return;
         }
-        t.fmm_g->set_gradient_targets(true);
-        t.g_sources_dirty = t.g_targets_dirty = true;
-      }
-      if (t.g_sources_dirty) t.fmm_g->set_sources(t.spos_d.data(), mu_);
-      if (t.g_targets_dirty) t.fmm_g->set_targets(t.tgpos_d.data(), mg_);
-      t.g_sources_dirty = t.g_targets_dirty = false;
-      DevBuf<double> g3(static_cast<size_t>(3 * mg_));
-      g3.zero();
-      t.fmm_g->set_near_fp64(sizeof(T) == 4 && near64_, t.kp64);
-      t.fmm_g->evaluate(t.vw.data(), t.gg.data(), w_, g3.data(), nullptr);
-      frame_gradient_add(t.a, g3.data(), mg_, out_g);
-      stats_.near_pairs += t.fmm_g->near_pairs();
-      stats_.backend = 1;
+        if (!f) {
+          f = std::make_unique<Fmm<T>>(t.rbf.kind, t.kp, t.a, rel_min, t.box_width, term_acc);
+          if (ff_set_ || t.order > 0) {
+            FarFieldConfig c = ff_set_ ? ff_ : FarFieldConfig{};
+            if (order_free && t.order > 0) c.order = t.order;
+            f->set_config(c);
+          }
+          f->set_gradient_sources(gsrc);
+          f->set_gradient_targets(gtrg);
+          sdirty = tdirty = true;
+        }
+        if (sdirty) f->set_sources(gsrc ? t.sgpos_d.data() : t.spos_d.data(), ns_b);
+        if (tdirty) f->set_targets(gtrg ? t.tgpos_d.data() : t.tpos_d.data(), nt_b);
+        sdirty = tdirty = false;
+        f->set_near_fp64(sizeof(T) == 4 && near64_ && !gsrc, t.kp64);
+        if (gtrg) {
+          DevBuf<double> g3(static_cast<size_t>(3 * nt_b));
+          g3.zero();
+          f->evaluate(t.vw.data(), t.gg.data(), w_, g3.data(), nullptr);
+          frame_gradient_add(t.a, g3.data(), nt_b, out_g);
+        } else {
+          f->evaluate(t.vw.data(), t.gg.data(), w_, out_v, nullptr);
+        }
+        stats_.near_pairs += f->near_pairs();
+        stats_.backend = 1;
+      };
+      block(t.fmm_g, t.g_sources_dirty, t.g_targets_dirty, false, true);
+      block(t.fmm_d, t.d_sources_dirty, t.d_targets_dirty, true, false);
+      block(t.fmm_dg, t.dg_sources_dirty, t.dg_targets_dirty, true, true);
     }
   }
   if (with_poly && model_.l() > 0) {

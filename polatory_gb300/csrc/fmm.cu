@@ -213,6 +213,18 @@ __global__ void gather_w_kernel(const T* __restrict__ w, const Index* __restrict
   if (i < n) out[i] = w[perm[i]];
 }
 
+// Gradient-source weights (three per source) into the sorted order.
+template <class T>
+__global__ void gather_w3_kernel(const T* __restrict__ g, const Index* __restrict__ perm, Index n,
+                                 T* __restrict__ out) {
+  Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Index j = perm[i];
+  out[3 * i] = g[3 * j];
+  out[3 * i + 1] = g[3 * j + 1];
+  out[3 * i + 2] = g[3 * j + 2];
+}
+
 __global__ void rle_flags_kernel(const uint64_t* __restrict__ keys, Index n, int shift,
                                  Index* __restrict__ flags) {
   Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -351,6 +363,56 @@ __global__ void __launch_bounds__(256)
         const int ax = a / (P * P), ay = (a / P) % P, az = a % P;
         T s = T(0);
         for (int j = 0; j < cnt; ++j) s += s_w[j] * s_b[j][0][ax] * s_b[j][1][ay] * s_b[j][2][az];
+        acc[q] += s;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < (P3 + 255) / 256; ++q) {
+    const int a = threadIdx.x + 256 * q;
+    if (a < P3) M[leaf * P3 + a] = acc[q];
+  }
+}
+
+// P2M of gradient sources (dipoles): the potential of weight G at y is G . grad_y phi(x - y),
+// which the interpolation turns into sum_n (G . grad S_n(y)) phi(x - y_n): each source adds
+// G . grad S_n(y) to node n (frame coordinates; the chain rule's 2 / w factor included).
+template <int P, class T>
+__global__ void __launch_bounds__(256)
+    p2m_dipole_kernel(Cheb<T> ch, const P4<T>* __restrict__ spos, const T* __restrict__ sw3,
+                      const Index* __restrict__ leaf_start, Box box, int lf, T* __restrict__ M) {
+  constexpr int P3 = P * P * P;
+  const Index leaf = blockIdx.x;
+  __shared__ T s_b[32][3][P];
+  __shared__ T s_d[32][3][P];
+  __shared__ T s_g[32][3];
+  const double wk = box.width / static_cast<double>(1 << lf);
+  const T inv_r = static_cast<T>(2.0 / wk);
+  const Index beg = leaf_start[leaf], end = leaf_start[leaf + 1];
+  T acc[(P3 + 255) / 256];
+#pragma unroll
+  for (int q = 0; q < (P3 + 255) / 256; ++q) acc[q] = T(0);
+  for (Index base = beg; base < end; base += 32) {
+    const int cnt = static_cast<int>(min(static_cast<Index>(32), end - base));
+    __syncthreads();
+    if (threadIdx.x < 3 * cnt) {
+      const int j = threadIdx.x / 3, d = threadIdx.x % 3;
+      const P4<T> pt = spos[base + j];
+      const T x = (d == 0 ? pt.x : (d == 1 ? pt.y : pt.z));
+      cheb_basis_d<P>(ch, x * inv_r, s_b[j][d], s_d[j][d]);
+      s_g[j][d] = sw3[3 * (base + j) + d] * inv_r;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < (P3 + 255) / 256; ++q) {
+      const int a = threadIdx.x + 256 * q;
+      if (a < P3) {
+        const int ax = a / (P * P), ay = (a / P) % P, az = a % P;
+        T s = T(0);
+        for (int j = 0; j < cnt; ++j)
+          s += s_g[j][0] * s_d[j][0][ax] * s_b[j][1][ay] * s_b[j][2][az] +
+               s_g[j][1] * s_b[j][0][ax] * s_d[j][1][ay] * s_b[j][2][az] +
+               s_g[j][2] * s_b[j][0][ax] * s_b[j][1][ay] * s_d[j][2][az];
         acc[q] += s;
       }
     }
@@ -746,6 +808,72 @@ __global__ void __launch_bounds__(128)
       out3[o] += tot[0];
       out3[o + 1] += tot[1];
       out3[o + 2] += tot[2];
+    }
+  }
+}
+
+// Near field of gradient sources (weights G, three per source, anisotropy frame): value targets
+// take G . grad_y phi, gradient targets -H G (kernels.cuh: acc_value_from_grad,
+// acc_grad_from_grad); out has one or three entries per target.
+template <int KIND, class T, bool GRAD_TARGETS>
+__global__ void __launch_bounds__(128)
+    p2p_dipole_kernel(KParams<T> kp, const P4<T>* __restrict__ tpos, const Index* __restrict__ tperm,
+                      const Index* __restrict__ tleaf_start, const int* __restrict__ chunk_leaf,
+                      const int* __restrict__ table, const P4<T>* __restrict__ spos,
+                      const T* __restrict__ sw3, const Index* __restrict__ sleaf_start, T wleaf,
+                      double* __restrict__ out) {
+  __shared__ P4<T> s_p[128];
+  __shared__ T s_g[128][3];
+  __shared__ int s_nb[27];
+  const int leaf = chunk_leaf[2 * blockIdx.x];
+  if (threadIdx.x < 27) s_nb[threadIdx.x] = table[static_cast<Index>(leaf) * 27 + threadIdx.x];
+  __syncthreads();
+  const Index tb = tleaf_start[leaf] + static_cast<Index>(chunk_leaf[2 * blockIdx.x + 1]) * kP2PChunk;
+  const Index te = min(tleaf_start[leaf + 1], tb + kP2PChunk);
+  for (Index i0 = tb; i0 < te; i0 += blockDim.x) {
+    const Index i = i0 + threadIdx.x;
+    const bool active = i < te;
+    const P4<T> t = active ? tpos[i] : P4<T>{T(0), T(0), T(0), T(0)};
+    double tot[3] = {0.0, 0.0, 0.0};
+    for (int nb = 0; nb < 27; ++nb) {
+      const int s = s_nb[nb];
+      if (s < 0) continue;
+      const T tx = t.x - static_cast<T>(nb / 9 - 1) * wleaf;
+      const T ty = t.y - static_cast<T>((nb / 3) % 3 - 1) * wleaf;
+      const T tz = t.z - static_cast<T>(nb % 3 - 1) * wleaf;
+      const Index sb = sleaf_start[s], se = sleaf_start[s + 1];
+      for (Index base = sb; base < se; base += 128) {
+        const int cnt = static_cast<int>(min(static_cast<Index>(128), se - base));
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+          s_p[threadIdx.x] = spos[base + threadIdx.x];
+          for (int k = 0; k < 3; ++k) s_g[threadIdx.x][k] = sw3[3 * (base + threadIdx.x) + k];
+        }
+        __syncthreads();
+        T a0 = T(0), a1 = T(0), a2 = T(0);
+        for (int j = 0; j < cnt; ++j) {
+          const P4<T> q = s_p[j];
+          if constexpr (GRAD_TARGETS)
+            acc_grad_from_grad<KIND>(tx - q.x, ty - q.y, tz - q.z, s_g[j][0], s_g[j][1], s_g[j][2],
+                                     kp, a0, a1, a2);
+          else
+            acc_value_from_grad<KIND>(tx - q.x, ty - q.y, tz - q.z, s_g[j][0], s_g[j][1], s_g[j][2],
+                                      kp, a0);
+        }
+        tot[0] += a0;
+        tot[1] += a1;
+        tot[2] += a2;
+      }
+    }
+    if (active) {
+      if constexpr (GRAD_TARGETS) {
+        const Index o = 3 * tperm[i];
+        out[o] += tot[0];
+        out[o + 1] += tot[1];
+        out[o + 2] += tot[2];
+      } else {
+        out[tperm[i]] += tot[0];
+      }
     }
   }
 }
@@ -1474,6 +1602,8 @@ struct Fmm<T>::Impl {
   int lf = 2;
   bool near_only = false;  // compact support: near field only (FarFieldConfig::near_only)
   bool grad_out = false;   // gradient targets: three outputs per target (set_gradient_targets)
+  bool dipole = false;     // gradient sources: three weights per source (set_gradient_sources)
+  DevBuf<T> sw3;           // sorted gradient-source weights
   bool built = false;
   // M2L tables per level (target cells x 343) and P2P table (target leaves x 27).
   std::vector<DevBuf<int>> m2l_table;
@@ -1699,9 +1829,13 @@ struct Fmm<T>::Impl {
     if (src.ncell[lf] > 0) {
       ProfScope ps(f32 ? "fmm_p2m_f32" : "fmm_p2m_f64", 4.0 * P3 * static_cast<double>(ns),
                    static_cast<double>(ns) * 5 * sizeof(T));
-      p2m_kernel<P, T><<<static_cast<unsigned>(src.ncell[lf]), 256, 0, st>>>(
-          ch, src.pos.data(), sw.data(), src.start[lf].data(), src.keys[lf].data(), box, lf,
-          M[lf].data());
+      if (dipole)
+        p2m_dipole_kernel<P, T><<<static_cast<unsigned>(src.ncell[lf]), 256, 0, st>>>(
+            ch, src.pos.data(), sw3.data(), src.start[lf].data(), box, lf, M[lf].data());
+      else
+        p2m_kernel<P, T><<<static_cast<unsigned>(src.ncell[lf]), 256, 0, st>>>(
+            ch, src.pos.data(), sw.data(), src.start[lf].data(), src.keys[lf].data(), box, lf,
+            M[lf].data());
       PGPU_LAUNCH_CHECK();
     }
     for (int k = lf - 1; k >= 2; --k) {
@@ -1801,13 +1935,19 @@ struct Fmm<T>::Impl {
     }
   }
 
-  void evaluate(const T* vw, const double* w64, double* out) {
+  void evaluate(const T* vw, const T* gg, const double* w64, double* out) {
     if (!built) build();
     cudaStream_t st = stream();
     Tree<T>& tt = ttree();
     if (ns == 0 || (symmetric ? ns : nt) == 0) return;
-    const bool fp64_near = sizeof(T) == 4 && near64 && w64 != nullptr;
-    gather_w_kernel<T><<<blocks_for(ns, 256), 256, 0, st>>>(vw, src.perm.data(), ns, sw.data());
+    // Gradient sources keep their near field in T (their FP64 weights are not at hand here).
+    const bool fp64_near = sizeof(T) == 4 && near64 && w64 != nullptr && !dipole;
+    if (dipole) {
+      sw3.resize(static_cast<size_t>(3 * ns));
+      gather_w3_kernel<T><<<blocks_for(ns, 256), 256, 0, st>>>(gg, src.perm.data(), ns, sw3.data());
+    } else {
+      gather_w_kernel<T><<<blocks_for(ns, 256), 256, 0, st>>>(vw, src.perm.data(), ns, sw.data());
+    }
     PGPU_LAUNCH_CHECK();
     if (lf >= 2 && !near_only) {
       switch (p) {
@@ -1826,7 +1966,23 @@ struct Fmm<T>::Impl {
       }
     }
     const Index ntl = tt.ncell[lf];
-    if (ntl > 0 && grad_out) {
+    if (ntl > 0 && dipole) {
+      ProfScope ps(sizeof(T) == 4 ? "fmm_p2p_dipole_f32" : "fmm_p2p_dipole_f64",
+                   (grad_out ? 9.0 : 3.0) * pair_flops(kind) * static_cast<double>(near_pairs));
+      const T wl = static_cast<T>(box.width / static_cast<double>(1 << lf));
+      dispatch_kind(kind, [&]<int K>() {
+        if (grad_out)
+          p2p_dipole_kernel<K, T, true><<<static_cast<unsigned>(n_chunks), 128, 0, st>>>(
+              kp, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), chunk_leaf.data(),
+              p2p_table.data(), src.pos.data(), sw3.data(), src.start[lf].data(), wl, out);
+        else
+          p2p_dipole_kernel<K, T, false><<<static_cast<unsigned>(n_chunks), 128, 0, st>>>(
+              kp, tt.pos.data(), tt.perm.data(), tt.start[lf].data(), chunk_leaf.data(),
+              p2p_table.data(), src.pos.data(), sw3.data(), src.start[lf].data(), wl, out);
+        return 0;
+      });
+      PGPU_LAUNCH_CHECK();
+    } else if (ntl > 0 && grad_out) {
       // Gradient targets (3 outputs per target), public smooth kinds only.
       ProfScope ps(sizeof(T) == 4 && !fp64_near ? "fmm_p2p_grad_f32" : "fmm_p2p_grad_f64",
                    3.0 * pair_flops(kind) * static_cast<double>(near_pairs));
@@ -1995,8 +2151,13 @@ void Fmm<T>::set_near_fp64(bool on, const KParams<double>& kp64) {
 }
 
 template <class T>
-void Fmm<T>::evaluate(const T* vw, const T*, const double* w64, double* out_v, double*) {
-  impl_->evaluate(vw, w64, out_v);
+void Fmm<T>::evaluate(const T* vw, const T* gg, const double* w64, double* out_v, double*) {
+  impl_->evaluate(vw, gg, w64, out_v);
+}
+
+template <class T>
+void Fmm<T>::set_gradient_sources(bool on) {
+  impl_->dipole = on;
 }
 
 template <class T>

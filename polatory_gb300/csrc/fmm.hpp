@@ -30,6 +30,9 @@ class Fmm {
   // gradient in the anisotropy frame (out_v[3 i + k]; the caller maps them back with A^T).
   // Smooth public kinds only.
   void set_gradient_targets(bool on);
+  // Sources are gradient sources: their weights are the three frame components per source (gg
+  // of evaluate, A g in the caller's order). Smooth public kinds only; the near field stays in T.
+  void set_gradient_sources(bool on);
   // FP32 trees: take the near field with FP64 positions (leaf-relative), weights and sums,
   // the far field staying in T. Ignored for FP64 trees.
   void set_near_fp64(bool on, const KParams<double>& kp64);

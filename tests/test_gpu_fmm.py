@@ -214,3 +214,34 @@ def test_interpolant_gradients_through_the_fmm():
     sub = g.choice(q.shape[0], 1000, replace=False)
     want = oracle.direct_evaluate(model, pts, it.weights, np.zeros((0, 3)), gtrg=q[sub]).reshape(-1, 3)
     assert np.max(np.abs(grads[sub] - want)) <= 1e-4 * max(1.0, np.max(np.abs(want)))
+
+
+@pytest.mark.parametrize("precision", [pg.PLAIN, pg.MIXED], ids=["plain", "mixed"])
+@pytest.mark.parametrize("kernel", [_lib.KERNEL_GRADIENT, _lib.KERNEL_HESSIAN], ids=["grad", "hess"])
+@pytest.mark.parametrize("cls,params", [(pg.Biharmonic3D, [1.0]), (pg.CovGaussian, [1.0, 0.4])],
+                         ids=["bh3", "gau"])
+def test_fmm_gradient_sources(cls, params, kernel, precision):
+    # Gradient sources (fmm/gradient_kernel.hpp, hessian_kernel.hpp): dipole P2M and near field,
+    # value or gradient targets, against the oracle's exact sums (test_evaluator.cpp:27-76).
+    g = np.random.Generator(np.random.PCG64(38))
+    src = g.random((40000, 3))
+    trg = g.random((15000, 3))
+    w = g.standard_normal(3 * 40000)
+    rbf = cls(params)
+    rbf.anisotropy = np.array([[1.0, 0.1, 0.0], [0.0, 0.9, 0.0], [0.1, 0.0, 1.2]])
+    ev = pg.FmmEvaluator(rbf, [0, 0, 0, 1, 1, 1], kernel=kernel, precision=precision)
+    ev.configure(backend=2)
+    ev.set_source_points(src)
+    ev.set_target_points(trg)
+    ev.set_weights(w)
+    got = ev.evaluate()
+    m = pg.Model(rbf, 0)._c()
+    m.poly_degree = -1
+    empty = np.zeros((0, 3))
+    if kernel == _lib.KERNEL_GRADIENT:
+        want = oracle.direct_evaluate(m, empty, w, trg, gsrc=src)
+    else:
+        want = oracle.direct_evaluate(m, empty, w, empty, gsrc=src, gtrg=trg)
+    scale = np.abs(w).sum() / 3 * max(1.0, np.max(np.abs(want)) / (np.abs(w).sum() / 3))
+    bound = 1e-4 if cls is pg.Biharmonic3D else 1e-3
+    assert np.max(np.abs(got - want)) <= bound * scale, (np.max(np.abs(got - want)), scale)
