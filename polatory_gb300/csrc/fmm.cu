@@ -1005,7 +1005,8 @@ __global__ void __launch_bounds__(128)
                   const int* __restrict__ table, const P4<double>* __restrict__ spos,
                   const double* __restrict__ sw, const Index* __restrict__ sleaf_start,
                   double wleaf, double* __restrict__ out) {
-  __shared__ float s_p[8][128];  // x, y, z, w as (hi, lo)
+  // Sources as (x hi, x lo, y hi, y lo) and (z hi, z lo, w hi, w lo): two 16-byte loads a pair.
+  __shared__ float4 s_a[128], s_b[128];
   __shared__ int s_nb[27];
   const Index leaf = blockIdx.x;
   if (threadIdx.x < 27) s_nb[threadIdx.x] = table[leaf * 27 + threadIdx.x];
@@ -1014,44 +1015,78 @@ __global__ void __launch_bounds__(128)
   ff_split(kp.p1 * kp.p1, c_hi, c_lo);
   const bool reg = kp.p1 != 0.0;
   const Index tb = tleaf_start[leaf], te = tleaf_start[leaf + 1];
-  for (Index i0 = tb; i0 < te; i0 += blockDim.x) {
-    const Index i = i0 + threadIdx.x;
-    const bool active = i < te;
-    const P4<double> t = active ? tpos[i] : P4<double>{0.0, 0.0, 0.0, 0.0};
-    // Warps past the leaf's last target (the tail of a leaf) only help stage the sources.
-    const bool warp_busy = __any_sync(0xffffffffu, active);
-    double tot = 0.0;
+  // NT targets per thread (1 or 2), consecutive, so that threads without targets fill whole
+  // warps, which only help stage the sources.
+  auto pass = [&]<int NT>(Index i0) {
+    bool active[NT];
+    Index idx[NT];
+    P4<double> t[NT];
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < NT; ++q) {
+      idx[q] = i0 + NT * threadIdx.x + q;
+      active[q] = idx[q] < te;
+      any |= active[q];
+      t[q] = active[q] ? tpos[idx[q]] : P4<double>{0.0, 0.0, 0.0, 0.0};
+    }
+    const bool warp_busy = __any_sync(0xffffffffu, any);
+    double tot[NT];
+#pragma unroll
+    for (int q = 0; q < NT; ++q) tot[q] = 0.0;
     for (int nb = 0; nb < 27; ++nb) {
       const int s = s_nb[nb];
       if (s < 0) continue;
-      float txh, txl, tyh, tyl, tzh, tzl;
-      ff_split(t.x - static_cast<double>(nb / 9 - 1) * wleaf, txh, txl);
-      ff_split(t.y - static_cast<double>((nb / 3) % 3 - 1) * wleaf, tyh, tyl);
-      ff_split(t.z - static_cast<double>(nb % 3 - 1) * wleaf, tzh, tzl);
+      float txh[NT], txl[NT], tyh[NT], tyl[NT], tzh[NT], tzl[NT];
+#pragma unroll
+      for (int q = 0; q < NT; ++q) {
+        ff_split(t[q].x - static_cast<double>(nb / 9 - 1) * wleaf, txh[q], txl[q]);
+        ff_split(t[q].y - static_cast<double>((nb / 3) % 3 - 1) * wleaf, tyh[q], tyl[q]);
+        ff_split(t[q].z - static_cast<double>(nb % 3 - 1) * wleaf, tzh[q], tzl[q]);
+      }
       const Index sb = sleaf_start[s], se = sleaf_start[s + 1];
       for (Index base = sb; base < se; base += 128) {
         const int cnt = static_cast<int>(min(static_cast<Index>(128), se - base));
         __syncthreads();
         if (threadIdx.x < cnt) {
           const P4<double> p = spos[base + threadIdx.x];
-          ff_split(p.x, s_p[0][threadIdx.x], s_p[1][threadIdx.x]);
-          ff_split(p.y, s_p[2][threadIdx.x], s_p[3][threadIdx.x]);
-          ff_split(p.z, s_p[4][threadIdx.x], s_p[5][threadIdx.x]);
-          ff_split(sw[base + threadIdx.x], s_p[6][threadIdx.x], s_p[7][threadIdx.x]);
+          float4 a, b;
+          ff_split(p.x, a.x, a.y);
+          ff_split(p.y, a.z, a.w);
+          ff_split(p.z, b.x, b.y);
+          ff_split(sw[base + threadIdx.x], b.z, b.w);
+          s_a[threadIdx.x] = a;
+          s_b[threadIdx.x] = b;
         }
         __syncthreads();
         if (!warp_busy) continue;
-        float ah = 0.0f, al = 0.0f;
+        float ah[NT], al[NT];
+#pragma unroll
+        for (int q = 0; q < NT; ++q) ah[q] = al[q] = 0.0f;
 #pragma unroll 2
-        for (int j = 0; j < cnt; ++j)
-          ff_poly_accumulate<KIND>(txh, txl, tyh, tyl, tzh, tzl, s_p[0][j], s_p[1][j], s_p[2][j],
-                                   s_p[3][j], s_p[4][j], s_p[5][j], s_p[6][j], s_p[7][j], reg,
-                                   c_hi, c_lo, ah, al);
-        tot += static_cast<double>(ah) + static_cast<double>(al);
+        for (int j = 0; j < cnt; ++j) {
+          const float4 a = s_a[j], b = s_b[j];
+#pragma unroll
+          for (int q = 0; q < NT; ++q)
+            ff_poly_accumulate<KIND>(txh[q], txl[q], tyh[q], tyl[q], tzh[q], tzl[q], a.x, a.y, a.z,
+                                     a.w, b.x, b.y, b.z, b.w, reg, c_hi, c_lo, ah[q], al[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < NT; ++q) tot[q] += static_cast<double>(ah[q]) + static_cast<double>(al[q]);
       }
     }
     const double scale = KIND == PGPU_RBF_BH3 ? -kp.p0 : kp.p0;
-    if (active) out[tperm[i]] += scale * tot;
+#pragma unroll
+    for (int q = 0; q < NT; ++q)
+      if (active[q]) out[tperm[idx[q]]] += scale * tot[q];
+  };
+  for (Index i0 = tb; i0 < te;) {
+    if (te - i0 > static_cast<Index>(blockDim.x)) {
+      pass.template operator()<2>(i0);
+      i0 += 2 * blockDim.x;
+    } else {
+      pass.template operator()<1>(i0);
+      i0 += blockDim.x;
+    }
   }
 }
 
