@@ -163,6 +163,19 @@ def run_serving(args):
             plan.append((t_arr, "fit", int(g.integers(n_slots)), log_uniform(g, 1000, 200_000)))
     models = [model_for(g) for _ in range(n_req)]
     tickets = []
+    # Device memory in use (the whole device, from cudaMemGetInfo) sampled through the stream.
+    import torch
+
+    mem = {"max": 0}
+    mem_stop = threading.Event()
+
+    def sample_memory():
+        while not mem_stop.wait(0.5):
+            free, total = torch.cuda.mem_get_info()
+            mem["max"] = max(mem["max"], total - free)
+
+    sampler = threading.Thread(target=sample_memory, daemon=True)
+    sampler.start()
     start = time.perf_counter()
     for (ta, kind, slot, n), m in zip(plan, models):
         delay = start + ta - time.perf_counter()
@@ -187,7 +200,10 @@ def run_serving(args):
         lat[kind].append(latency)
         points += n
     wall = time.perf_counter() - start
+    mem_stop.set()
+    sampler.join()
     stats = server.stats()
+    cache = pg.operator_cache_stats()
     server.close()
     allv = lat["fit"] + lat["evaluate"]
 
@@ -206,6 +222,7 @@ def run_serving(args):
                           "evaluate_p50": pct(lat["evaluate"], 50),
                           "evaluate_p99": pct(lat["evaluate"], 99)},
             "failed": failed, "errors": errors, "peak_bytes": stats["peak_bytes"],
+            "device_used_max_bytes": mem["max"], "operator_cache": cache,
             "timing": "host wall clock from the first arrival to the last completion"}
     print(json.dumps(line), flush=True)
 

@@ -118,6 +118,15 @@ int pgpu_launch_count(int64_t* out);
  * PGPU_TIMEOUT. after <= 0 clears the injection. */
 enum { PGPU_INJECT_ALLOC = 1, PGPU_INJECT_M2L_STALL = 2 };
 int pgpu_debug_inject(int what, int64_t after);
+/* The process-wide cache of far-field (M2L) operators (no reference counterpart): bytes and
+ * entries it holds, and its byte limit. Operators of the homogeneous kernels (bh3, th3) are
+ * stored once for every box; other kernels have one entry per cell radius, which follows the
+ * bounding box of each point set, so the least recently used entries are dropped past the
+ * limit (PGPU_M2L_CACHE_MB in the environment at start-up, 8192 MiB by default). An entry in
+ * use by a running evaluation is freed when that evaluation ends. Any pointer may be NULL.
+ * pgpu_operator_cache_limit sets the limit in bytes (>= 0) and evicts down to it. */
+int pgpu_operator_cache_stats(int64_t* bytes, int64_t* entries, int64_t* limit);
+int pgpu_operator_cache_limit(int64_t bytes);
 /* Synchronizes the library stream of this thread. */
 int pgpu_synchronize(void);
 /* The library's CUDA stream of this thread (a cudaStream_t), for event timing by callers. */

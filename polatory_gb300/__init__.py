@@ -494,6 +494,18 @@ def synchronize() -> None:
     check(lib.pgpu_synchronize())
 
 
+def operator_cache_stats() -> dict:
+    """Bytes and entries of the process-wide far-field operator cache, and its byte limit."""
+    b, e, lim = C.c_int64(), C.c_int64(), C.c_int64()
+    check(lib.pgpu_operator_cache_stats(C.byref(b), C.byref(e), C.byref(lim)))
+    return {"bytes": b.value, "entries": e.value, "limit": lim.value}
+
+
+def set_operator_cache_limit(nbytes: int) -> None:
+    """Sets the far-field operator cache's byte limit and evicts down to it."""
+    check(lib.pgpu_operator_cache_limit(int(nbytes)))
+
+
 def stream_handle() -> int:
     """The library's cudaStream_t of this thread, as an integer handle."""
     out = C.c_void_p()

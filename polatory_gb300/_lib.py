@@ -102,6 +102,8 @@ def _load():
         "pgpu_launch_count": ([C.POINTER(I64)], C.c_int),
         "pgpu_synchronize": ([], C.c_int),
         "pgpu_debug_inject": ([C.c_int, I64], C.c_int),
+        "pgpu_operator_cache_stats": ([C.POINTER(I64), C.POINTER(I64), C.POINTER(I64)], C.c_int),
+        "pgpu_operator_cache_limit": ([I64], C.c_int),
         "pgpu_stream": ([C.POINTER(C.c_void_p)], C.c_int),
         "pgpu_rbf_evaluate": ([C.POINTER(PgpuRbf), P, I64, P, P, P], C.c_int),
         "pgpu_rbf_cpd_order": ([C.POINTER(PgpuRbf), C.POINTER(C.c_int)], C.c_int),

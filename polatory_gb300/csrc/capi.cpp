@@ -21,6 +21,8 @@
 namespace pgpu {
 void set_device(int device);
 void release_cached_memory();
+void m2l_cache_stats(int64_t* bytes, int64_t* entries, int64_t* limit);
+void m2l_cache_set_limit(int64_t bytes);
 int direct_evaluate_noalloc(const pgpu_rbf* rbf, const double* src, int64_t ns,
                             const double* weights, const double* trg, int64_t nt, double* out,
                             cudaStream_t st, const char** msg);
@@ -80,7 +82,7 @@ struct pgpu_interpolant {
   int precision = PGPU_PRECISION_PLAIN;
   bool fitted = false;
   DevBuf<double> centers, grad_centers, weights;
-  std::vector<double> centers_host;
+  std::vector<double> centers_host, grad_centers_host;
   Index mu = 0, sigma = 0;
   Bbox3 bbox;
   pgpu_fit_stats stats{};
@@ -138,6 +140,17 @@ int pgpu_debug_inject(int what, int64_t after) {
       inject_m2l_stall(after);
     else
       throw_invalid("unknown injection");
+  });
+}
+
+int pgpu_operator_cache_stats(int64_t* bytes, int64_t* entries, int64_t* limit) {
+  return guarded([&] { m2l_cache_stats(bytes, entries, limit); });
+}
+
+int pgpu_operator_cache_limit(int64_t bytes) {
+  return guarded([&] {
+    if (bytes < 0) throw_invalid("the limit must be >= 0");
+    m2l_cache_set_limit(bytes);
   });
 }
 
@@ -579,6 +592,17 @@ int pgpu_interpolant_fit(pgpu_interpolant* it, const double* points, int64_t mu,
           auto f = pos.find(std::string(reinterpret_cast<const char*>(&pts[3 * i]), 3 * sizeof(double)));
           if (f != pos.end()) init[i] = iw[f->second];
         }
+        // Gradient centres: their three weights (interpolant.hpp:262-268).
+        std::unordered_map<std::string, Index> gpos;
+        for (Index i = 0; i < initial->sigma; ++i)
+          gpos.emplace(std::string(reinterpret_cast<const char*>(&initial->grad_centers_host[3 * i]),
+                                   3 * sizeof(double)),
+                       i);
+        for (Index i = 0; i < sigma; ++i) {
+          auto f = gpos.find(std::string(reinterpret_cast<const char*>(&gpts[3 * i]), 3 * sizeof(double)));
+          if (f != gpos.end())
+            for (int c = 0; c < 3; ++c) init[mu + 3 * i + c] = iw[initial->mu + 3 * f->second + c];
+        }
         for (int k = 0; k < l; ++k) init[mu + 3 * sigma + k] = iw[iw.size() - l + k];
       }
     }
@@ -609,6 +633,7 @@ int pgpu_interpolant_fit(pgpu_interpolant* it, const double* points, int64_t mu,
     it->sigma = sigma;
     it->bbox = Bbox3::from_host_points(it->centers_host.data(), mu)
                    .hull(Bbox3::from_host_points(gpts.data(), sigma));
+    it->grad_centers_host = std::move(gpts);
     it->stats.iterations = r.iterations;
     it->stats.levels = r.levels;
     it->stats.residual = r.residual;
@@ -1023,6 +1048,7 @@ std::unique_ptr<pgpu_interpolant> deserialize(const std::vector<char>& bytes) {
     pgpu::sync();
   }
   it->centers_host = std::move(pts);
+  it->grad_centers_host = std::move(gpts);
   it->mu = mu;
   it->sigma = sigma;
   it->fitted = fitted;
@@ -1232,6 +1258,7 @@ int pgpu_interpolant_fit_incrementally(pgpu_interpolant* it, const double* point
     it->weights.upload(weights);
     it->centers.upload(cp);
     it->grad_centers.resize(0);
+    it->grad_centers_host.clear();
     it->centers_host = std::move(cp);
     it->mu = mu;
     it->sigma = 0;
@@ -1405,6 +1432,7 @@ int pgpu_interpolant_fit_inequality(pgpu_interpolant* it, const double* points, 
     it->weights.upload(center_weights);
     it->centers.upload(cp);
     it->grad_centers.resize(0);
+    it->grad_centers_host.clear();
     it->centers_host = std::move(cp);
     it->mu = nc;
     it->sigma = 0;

@@ -132,6 +132,9 @@ void copy_in(DevBuf<double>& dst, const double* src, size_t n);
 void copy_out(double* dst, const double* src_dev, size_t n);
 
 inline void sync() { PGPU_CUDA(cudaStreamSynchronize(stream())); }
+// Waits for this thread's stream without throwing (destructors): errors are left for the next
+// checked call.
+void sync_quiet() noexcept;
 
 inline int blocks_for(Index n, int threads) {
   Index b = (n + threads - 1) / threads;

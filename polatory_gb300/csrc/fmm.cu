@@ -18,6 +18,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <list>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -650,6 +652,13 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1)
       }
     }
   }
+}
+
+// x[i] *= s (a level's multipole expansions, for operators stored at radius 1).
+template <class T>
+__global__ void scale_expansions_kernel(T* __restrict__ x, Index n, T s) {
+  const Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) x[i] *= s;
 }
 
 template <class T>
@@ -1292,30 +1301,9 @@ void build_tree(Tree<T>& tr, const SortedPoints& sp, const P4<double>* pos, cons
   }
 }
 
-// Process-wide cache of M2L operator matrices keyed by (kind, params, cell radius, order, type).
-struct KKey {
-  int kind;
-  double p0, p1, r;
-  int p;
-  int tsize;
-  bool operator<(const KKey& o) const {
-    return std::tie(kind, p0, p1, r, p, tsize) < std::tie(o.kind, o.p0, o.p1, o.r, o.p, o.tsize);
-  }
-};
-
-std::mutex g_kcache_mu;
-std::map<KKey, std::shared_ptr<void>> g_kcache;
-
+// M2L operator matrices K_o (the 7^3 offsets, p^3 x p^3 each) between cells of radius r.
 template <class T>
-std::shared_ptr<DevBuf<T>> m2l_matrices(int kind, const KParams<T>& kp, double r, int p,
-                                        bool cache = true) {
-  KKey key{kind, static_cast<double>(kp.p0), static_cast<double>(kp.p1), r, p,
-           static_cast<int>(sizeof(T))};
-  if (cache) {
-    std::lock_guard<std::mutex> lk(g_kcache_mu);
-    auto it = g_kcache.find(key);
-    if (it != g_kcache.end()) return std::static_pointer_cast<DevBuf<T>>(it->second);
-  }
+std::shared_ptr<DevBuf<T>> m2l_matrices(int kind, const KParams<T>& kp, double r, int p) {
   const Index p3 = static_cast<Index>(p) * p * p;
   auto buf = std::make_shared<DevBuf<T>>(static_cast<size_t>(kNOff) * p3 * p3);
   std::vector<double> nodes(p);
@@ -1328,10 +1316,6 @@ std::shared_ptr<DevBuf<T>> m2l_matrices(int kind, const KParams<T>& kp, double r
   });
   PGPU_LAUNCH_CHECK();
   sync();
-  if (cache) {
-    std::lock_guard<std::mutex> lk(g_kcache_mu);
-    g_kcache[key] = buf;
-  }
   return buf;
 }
 
@@ -1481,12 +1465,18 @@ constexpr int kRanks[] = {16, 32, 48, 64, 80, 96, 112, 128};
 template <class T>
 struct M2LOps {
   int n = 0;  // p^3
-  int r = 0;  // padded rank; 0 = dense operators in K
+  int r = 0;  // padded rank; 0 = dense operators
+  // Dense operators; for FP32 at order 6 with the tensor-core M2L on, the head/tail operator
+  // blocks in the MMA layout (tc) replace them.
   std::shared_ptr<DevBuf<T>> K;
-  DevBuf<T> U, V, C;
-  // Tensor-core operator blocks (FP32, order 6), made on first use under tc_mu.
-  std::mutex tc_mu;
   std::shared_ptr<M2LTcBlocks> tc;
+  DevBuf<T> U, V, C;  // low-rank form: K_o ~ U C_o V^T
+  size_t bytes() const {
+    size_t b = (U.size() + V.size() + C.size()) * sizeof(T);
+    if (K) b += K->size() * sizeof(T);
+    if (tc) b += (tc->hi.size() + tc->lo.size()) * sizeof(float);
+    return b;
+  }
 };
 
 struct SvdBasis {
@@ -1494,12 +1484,104 @@ struct SvdBasis {
   std::vector<double> U, V;  // n x r row-major
 };
 
-std::mutex g_ops_mu;
-std::map<std::tuple<int, double, double, double, int, int, double>, std::shared_ptr<void>> g_ops;
-std::map<std::tuple<int, double, double, double, int, double>, std::shared_ptr<SvdBasis>> g_basis;
+// Process-wide cache of M2L operators, keyed by (kind, p0, p1, cell radius, order, element
+// size, eps). The homogeneous kernels (phi(s d) = s^deg phi(d)) are stored at radius 1 and
+// scaled per level by the caller, so one entry serves every box; the others have one entry per
+// radius, and the radius follows each point set's bounding box. The cache therefore keeps the
+// most recently used entries within a byte budget (PGPU_M2L_CACHE_MB, default 8192). An entry
+// dropped from the cache lives on while an FMM holds it; an FMM synchronizes its stream before
+// it lets go of its entries, so whichever holder frees an entry last does so after every launch
+// that read it has finished.
+using OpKey = std::tuple<int, double, double, double, int, int, double>;
 
-// Homogeneous kernels (phi(s d) = s^deg phi(d)): the singular vectors do not depend on the cell
-// radius and C_o scales by r^deg. Returns deg, or -1.
+struct OpCache {
+  std::mutex mu;
+  std::list<OpKey> lru;  // most recently used first
+  struct Slot {
+    std::shared_ptr<void> ops;
+    size_t bytes = 0;
+    std::list<OpKey>::iterator pos;
+  };
+  std::map<OpKey, Slot> slots;
+  size_t bytes = 0;
+  // Bases of the low-rank form (host memory), cleared when they grow past a few dozen.
+  std::map<std::tuple<int, double, double, double, int, double>, std::shared_ptr<SvdBasis>> bases;
+};
+
+OpCache g_op_cache;
+
+size_t& op_cache_budget_ref() {
+  static size_t budget = [] {
+    const char* e = std::getenv("PGPU_M2L_CACHE_MB");
+    const double mb = e ? std::max(std::atof(e), 0.0) : 8192.0;
+    return static_cast<size_t>(mb * 1048576.0);
+  }();
+  return budget;
+}
+
+size_t op_cache_budget() { return op_cache_budget_ref(); }  // g_op_cache.mu held
+
+std::shared_ptr<void> op_cache_find(const OpKey& key) {
+  std::lock_guard<std::mutex> lk(g_op_cache.mu);
+  auto it = g_op_cache.slots.find(key);
+  if (it == g_op_cache.slots.end()) return nullptr;
+  g_op_cache.lru.splice(g_op_cache.lru.begin(), g_op_cache.lru, it->second.pos);
+  return it->second.ops;
+}
+
+// Inserts ops under key (or returns the entry another thread inserted first) and evicts the
+// least recently used entries past the budget; the newest entry always stays.
+std::shared_ptr<void> op_cache_insert(const OpKey& key, std::shared_ptr<void> ops, size_t bytes) {
+  std::vector<std::shared_ptr<void>> evicted;  // released after the lock
+  std::shared_ptr<void> out;
+  {
+    std::lock_guard<std::mutex> lk(g_op_cache.mu);
+    auto it = g_op_cache.slots.find(key);
+    if (it != g_op_cache.slots.end()) {
+      g_op_cache.lru.splice(g_op_cache.lru.begin(), g_op_cache.lru, it->second.pos);
+      out = it->second.ops;
+    } else {
+      g_op_cache.lru.push_front(key);
+      g_op_cache.slots[key] = OpCache::Slot{ops, bytes, g_op_cache.lru.begin()};
+      g_op_cache.bytes += bytes;
+      out = std::move(ops);
+      while (g_op_cache.bytes > op_cache_budget() && g_op_cache.slots.size() > 1) {
+        auto victim = g_op_cache.slots.find(g_op_cache.lru.back());
+        g_op_cache.bytes -= victim->second.bytes;
+        evicted.push_back(std::move(victim->second.ops));
+        g_op_cache.slots.erase(victim);
+        g_op_cache.lru.pop_back();
+      }
+    }
+  }
+  return out;
+}
+
+}  // namespace
+
+void m2l_cache_stats(int64_t* bytes, int64_t* entries, int64_t* limit) {
+  std::lock_guard<std::mutex> lk(g_op_cache.mu);
+  if (bytes) *bytes = static_cast<int64_t>(g_op_cache.bytes);
+  if (entries) *entries = static_cast<int64_t>(g_op_cache.slots.size());
+  if (limit) *limit = static_cast<int64_t>(op_cache_budget());
+}
+
+void m2l_cache_set_limit(int64_t bytes) {
+  std::vector<std::shared_ptr<void>> evicted;  // released after the lock
+  std::lock_guard<std::mutex> lk(g_op_cache.mu);
+  op_cache_budget_ref() = static_cast<size_t>(std::max<int64_t>(bytes, 0));
+  while (g_op_cache.bytes > op_cache_budget() && !g_op_cache.slots.empty()) {
+    auto victim = g_op_cache.slots.find(g_op_cache.lru.back());
+    g_op_cache.bytes -= victim->second.bytes;
+    evicted.push_back(std::move(victim->second.ops));
+    g_op_cache.slots.erase(victim);
+    g_op_cache.lru.pop_back();
+  }
+}
+
+namespace {
+
+// Homogeneous kernels (phi(s d) = s^deg phi(d)): returns deg, or -1.
 int homogeneity_degree(int kind, double c) {
   if (c != 0.0) return -1;
   if (kind == PGPU_RBF_BH3) return 1;
@@ -1507,34 +1589,32 @@ int homogeneity_degree(int kind, double c) {
   return -1;
 }
 
+// The M2L operators for cells of radius r_cell, at radius 1 for homogeneous kernels: the caller
+// multiplies the multipole expansions of the level by *scale (r_cell^deg) before the transfer.
 template <class T>
-std::shared_ptr<M2LOps<T>> m2l_ops(int kind, const KParams<T>& kp, double r_cell, int p, double eps) {
+std::shared_ptr<M2LOps<T>> m2l_ops(int kind, const KParams<T>& kp, double r_cell, int p, double eps,
+                                   double* scale) {
   const int n = p * p * p;
   const double c = static_cast<double>(kp.p1);
   const int deg = homogeneity_degree(kind, c);
-  auto key = std::make_tuple(kind, static_cast<double>(kp.p0), c, r_cell, p,
-                             static_cast<int>(sizeof(T)), eps);
-  {
-    std::lock_guard<std::mutex> lk(g_ops_mu);
-    auto it = g_ops.find(key);
-    if (it != g_ops.end()) return std::static_pointer_cast<M2LOps<T>>(it->second);
-  }
+  const double r0 = deg >= 0 ? 1.0 : r_cell;
+  *scale = deg >= 0 ? std::pow(r_cell, deg) : 1.0;
+  const OpKey key = std::make_tuple(kind, static_cast<double>(kp.p0), c, r0, p,
+                                    static_cast<int>(sizeof(T)), eps);
+  if (auto hit = op_cache_find(key)) return std::static_pointer_cast<M2LOps<T>>(hit);
   auto ops = std::make_shared<M2LOps<T>>();
   ops->n = n;
   if (eps <= 0.0 || p > 6) {
-    ops->K = m2l_matrices<T>(kind, kp, r_cell, p);
+    ops->K = m2l_matrices<T>(kind, kp, r0, p);
   } else {
-    // Radius at which the operators are computed (1 for homogeneous kernels, then scaled).
-    const double r0 = deg >= 0 ? 1.0 : r_cell;
-    const double scale = deg >= 0 ? std::pow(r_cell, deg) : 1.0;
     KParams<double> kd{static_cast<double>(kp.p0), c};
-    auto K64 = m2l_matrices<double>(kind, kd, r0, p, /*cache=*/false);
-    auto bkey = std::make_tuple(kind, static_cast<double>(kp.p0), c, deg >= 0 ? -1.0 : r_cell, p, eps);
+    auto K64 = m2l_matrices<double>(kind, kd, r0, p);
+    auto bkey = std::make_tuple(kind, static_cast<double>(kp.p0), c, r0, p, eps);
     std::shared_ptr<SvdBasis> basis;
     {
-      std::lock_guard<std::mutex> lk(g_ops_mu);
-      auto it = g_basis.find(bkey);
-      if (it != g_basis.end()) basis = it->second;
+      std::lock_guard<std::mutex> lk(g_op_cache.mu);
+      auto it = g_op_cache.bases.find(bkey);
+      if (it != g_op_cache.bases.end()) basis = it->second;
     }
     if (!basis) {
       basis = std::make_shared<SvdBasis>();
@@ -1576,11 +1656,12 @@ std::shared_ptr<M2LOps<T>> m2l_ops(int kind, const KParams<T>& kp, double r_cell
             basis->V[static_cast<size_t>(a) * rp + j] = vec_v[static_cast<size_t>(a) * n + j];
           }
       }
-      std::lock_guard<std::mutex> lk(g_ops_mu);
-      g_basis[bkey] = basis;
+      std::lock_guard<std::mutex> lk(g_op_cache.mu);
+      if (g_op_cache.bases.size() >= 64) g_op_cache.bases.clear();
+      g_op_cache.bases[bkey] = basis;
     }
     if (basis->r == 0) {
-      ops->K = m2l_matrices<T>(kind, kp, r_cell, p);
+      ops->K = m2l_matrices<T>(kind, kp, r0, p);
     } else {
       const int r = basis->r;
       ops->r = r;
@@ -1592,18 +1673,23 @@ std::shared_ptr<M2LOps<T>> m2l_ops(int kind, const KParams<T>& kp, double r_cell
       PGPU_LAUNCH_CHECK();
       ops->C.resize(static_cast<size_t>(kNOff) * r * r);
       const Index nc = static_cast<Index>(kNOff) * r * r;
-      ukv_kernel<T><<<blocks_for(nc, 256), 256, 0, stream()>>>(w.data(), du.data(), n, r, scale,
+      ukv_kernel<T><<<blocks_for(nc, 256), 256, 0, stream()>>>(w.data(), du.data(), n, r, 1.0,
                                                                 ops->C.data());
       PGPU_LAUNCH_CHECK();
       std::vector<T> hu(basis->U.begin(), basis->U.end()), hv(basis->V.begin(), basis->V.end());
       ops->U.upload(hu);
       ops->V.upload(hv);
-      sync();
     }
   }
-  std::lock_guard<std::mutex> lk(g_ops_mu);
-  g_ops[key] = ops;
-  return ops;
+  if constexpr (sizeof(T) == 4) {
+    if (p == 6 && ops->r == 0 && m2l_tc_enabled()) {
+      ops->tc = std::make_shared<M2LTcBlocks>(make_m2l_tc_blocks(ops->K->data()));
+      ops->K.reset();
+    }
+  }
+  sync();  // the entry is read from other threads' streams
+  const size_t bytes = ops->bytes();
+  return std::static_pointer_cast<M2LOps<T>>(op_cache_insert(key, std::move(ops), bytes));
 }
 
 int order_for_accuracy(double accuracy) {
@@ -1646,7 +1732,10 @@ struct Fmm<T>::Impl {
   DevBuf<int> tleaf;  // leaf of each sorted target point (sparse target leaves only)
   DevBuf<int> chunk_leaf;  // P2P chunk -> (target leaf, chunk index within the leaf)
   Index n_chunks = 0;
+  // Shared M2L operators per level (cached process-wide) and the factor each level's multipole
+  // expansions take before the transfer (r^deg for the homogeneous kernels, else 1).
   std::vector<std::shared_ptr<M2LOps<T>>> kmats;
+  std::vector<double> kscale;
   std::vector<DevBuf<T>> M, L, Mt, Lt;  // Mt/Lt: compressed expansions (rank r) when used
   DevBuf<T> sw;
   Index near_pairs = 0;
@@ -1660,6 +1749,16 @@ struct Fmm<T>::Impl {
   bool tc_used = false;
 
   Tree<T>& ttree() { return symmetric ? src : trg; }
+
+  ~Impl() { release_ops(); }
+
+  // Other threads' FMMs read the shared operators: this stream's launches finish before the
+  // references go, so the holder that frees an operator set last frees it unused.
+  void release_ops() {
+    if (kmats.empty()) return;
+    sync_quiet();
+    kmats.clear();
+  }
 
   void ensure_pos64(Tree<T>& tr, const P4<double>* pos_in) {
     if (tr.n == 0 || tr.pos64.size() == static_cast<size_t>(tr.n)) return;
@@ -1718,7 +1817,9 @@ struct Fmm<T>::Impl {
     m2l_table.clear();
     m2l_table.resize(lf + 1);
     m2l_pairs.assign(lf + 1, 0);
+    release_ops();
     kmats.assign(lf + 1, nullptr);
+    kscale.assign(lf + 1, 1.0);
     for (int k = 2; k <= (near_only ? 1 : lf); ++k) {
       const Index n_t = tt.ncell[k];
       m2l_table[k].resize(std::max<Index>(n_t, 1) * kNOff);
@@ -1740,7 +1841,7 @@ struct Fmm<T>::Impl {
       // fits need (eps <= 1e-8 with order 6) the rank exceeds 128 and nothing is gained.
       static const double env_eps = std::getenv("PGPU_M2L_EPS") ? std::atof(std::getenv("PGPU_M2L_EPS")) : 0.0;
       const double eps = env_eps;
-      kmats[k] = m2l_ops<T>(kind, kp, r, p, eps);
+      kmats[k] = m2l_ops<T>(kind, kp, r, p, eps, &kscale[k]);
       if (verbose() && k == lf)
         std::printf("fmm: n %ld -> lf %d, p %d, m2l rank %d\n", static_cast<long>(ns), lf, p,
                     kmats[k]->r);
@@ -1881,6 +1982,14 @@ struct Fmm<T>::Impl {
           ch, src.start[k].data(), src.keys[k + 1].data(), M[k + 1].data(), M[k].data());
       PGPU_LAUNCH_CHECK();
     }
+    // Operators of homogeneous kernels are stored at radius 1: the expansions take r^deg.
+    for (int k = 2; k <= lf; ++k) {
+      const Index n = src.ncell[k] * P3;
+      if (n == 0 || tt.ncell[k] == 0 || kscale[k] == 1.0) continue;
+      scale_expansions_kernel<T><<<blocks_for(n, 256), 256, 0, st>>>(M[k].data(), n,
+                                                                       static_cast<T>(kscale[k]));
+      PGPU_LAUNCH_CHECK();
+    }
     // Transfer + downward pass.
     const size_t smem = (static_cast<size_t>(P3) * (kTT + 1) + 8 * P3) * sizeof(T);
     for (int k = 2; k <= lf; ++k) {
@@ -1897,21 +2006,15 @@ struct Fmm<T>::Impl {
         M2LOps<T>& ops = *kmats[k];
         bool tc = false;
         if constexpr (sizeof(T) == 4 && P3 == 216) {
-          tc = ops.r == 0 && n_t >= m2l_tc_min_cells() && m2l_tc_enabled();
+          tc = ops.tc != nullptr;
           if (tc) {
-            std::shared_ptr<M2LTcBlocks> blocks;
-            {
-              std::lock_guard<std::mutex> lk(ops.tc_mu);
-              if (!ops.tc) ops.tc = std::make_shared<M2LTcBlocks>(make_m2l_tc_blocks(ops.K->data()));
-              blocks = ops.tc;
-            }
             if (!tc_used) {
               tc_err.resize(1);
               tc_err.zero();
               tc_used = true;
             }
             ProfScope ps("fmm_m2l_tc", 2.0 * P3 * P3 * static_cast<double>(m2l_pairs[k]));
-            m2l_tc_apply(*blocks, m2l_table[k].data(), n_t, M[k].data(), L[k].data(),
+            m2l_tc_apply(*ops.tc, m2l_table[k].data(), n_t, M[k].data(), L[k].data(),
                          tc_err.data(), st);
           }
         }

@@ -46,4 +46,9 @@ class Fmm {
   Impl* impl_;
 };
 
+// The process-wide M2L operator cache: bytes and entries held, and its byte limit
+// (PGPU_M2L_CACHE_MB at start-up, 8 GiB by default). Setting the limit evicts down to it.
+void m2l_cache_stats(int64_t* bytes, int64_t* entries, int64_t* limit);
+void m2l_cache_set_limit(int64_t bytes);
+
 }  // namespace pgpu

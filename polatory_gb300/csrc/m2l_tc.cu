@@ -404,8 +404,6 @@ M2LTcBlocks make_m2l_tc_blocks(const float* K) {
   return b;
 }
 
-Index m2l_tc_min_cells() { return 1; }
-
 __global__ void m2l_tc_reduce_kernel(const float* __restrict__ part, int groups, Index n,
                                      float* __restrict__ L) {
   const Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;

@@ -14,8 +14,6 @@ struct M2LTcBlocks {
 bool m2l_tc_enabled();
 // K: 343 x 216 x 216 row-major (target node, source node) operators of one level.
 M2LTcBlocks make_m2l_tc_blocks(const float* K);
-// Levels with fewer target cells stay on the CUDA-core kernel.
-Index m2l_tc_min_cells();
 // L[t] += sum_o K_o M[table[t][o]] for the nt target cells; *err is set if a wait timed out.
 void m2l_tc_apply(const M2LTcBlocks& b, const int* table, Index nt, const float* Ms, float* L,
                   int* err, cudaStream_t st);

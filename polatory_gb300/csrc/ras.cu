@@ -58,6 +58,116 @@ __device__ __forceinline__ double kernel_sum(const RbfSet& rs, const double* x, 
   return s;
 }
 
+// ---- fits with gradient points -------------------------------------------------------------
+// The system's rows are the value points (type -1) followed by three rows per gradient point
+// (types 0-2: the derivative along x, y, z). Domains, level sets and the polynomial points are
+// lists of rows.
+
+// Monomial row (type -1) or its derivative along axis `type`, degree <= 2, in the column order
+// of monomial_basis.hpp:171-247 (entries past the basis size are unused).
+__host__ __device__ inline void poly_row(int type, double x, double y, double z, double* m) {
+  if (type < 0) {
+    const double v[10] = {1.0, x, y, z, x * x, x * y, x * z, y * y, y * z, z * z};
+    for (int k = 0; k < 10; ++k) m[k] = v[k];
+  } else if (type == 0) {
+    const double v[10] = {0.0, 1.0, 0.0, 0.0, 2.0 * x, y, z, 0.0, 0.0, 0.0};
+    for (int k = 0; k < 10; ++k) m[k] = v[k];
+  } else if (type == 1) {
+    const double v[10] = {0.0, 0.0, 1.0, 0.0, 0.0, x, 0.0, 2.0 * y, z, 0.0};
+    for (int k = 0; k < 10; ++k) m[k] = v[k];
+  } else {
+    const double v[10] = {0.0, 0.0, 0.0, 1.0, 0.0, 0.0, x, 0.0, y, 2.0 * z};
+    for (int k = 0; k < 10; ++k) m[k] = v[k];
+  }
+}
+
+// Entry of A between two rows, summed over the RBFs, without the nugget (mat_a.hpp:10-61):
+// value-value phi(A d); value-gradient -(A^T grad phi(A d))_j with d = x (value) - y (gradient
+// point); gradient-gradient -(A^T H(A d) A)_ij with d = y_i - y_j. The gradient of phi at t is
+// g(|t|^2) t and its Hessian ha I + hb t t^T (rbf_gcoef, rbf_hess).
+__host__ __device__ inline double row_entry(const RbfSet& rs, int ta, const double* pa, int tb,
+                                            const double* pb) {
+  if (ta >= 0 && tb < 0) {
+    const int tt = ta;
+    ta = tb;
+    tb = tt;
+    const double* pp = pa;
+    pa = pb;
+    pb = pp;
+  }
+  const double d0 = pa[0] - pb[0], d1 = pa[1] - pb[1], d2 = pa[2] - pb[2];
+  double s = 0;
+  for (int r = 0; r < rs.n; ++r) {
+    const double* a = rs.a[r];
+    const double t0 = a[0] * d0 + a[1] * d1 + a[2] * d2;
+    const double t1 = a[3] * d0 + a[4] * d1 + a[5] * d2;
+    const double t2 = a[6] * d0 + a[7] * d1 + a[8] * d2;
+    const double r2 = t0 * t0 + t1 * t1 + t2 * t2;
+    KParams<double> kp{rs.p0[r], rs.p1[r]};
+    if (ta < 0 && tb < 0) {
+      s += dispatch_kind(rs.kind[r], [&]<int K>() { return rbf_value<K>(r2, kp); });
+    } else if (ta < 0) {
+      const double g = dispatch_kind(rs.kind[r], [&]<int K>() { return rbf_gcoef<K>(r2, kp); });
+      s -= g * (a[tb] * t0 + a[3 + tb] * t1 + a[6 + tb] * t2);
+    } else {
+      double ha = 0, hb = 0;
+      dispatch_kind(rs.kind[r], [&]<int K>() {
+        rbf_hess<K>(r2, kp, ha, hb);
+        return 0;
+      });
+      const double ata = a[ta] * a[tb] + a[3 + ta] * a[3 + tb] + a[6 + ta] * a[6 + tb];
+      const double ua = a[ta] * t0 + a[3 + ta] * t1 + a[6 + ta] * t2;
+      const double ub = a[tb] * t0 + a[3 + tb] * t1 + a[6 + tb] * t2;
+      s -= ha * ata + hb * ua * ub;
+    }
+  }
+  return s;
+}
+
+// Positions and types of the rows: the mu points, then each gradient point three times.
+__global__ void rows_kernel(const double* __restrict__ pts, Index mu, const double* __restrict__ gpts,
+                            Index sigma, double* __restrict__ pos, int* __restrict__ type) {
+  const Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= mu + 3 * sigma) return;
+  const double* p = i < mu ? pts + 3 * i : gpts + 3 * ((i - mu) / 3);
+  pos[3 * i] = p[0];
+  pos[3 * i + 1] = p[1];
+  pos[3 * i + 2] = p[2];
+  type[i] = i < mu ? -1 : static_cast<int>((i - mu) % 3);
+}
+
+// Lagrange rows of every row: the monomial (or derivative) row times the coefficients.
+__global__ void lagrange_rows_kernel(int l, const double* __restrict__ pos, const int* __restrict__ type,
+                                     Index rows, const double* __restrict__ coeffs,
+                                     double* __restrict__ lag) {
+  const Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= rows) return;
+  double m[10];
+  poly_row(type[i], pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], m);
+  for (int c = 0; c < l; ++c) {
+    double s = 0;
+    for (int r = 0; r < l; ++r) s += m[r] * coeffs[r * l + c];
+    lag[i * l + c] = s;
+  }
+}
+
+// u_g[k] = A(poly row k, row g) and v_g = A11 L_g for every row g.
+__global__ void uv_rows_kernel(RbfSet rs, const double* __restrict__ pos, const int* __restrict__ type,
+                               Index rows, const double* __restrict__ poly_pos,
+                               const int* __restrict__ poly_type, int l, const double* __restrict__ a11,
+                               const double* __restrict__ lag, double* __restrict__ u,
+                               double* __restrict__ v) {
+  const Index i = static_cast<Index>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= rows) return;
+  for (int k = 0; k < l; ++k)
+    u[i * l + k] = row_entry(rs, poly_type[k], poly_pos + 3 * k, type[i], pos + 3 * i);
+  for (int k = 0; k < l; ++k) {
+    double s = 0;
+    for (int kk = 0; kk < l; ++kk) s += a11[k * l + kk] * lag[i * l + kk];
+    v[i * l + k] = s;
+  }
+}
+
 // u_i[k] = sum_r K_r(p_k - x_i), v_i = A11 L_i, per global point i.
 __global__ void uv_kernel(RbfSet rs, const double* __restrict__ pts, Index mu,
                           const double* __restrict__ poly_pts, int l,
@@ -192,6 +302,43 @@ __global__ void assemble_kernel(KParams<T> kp, const P4<T>* __restrict__ frame,
       acc += corr;
     }
     *dst = acc;
+  }
+}
+
+// Q^T A Q of every domain of a fit with gradient points (lower tiles, FP64 entries from
+// row_entry, nugget on the value rows' diagonal), with the same correction terms as
+// assemble_kernel; padding rows/columns become identity.
+template <class T>
+__global__ void assemble_rows_kernel(RbfSet rs, const double* __restrict__ pos,
+                                     const int* __restrict__ type, const int* __restrict__ nsz,
+                                     const int* __restrict__ lds, const Index* __restrict__ mat_off,
+                                     T* __restrict__ mats, const Index* __restrict__ pt_off,
+                                     const Index* __restrict__ pts, int l, double nugget,
+                                     const double* __restrict__ lag, const double* __restrict__ u,
+                                     const double* __restrict__ v, int tiles_in_x) {
+  const Index d = tiles_in_x ? blockIdx.y : blockIdx.x;
+  const int n = nsz[d], ld = lds[d];
+  int bi, bj;
+  tile_of(tiles_in_x ? blockIdx.x : blockIdx.y, bi, bj);
+  if (bi * NB >= ld) return;
+  T* m = mats + mat_off[d];
+  const Index* dp = pts + pt_off[d] + l;
+  const int rr = threadIdx.x & 31;
+  const int r = bi * NB + rr;
+  for (int cc = threadIdx.x >> 5; cc < NB; cc += blockDim.x >> 5) {
+    const int c = bj * NB + cc;
+    T* dst = m + r + static_cast<Index>(c) * ld;
+    if (r >= n || c >= n) {
+      *dst = (r == c) ? T(1) : T(0);
+      continue;
+    }
+    const Index gr = dp[r], gc = dp[c];
+    double acc = row_entry(rs, type[gr], pos + 3 * gr, type[gc], pos + 3 * gc);
+    if (r == c && type[gr] < 0) acc += nugget;
+    for (int k = 0; k < l; ++k)
+      acc += -u[gr * l + k] * lag[gc * l + k] - lag[gr * l + k] * u[gc * l + k] +
+             lag[gr * l + k] * v[gc * l + k];
+    *dst = static_cast<T>(acc);
   }
 }
 
@@ -1146,23 +1293,56 @@ RbfSet rbf_set(const ModelDesc& m) {
 template <class T>
 RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* points_host,
                                         const double* points_dev, Index mu, const Bbox3& bbox)
-    : model_(model), l_(model.l()), mu_(mu), bbox_(bbox), points_dev_(points_dev) {
+    : RasPreconditioner(model, points_host, points_dev, mu, nullptr, nullptr, 0, bbox) {}
+
+template <class T>
+RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* points_host,
+                                        const double* points_dev, Index mu,
+                                        const double* grad_host, const double* grad_dev,
+                                        Index sigma, const Bbox3& bbox)
+    : model_(model), l_(model.l()), mu_(mu), sigma_(sigma), rows_(mu + 3 * sigma), bbox_(bbox),
+      points_dev_(points_dev), grad_dev_(grad_dev) {
   constexpr double kFineToCoarseRatio = 10.0;
   constexpr Index kNCoarsestPoints = 2048;
-  n_levels_ = std::max(static_cast<int>(std::ceil(std::log(static_cast<double>(mu_) / kNCoarsestPoints) /
+  n_levels_ = std::max(static_cast<int>(std::ceil(std::log(static_cast<double>(rows_) / kNCoarsestPoints) /
                                                   std::log(kFineToCoarseRatio))),
                        0) +
               1;
   point_idcs_.resize(n_levels_);
+  grad_point_idcs_.resize(n_levels_);
   fine_.resize(n_levels_);
+  {
+    auto& gtop = grad_point_idcs_[n_levels_ - 1];
+    gtop.resize(sigma_);
+    for (Index i = 0; i < sigma_; ++i) gtop[i] = i;
+  }
+  // Degree 1 with one point and gradient points (ras_preconditioner.hpp:80-84): the Lagrange
+  // functionals are the point's value and the first gradient point's derivatives.
+  const bool special = l_ > 0 && model_.poly_degree == 1 && mu_ == 1 && sigma_ >= 1;
+  if (l_ > 0 && mu_ < l_ && !special) throw_invalid("too few points for the polynomial degree");
 
   // Polynomial points and the Lagrange basis (ras_preconditioner.hpp:76-106).
   if (l_ > 0) {
-    poly_idcs_ = unisolvent_point_set(points_host, mu_, model_.poly_degree);
-    std::vector<double> pp;
-    for (auto i : poly_idcs_)
-      for (int k = 0; k < 3; ++k) pp.push_back(points_host[3 * i + k]);
-    lagrange_coeffs_ = lagrange_coeffs(model_.poly_degree, pp.data(), l_);
+    poly_idcs_ = special ? std::vector<Index>{0}
+                         : unisolvent_point_set(points_host, mu_, model_.poly_degree);
+    if (special) {
+      poly_rows_ = {0, mu_, mu_ + 1, mu_ + 2};
+      std::vector<double> rows(static_cast<size_t>(l_) * l_);
+      double m[10];
+      poly_row(-1, points_host[0], points_host[1], points_host[2], m);
+      for (int c = 0; c < l_; ++c) rows[c] = m[c];
+      for (int t = 0; t < 3; ++t) {
+        poly_row(t, grad_host[0], grad_host[1], grad_host[2], m);
+        for (int c = 0; c < l_; ++c) rows[(t + 1) * l_ + c] = m[c];
+      }
+      lagrange_coeffs_ = lagrange_coeffs_of(rows, l_);
+    } else {
+      poly_rows_ = poly_idcs_;
+      std::vector<double> pp;
+      for (auto i : poly_idcs_)
+        for (int k = 0; k < 3; ++k) pp.push_back(points_host[3 * i + k]);
+      lagrange_coeffs_ = lagrange_coeffs(model_.poly_degree, pp.data(), l_);
+    }
     auto& top = point_idcs_[n_levels_ - 1];
     top = poly_idcs_;
     top.reserve(mu_);
@@ -1180,7 +1360,7 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
   // anisotropic RBF (ras_preconditioner.hpp:108-119).
   const bool aniso = model_.rbfs.size() == 1 && !model_.rbfs[0].aniso_is_identity();
   auto n_coarse_of = [&](int level) {
-    const double finest = std::log(static_cast<double>(mu_)) / std::log(kFineToCoarseRatio);
+    const double finest = std::log(static_cast<double>(rows_)) / std::log(kFineToCoarseRatio);
     const double coarsest = std::log(static_cast<double>(kNCoarsestPoints)) / std::log(kFineToCoarseRatio);
     return static_cast<Index>(
         std::pow(kFineToCoarseRatio, coarsest + (level - 1) * (finest - coarsest) / (n_levels_ - 1)));
@@ -1190,17 +1370,25 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
   // then the host divides them (ras_host.cpp, finest first) on a helper thread and publishes
   // each level's domains as soon as they exist, while this thread runs the device set-up of
   // the levels already published.
-  const bool host_division = std::getenv("PGPU_RAS_HOST_DIVIDE") != nullptr;
-  std::vector<double> a_points;
+  const bool host_division = sigma_ > 0 || std::getenv("PGPU_RAS_HOST_DIVIDE") != nullptr;
+  std::vector<double> a_points, a_grad_points;
   const double* div_points = points_host;
+  const double* div_grad_points = grad_host;
   if (host_division && aniso) {
     const double* a = model_.rbfs[0].a;
-    a_points.resize(3 * mu_);
-    for (Index i = 0; i < mu_; ++i) {
-      const double* p = points_host + 3 * i;
-      for (int r = 0; r < 3; ++r) a_points[3 * i + r] = a[3 * r] * p[0] + a[3 * r + 1] * p[1] + a[3 * r + 2] * p[2];
-    }
+    auto transform = [&](const double* in, Index n, std::vector<double>& out) {
+      out.resize(3 * n);
+      for (Index i = 0; i < n; ++i) {
+        const double* p = in + 3 * i;
+        for (int r = 0; r < 3; ++r) out[3 * i + r] = a[3 * r] * p[0] + a[3 * r + 1] * p[1] + a[3 * r + 2] * p[2];
+      }
+    };
+    transform(points_host, mu_, a_points);
     div_points = a_points.data();
+    if (sigma_ > 0) {
+      transform(grad_host, sigma_, a_grad_points);
+      div_grad_points = a_grad_points.data();
+    }
   }
   std::vector<std::vector<Domain>> level_domains(n_levels_);
   std::mutex div_mu;
@@ -1213,20 +1401,19 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
     omp_set_num_threads(omp_threads);
     try {
       for (int level = n_levels_ - 1; level >= 1; --level) {
-        std::vector<Index> no_grad;
         const double t0 = wall_seconds();
         const Index n_coarse = n_coarse_of(level);
         // The coarse points of this level (the next level's point set) are chosen on a second
         // thread while this one divides the level; each takes half of the host threads.
-        std::vector<Index> coarse;
+        std::pair<std::vector<Index>, std::vector<Index>> coarse;
         std::exception_ptr coarse_error;
         const int half = std::max(1, omp_threads / 2);
         std::thread coarse_thread([&] {
           omp_set_num_threads(half);
           try {
-            coarse = DomainDivider::choose_coarse_points(div_points, nullptr, point_idcs_[level],
-                                                         no_grad, poly_idcs_, n_coarse)
-                         .first;
+            coarse = DomainDivider::choose_coarse_points(div_points, div_grad_points,
+                                                         point_idcs_[level], grad_point_idcs_[level],
+                                                         poly_idcs_, n_coarse);
           } catch (...) {
             coarse_error = std::current_exception();
           }
@@ -1234,7 +1421,8 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
         omp_set_num_threads(std::max(1, omp_threads - half));
         double t1 = 0;
         try {
-          DomainDivider divider(div_points, nullptr, point_idcs_[level], no_grad, poly_idcs_);
+          DomainDivider divider(div_points, div_grad_points, point_idcs_[level],
+                                grad_point_idcs_[level], poly_idcs_);
           t1 = wall_seconds();
           std::lock_guard<std::mutex> lk(div_mu);
           level_domains[level] = std::move(divider.domains());
@@ -1252,7 +1440,8 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
                       level, point_idcs_[level].size(), level_domains[level].size(), t1 - t0,
                       wall_seconds() - t0);
         std::lock_guard<std::mutex> lk(div_mu);
-        point_idcs_[level - 1] = std::move(coarse);
+        point_idcs_[level - 1] = std::move(coarse.first);
+        grad_point_idcs_[level - 1] = std::move(coarse.second);
       }
     } catch (...) {
       std::lock_guard<std::mutex> lk(div_mu);
@@ -1280,13 +1469,19 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
 
   // Device-side per-point data.
   const int l = l_;
-  setup_polynomial(points_host, points_dev);
+  if (sigma_ > 0)
+    setup_rows(points_host, grad_host);
+  else
+    setup_polynomial(points_host, points_dev);
 
   if (host_division) {
     for (int level = n_levels_ - 1; level >= 1; --level) {
       wait_level(level);
       fine_[level] = std::make_unique<DomainBatch<T>>();
-      build_batch(*fine_[level], level_domains[level]);
+      if (sigma_ > 0)
+        build_batch_rows(*fine_[level], level_domains[level]);
+      else
+        build_batch(*fine_[level], level_domains[level]);
     }
     divide_thread.join();
     if (div_error) std::rethrow_exception(div_error);
@@ -1319,9 +1514,21 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
     Domain cd;
     cd.point_indices = point_idcs_[0];
     cd.inner_point.assign(cd.point_indices.size(), 1);
+    if (special) {
+      // The coarse grid's first rows are the Lagrange functionals (its polynomial solve inverts
+      // them): the first gradient point leads the coarse gradient points.
+      auto& g = grad_point_idcs_[0];
+      g.erase(std::remove(g.begin(), g.end(), Index{0}), g.end());
+      g.insert(g.begin(), Index{0});
+    }
+    cd.grad_point_indices = grad_point_idcs_[0];
+    cd.inner_grad_point.assign(cd.grad_point_indices.size(), 1);
     std::vector<Domain> v{cd};
-    build_batch(coarse_, v);
-    coarse_n_ = std::max(static_cast<int>(cd.point_indices.size()) - l_, 0);
+    if (sigma_ > 0)
+      build_batch_rows(coarse_, v);
+    else
+      build_batch(coarse_, v);
+    coarse_n_ = std::max(static_cast<int>(cd.point_indices.size() + 3 * cd.grad_point_indices.size()) - l_, 0);
     const int cld = std::max(NB, ((coarse_n_ + NB - 1) / NB) * NB);
     // With several levels the coarse grid is solved 2L-1 times per application: keep an explicit
     // inverse (one matrix-vector product per solve). A single-level preconditioner solves once
@@ -1340,40 +1547,53 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
     coarse_out_.zero();
   }
 
-  // Level point sets on the device (for the residual-update evaluators).
+  // Level row sets on the device (for the residual-update evaluators): the level's points,
+  // then three rows per gradient point.
   level_idx_dev_.resize(n_levels_);
   level_pts_dev_.resize(n_levels_);
+  level_grad_pts_dev_.resize(n_levels_);
   for (int level = 0; level < n_levels_; ++level) {
     const auto& idx = point_idcs_[level];
-    level_idx_dev_[level].upload(idx);
+    const auto& gidx = grad_point_idcs_[level];
+    std::vector<Index> rows(idx);
+    for (Index j : gidx)
+      for (int c = 0; c < 3; ++c) rows.push_back(mu_ + 3 * j + c);
+    level_idx_dev_[level].upload(rows);
     std::vector<double> lp(3 * idx.size());
     for (size_t i = 0; i < idx.size(); ++i)
       for (int k = 0; k < 3; ++k) lp[3 * i + k] = points_host[3 * idx[i] + k];
     level_pts_dev_[level].upload(lp);
+    if (!gidx.empty()) {
+      std::vector<double> gp(3 * gidx.size());
+      for (size_t i = 0; i < gidx.size(); ++i)
+        for (int k = 0; k < 3; ++k) gp[3 * i + k] = grad_host[3 * gidx[i] + k];
+      level_grad_pts_dev_[level].upload(gp);
+    }
   }
 
   if (n_levels_ > 1 && l > 0) {
     // Orthonormalised monomials and their images (ras_preconditioner.hpp:168-188).
-    p_.resize(mu_ * l);
-    monomial_basis(model_.poly_degree, points_dev, mu_, nullptr, 0, p_.data());
+    const Index R = rows_;
+    p_.resize(R * l);
+    monomial_basis(model_.poly_degree, points_dev, mu_, grad_dev_, sigma_, p_.data());
     for (int i = 0; i < l; ++i) {
-      double* ci = p_.data() + static_cast<Index>(i) * mu_;
-      double nrm = norm2(ci, mu_);
-      scal(mu_, 1.0 / nrm, ci);
+      double* ci = p_.data() + static_cast<Index>(i) * R;
+      double nrm = norm2(ci, R);
+      scal(R, 1.0 / nrm, ci);
       for (int j = i + 1; j < l; ++j) {
-        double* cj = p_.data() + static_cast<Index>(j) * mu_;
-        axpy(mu_, -dot(ci, cj, mu_), ci, cj);
+        double* cj = p_.data() + static_cast<Index>(j) * R;
+        axpy(R, -dot(ci, cj, R), ci, cj);
       }
     }
-    ap_.resize(mu_ * l);
+    ap_.resize(R * l);
     Evaluator<T> ev(model_, bbox_, INFINITY, INFINITY);
-    ev.set_points(points_dev, mu_, nullptr, 0);
-    DevBuf<double> w(mu_ + l);
+    ev.set_points(points_dev, mu_, grad_dev_, sigma_);
+    DevBuf<double> w(R + l);
     for (int i = 0; i < l; ++i) {
       w.zero();
-      copy(w.data(), p_.data() + static_cast<Index>(i) * mu_, mu_);
+      copy(w.data(), p_.data() + static_cast<Index>(i) * R, R);
       ev.set_weights(w.data());
-      ev.evaluate(ap_.data() + static_cast<Index>(i) * mu_, false);
+      ev.evaluate(ap_.data() + static_cast<Index>(i) * R, false);
     }
   }
   if (verbose()) {
@@ -1381,12 +1601,84 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
     std::printf("ras device setup (lagrange, factors, coarse inverse, AP) %.3f s\n",
                 wall_seconds() - t_dev);
   }
-  work_res_.resize(mu_);
-  work_w_.resize(mu_ + l);
-  work_tot_.resize(mu_ + l);
-  work_fit_.resize(mu_);
-  work_src_w_.resize(mu_ + l);
+  work_res_.resize(rows_);
+  work_w_.resize(rows_ + l);
+  work_tot_.resize(rows_ + l);
+  work_fit_.resize(rows_);
+  work_src_w_.resize(rows_ + l);
   sync();
+}
+
+// Rows of a fit with gradient points: positions and types on the device, the Lagrange rows,
+// u and v over all rows, and A11 among the polynomial rows (with the nugget on value rows).
+template <class T>
+void RasPreconditioner<T>::setup_rows(const double* points_host, const double* grad_host) {
+  const Index R = rows_;
+  const int l = l_;
+  row_pos_.resize(3 * R);
+  row_type_.resize(R);
+  rows_kernel<<<blocks_for(R, 256), 256, 0, stream()>>>(points_dev_, mu_, grad_dev_, sigma_,
+                                                        row_pos_.data(), row_type_.data());
+  PGPU_LAUNCH_CHECK();
+  if (l == 0) return;
+  auto row_of = [&](Index g, double* p) {
+    const double* src = g < mu_ ? points_host + 3 * g : grad_host + 3 * ((g - mu_) / 3);
+    p[0] = src[0];
+    p[1] = src[1];
+    p[2] = src[2];
+    return g < mu_ ? -1 : static_cast<int>((g - mu_) % 3);
+  };
+  std::vector<double> ppos(3 * l);
+  std::vector<int> ptype(l);
+  for (int k = 0; k < l; ++k) ptype[k] = row_of(poly_rows_[k], ppos.data() + 3 * k);
+  const RbfSet rs = rbf_set(model_);
+  a11_.assign(l * l, 0.0);
+  for (int i = 0; i < l; ++i)
+    for (int j = 0; j < l; ++j)
+      a11_[i * l + j] = row_entry(rs, ptype[i], ppos.data() + 3 * i, ptype[j], ppos.data() + 3 * j) +
+                        ((i == j && ptype[i] < 0) ? model_.nugget : 0.0);
+  DevBuf<double> coeffs, dpp, da11;
+  DevBuf<int> dpt;
+  coeffs.upload(lagrange_coeffs_);
+  dpp.upload(ppos);
+  dpt.upload(ptype);
+  da11.upload(a11_);
+  lagrange_.resize(R * l);
+  lagrange_rows_kernel<<<blocks_for(R, 256), 256, 0, stream()>>>(l, row_pos_.data(), row_type_.data(),
+                                                                 R, coeffs.data(), lagrange_.data());
+  PGPU_LAUNCH_CHECK();
+  u_.resize(R * l);
+  v_.resize(R * l);
+  uv_rows_kernel<<<blocks_for(R, 128), 128, 0, stream()>>>(rs, row_pos_.data(), row_type_.data(), R,
+                                                           dpp.data(), dpt.data(), l, da11.data(),
+                                                           lagrange_.data(), u_.data(), v_.data());
+  PGPU_LAUNCH_CHECK();
+  sync();
+}
+
+// Domains of a fit with gradient points as row lists: the points (polynomial points first),
+// then the three rows of each gradient point, each row inheriting its point's inner flag
+// (fine_grid.hpp:63-70).
+template <class T>
+template <class U>
+void RasPreconditioner<T>::build_batch_rows(DomainBatch<U>& b, const std::vector<Domain>& domains) {
+  std::vector<Index> sizes, pts;
+  std::vector<char> inner;
+  for (const auto& dom : domains) {
+    sizes.push_back(dom.num_points() + 3 * dom.num_grad_points());
+    pts.insert(pts.end(), dom.point_indices.begin(), dom.point_indices.end());
+    inner.insert(inner.end(), dom.inner_point.begin(), dom.inner_point.end());
+    for (Index i = 0; i < dom.num_grad_points(); ++i)
+      for (int c = 0; c < 3; ++c) {
+        pts.push_back(mu_ + 3 * dom.grad_point_indices[i] + c);
+        inner.push_back(dom.inner_grad_point[i]);
+      }
+  }
+  DevBuf<Index> dpts;
+  DevBuf<char> dinner;
+  dpts.upload(pts);
+  dinner.upload(inner);
+  build_batch(b, sizes, std::move(dpts), std::move(dinner));
 }
 
 template <class T>
@@ -1440,14 +1732,16 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
                                         const double* points_dev, Index mu,
                                         const std::vector<Index>& order,
                                         const std::vector<char>& inner, bool coarse_inverse)
-    : model_(model), l_(model.l()), mu_(mu), n_levels_(2),
+    : model_(model), l_(model.l()), mu_(mu), rows_(mu), n_levels_(2),
       bbox_(Bbox3::from_host_points(points_host, mu)), points_dev_(points_dev) {
   if (static_cast<Index>(order.size()) != mu || static_cast<Index>(inner.size()) != mu)
     throw_invalid("order and inner must have one entry per point");
   if (mu < l_) throw_invalid("too few points for the polynomial degree");
   point_idcs_.resize(2);
+  grad_point_idcs_.resize(2);
   fine_.resize(2);
   poly_idcs_.assign(order.begin(), order.begin() + l_);
+  poly_rows_ = poly_idcs_;
   if (l_ > 0) {
     std::vector<double> pp;
     for (auto i : poly_idcs_)
@@ -1551,11 +1845,23 @@ void RasPreconditioner<T>::build_batch(DomainBatch<U>& b, const std::vector<Inde
   b.info.zero();
   if (b.n_dom == 0) return;
 
-  // Assembly, one pass per RBF in its own frame.
+  // Assembly, one pass per RBF in its own frame (fits with gradient points: one pass over the
+  // rows with every RBF).
   ProfScope ps(sizeof(U) == 4 ? "ras_factor_f32" : "ras_factor_f64", b.factor_flops);
   const int nbmax = b.max_n / NB;
   const Index ntiles = static_cast<Index>(nbmax) * (nbmax + 1) / 2;
-  for (size_t r = 0; r < model_.rbfs.size(); ++r) {
+  if (sigma_ > 0) {
+    const int tiles_in_x = b.n_dom <= 65535 ? 1 : 0;
+    if (!tiles_in_x && ntiles > 65535) throw_runtime("domain too large for the batched assembly");
+    const dim3 grid = tiles_in_x ? dim3(static_cast<unsigned>(ntiles), static_cast<unsigned>(b.n_dom))
+                                 : dim3(static_cast<unsigned>(b.n_dom), static_cast<unsigned>(ntiles));
+    assemble_rows_kernel<U><<<grid, 256, 0, stream()>>>(
+        rbf_set(model_), row_pos_.data(), row_type_.data(), b.n.data(), b.ld.data(),
+        b.mat_off.data(), b.mats.data(), b.pt_off.data(), b.pts.data(), l, model_.nugget,
+        lagrange_.data(), u_.data(), v_.data(), tiles_in_x);
+    PGPU_LAUNCH_CHECK();
+  }
+  for (size_t r = 0; r < model_.rbfs.size() && sigma_ == 0; ++r) {
     const auto& rb = model_.rbfs[r];
     Mat3 a;
     for (int k = 0; k < 9; ++k) a.a[k] = rb.a[k];
@@ -1664,7 +1970,7 @@ void RasPreconditioner<T>::build_batch(DomainBatch<U>& b, const std::vector<Inde
 
 template <class T>
 void RasPreconditioner<T>::solve_level(int level, const double* residuals, double* weights) {
-  fill(weights, mu_ + l_, 0.0);
+  fill(weights, rows_ + l_, 0.0);
   if (level > 0) {
     DomainBatch<T>& b = *fine_[level];
     if (b.n_dom == 0) return;
@@ -1716,7 +2022,7 @@ void RasPreconditioner<T>::solve_level(int level, const double* residuals, doubl
     std::vector<double> c(l, 0.0);
     for (int i = 0; i < l; ++i)
       for (int k = 0; k < l; ++k) c[i] += lagrange_coeffs_[i * l + k] * rhs[k];
-    PGPU_CUDA(cudaMemcpyAsync(weights + mu_, c.data(), l * sizeof(double), cudaMemcpyHostToDevice,
+    PGPU_CUDA(cudaMemcpyAsync(weights + rows_, c.data(), l * sizeof(double), cudaMemcpyHostToDevice,
                               stream()));
     sync();
   }
@@ -1729,9 +2035,13 @@ Evaluator<T>& RasPreconditioner<T>::evaluator(int src_level, int trg_level) {
   if (it == evaluators_.end()) {
     auto ev = std::make_unique<Evaluator<T>>(model_, bbox_, INFINITY, INFINITY);
     ev->set_sources(level_pts_dev_[src_level].data(),
-                    static_cast<Index>(point_idcs_[src_level].size()), nullptr, 0);
+                    static_cast<Index>(point_idcs_[src_level].size()),
+                    level_grad_pts_dev_[src_level].data(),
+                    static_cast<Index>(grad_point_idcs_[src_level].size()));
     ev->set_targets(level_pts_dev_[trg_level].data(),
-                    static_cast<Index>(point_idcs_[trg_level].size()), nullptr, 0);
+                    static_cast<Index>(point_idcs_[trg_level].size()),
+                    level_grad_pts_dev_[trg_level].data(),
+                    static_cast<Index>(grad_point_idcs_[trg_level].size()));
     it = evaluators_.emplace(key, std::move(ev)).first;
   }
   return *it->second;
@@ -1740,10 +2050,10 @@ Evaluator<T>& RasPreconditioner<T>::evaluator(int src_level, int trg_level) {
 template <class T>
 void RasPreconditioner<T>::update_residuals(int src_level, int trg_level, const double* weights,
                                             double* residuals) {
-  const Index ns = static_cast<Index>(point_idcs_[src_level].size());
-  const Index nt = static_cast<Index>(point_idcs_[trg_level].size());
+  const Index ns = static_cast<Index>(point_idcs_[src_level].size() + 3 * grad_point_idcs_[src_level].size());
+  const Index nt = static_cast<Index>(point_idcs_[trg_level].size() + 3 * grad_point_idcs_[trg_level].size());
   gather(weights, level_idx_dev_[src_level].data(), ns, work_src_w_.data());
-  if (l_ > 0) copy(work_src_w_.data() + ns, weights + mu_, l_);
+  if (l_ > 0) copy(work_src_w_.data() + ns, weights + rows_, l_);
   auto& ev = evaluator(src_level, trg_level);
   ev.set_weights(work_src_w_.data());
   ev.evaluate(work_fit_.data());
@@ -1755,45 +2065,46 @@ template <class T>
 void RasPreconditioner<T>::orthogonalize(double* weights, double* residuals) {
   if (l_ == 0) return;
   std::vector<double> dotv(l_);
-  tall_gemv_t(p_.data(), mu_, l_, weights, dotv.data());
+  tall_gemv_t(p_.data(), rows_, l_, weights, dotv.data());
   std::vector<double> neg(l_);
   for (int k = 0; k < l_; ++k) neg[k] = -dotv[k];
-  tall_gemv_add(p_.data(), mu_, l_, neg.data(), weights);
-  tall_gemv_add(ap_.data(), mu_, l_, dotv.data(), residuals);
+  tall_gemv_add(p_.data(), rows_, l_, neg.data(), weights);
+  tall_gemv_add(ap_.data(), rows_, l_, dotv.data(), residuals);
 }
 
 template <class T>
 void RasPreconditioner<T>::apply(const double* v, double* out) {
   double* r = work_res_.data();
-  copy(r, v, mu_);
+  const Index M = rows_ + l_;
+  copy(r, v, rows_);
   if (n_levels_ == 1) {
     solve_level(0, r, out);
     return;
   }
   double* w = work_w_.data();
   double* tot = out;
-  fill(tot, mu_ + l_, 0.0);
+  fill(tot, M, 0.0);
   const int L = n_levels_;
   solve_level(0, r, w);
   update_residuals(0, L - 1, w, r);
-  axpy(mu_ + l_, 1.0, w, tot);
+  axpy(M, 1.0, w, tot);
   for (int level = 1; level < L - 1; ++level) {
     solve_level(level, r, w);
     update_residuals(level, L - 1, w, r);
-    axpy(mu_ + l_, 1.0, w, tot);
+    axpy(M, 1.0, w, tot);
     orthogonalize(tot, r);
     solve_level(0, r, w);
     update_residuals(0, L - 1, w, r);
-    axpy(mu_ + l_, 1.0, w, tot);
+    axpy(M, 1.0, w, tot);
   }
   for (int level = L - 1; level >= 1; --level) {
     solve_level(level, r, w);
     update_residuals(level, level - 1, w, r);
-    axpy(mu_ + l_, 1.0, w, tot);
+    axpy(M, 1.0, w, tot);
     orthogonalize(tot, r);
     solve_level(0, r, w);
     if (level > 1) update_residuals(0, level - 1, w, r);
-    axpy(mu_ + l_, 1.0, w, tot);
+    axpy(M, 1.0, w, tot);
   }
 }
 

@@ -40,6 +40,12 @@ class RasPreconditioner {
   // points_host / points_dev: the mu data points (xyz rows). Value points only.
   RasPreconditioner(const ModelDesc& model, const double* points_host, const double* points_dev,
                     Index mu, const Bbox3& bbox);
+  // With sigma gradient points (grad_host / grad_dev): the system has mu + 3 sigma rows, the
+  // gradient point j owning rows mu + 3 j .. + 2 (ras_preconditioner.hpp:56-189 with
+  // grad_points). The levels are divided on the host (the device division is value-only).
+  RasPreconditioner(const ModelDesc& model, const double* points_host, const double* points_dev,
+                    Index mu, const double* grad_host, const double* grad_dev, Index sigma,
+                    const Bbox3& bbox);
   // One domain holding all points, for the component tests of the fine and coarse grids:
   // `order` lists the points (the first l are the polynomial points), `inner` the fine-grid
   // inner flags per entry of `order`; coarse_inverse keeps the coarse grid as an explicit inverse.
@@ -51,12 +57,12 @@ class RasPreconditioner {
   // coefficients) or as a fine-grid domain (weights of the inner points).
   void solve_domain(bool coarse, const double* residuals, double* weights);
 
-  // out (M) = RAS(v (M)), M = mu + l (ras_preconditioner.hpp:191-250).
+  // out (M) = RAS(v (M)), M = mu + 3 sigma + l (ras_preconditioner.hpp:191-250).
   void apply(const double* v, double* out);
 
   int levels() const { return n_levels_; }
   Index n_domains() const;
-  Index size() const { return mu_ + l_; }
+  Index size() const { return rows_ + l_; }
 
  private:
   void setup_polynomial(const double* points_host, const double* points_dev);
@@ -71,13 +77,26 @@ class RasPreconditioner {
                    DevBuf<char>&& inner);
   Evaluator<T>& evaluator(int src_level, int trg_level);
 
+  // Fits with gradient points: the rows' positions and types and the gradient-point sets.
+  void setup_rows(const double* points_host, const double* grad_host);
+  template <class U>
+  void build_batch_rows(DomainBatch<U>& b, const std::vector<Domain>& domains);
+
   ModelDesc model_;
   int l_;
   Index mu_;
+  Index sigma_ = 0;
+  Index rows_ = 0;  // mu + 3 sigma
   int n_levels_;
   Bbox3 bbox_;
   const double* points_dev_;
+  const double* grad_dev_ = nullptr;
   std::vector<Index> poly_idcs_;
+  std::vector<Index> poly_rows_;  // rows of the polynomial (Lagrange) functionals
+  DevBuf<double> row_pos_;        // gradient fits: rows x 3
+  DevBuf<int> row_type_;          // gradient fits: -1 value, 0-2 derivative axis
+  std::vector<std::vector<Index>> grad_point_idcs_;
+  std::vector<DevBuf<double>> level_grad_pts_dev_;
   std::vector<double> lagrange_coeffs_;  // l x l row-major inverse of the poly-point monomials
   std::vector<double> a11_;              // A restricted to the polynomial points (l x l)
   std::vector<std::vector<Index>> point_idcs_;

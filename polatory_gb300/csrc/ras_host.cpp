@@ -723,6 +723,13 @@ std::vector<double> lagrange_coeffs(int degree, const double* poly_points, Index
   return inv;
 }
 
+std::vector<double> lagrange_coeffs_of(const std::vector<double>& rows, Index l) {
+  std::vector<double> inv;
+  if (!full_piv_inverse(rows, static_cast<int>(l), inv))
+    throw_invalid("the set of points is not unisolvent");
+  return inv;
+}
+
 std::vector<Index> unisolvent_point_set(const double* points, Index n, int degree) {
   std::vector<Index> out;
   if (degree < 0) return out;

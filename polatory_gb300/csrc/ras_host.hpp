@@ -80,5 +80,8 @@ std::vector<Index> unisolvent_point_set(const double* points, Index n, int degre
 // Throws invalid_argument "the set of points is not unisolvent".
 std::vector<double> lagrange_coeffs(int degree, const double* poly_points, Index l,
                                     double* rcond_out = nullptr);
+// The same from the l x l matrix of monomial rows (value rows or gradient-component rows; the
+// special case of lagrange_basis.hpp:36-37: one point and one gradient point at degree 1).
+std::vector<double> lagrange_coeffs_of(const std::vector<double>& rows, Index l);
 
 }  // namespace pgpu

@@ -97,6 +97,10 @@ void dev_free(void* p, size_t bytes) {
   if (cudaFreeAsync(p, s) != cudaSuccess) cudaGetLastError();
 }
 
+void sync_quiet() noexcept {
+  if (g_ctx.initialized) cudaStreamSynchronize(g_ctx.stream);
+}
+
 int64_t thread_device_bytes() { return g_thread_bytes; }
 int64_t thread_device_peak() { return g_thread_peak; }
 void reset_thread_device_peak() { g_thread_peak = g_thread_bytes; }

@@ -238,6 +238,11 @@ struct pgpu_server {
       m = versions.at(it.dep);
       --version_refs[it.dep];
     }
+    // Other workers may read the model too: if this evaluation throws with launches in flight,
+    // they finish before the model's reference is dropped (the last holder frees it).
+    struct SyncOnExit {
+      ~SyncOnExit() { sync_quiet(); }
+    } sync_on_exit;
     const pgpu_request& r = it.req;
     DevBuf<double> q, out;
     copy_in(q, r.points, 3 * r.n);

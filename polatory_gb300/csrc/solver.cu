@@ -43,12 +43,15 @@ bool mixed_pays(double sources, double targets) { return sources * targets > kMi
 template <class T>
 class Operator {
  public:
+  // With sigma gradient points the rows are the mu values then 3 sigma derivatives, and P
+  // has mu + 3 sigma rows.
   Operator(const ModelDesc& model, const double* pts_dev, Index mu, const Bbox3& bbox,
-           double accuracy, const double* P)
-      : model_(model), mu_(mu), l_(model.l()), ev_(model, bbox, accuracy, accuracy), P_(P) {
-    ev_.set_points(pts_dev, mu, nullptr, 0);
+           double accuracy, const double* P, const double* grad_dev = nullptr, Index sigma = 0)
+      : model_(model), mu_(mu), rows_(mu + 3 * sigma), l_(model.l()),
+        ev_(model, bbox, accuracy, accuracy), P_(P) {
+    ev_.set_points(pts_dev, mu, grad_dev, sigma);
   }
-  Index size() const { return mu_ + l_; }
+  Index size() const { return rows_ + l_; }
   // Far-field interpolation order of the operator's FMM (0: from the accuracy).
   void set_order(int p) {
     FarFieldConfig c;
@@ -61,12 +64,12 @@ class Operator {
     if (model_.nugget != 0.0) axpy(mu_, model_.nugget, w, y);
     if (l_ > 0) {
       std::vector<double> c(l_), pt(l_);
-      PGPU_CUDA(cudaMemcpyAsync(c.data(), w + mu_, l_ * sizeof(double), cudaMemcpyDeviceToHost,
+      PGPU_CUDA(cudaMemcpyAsync(c.data(), w + rows_, l_ * sizeof(double), cudaMemcpyDeviceToHost,
                                 stream()));
       sync();
-      tall_gemv_add(P_, mu_, l_, c.data(), y);
-      tall_gemv_t(P_, mu_, l_, w, pt.data());
-      PGPU_CUDA(cudaMemcpyAsync(y + mu_, pt.data(), l_ * sizeof(double), cudaMemcpyHostToDevice,
+      tall_gemv_add(P_, rows_, l_, c.data(), y);
+      tall_gemv_t(P_, rows_, l_, w, pt.data());
+      PGPU_CUDA(cudaMemcpyAsync(y + rows_, pt.data(), l_ * sizeof(double), cudaMemcpyHostToDevice,
                                 stream()));
       sync();
     }
@@ -76,6 +79,7 @@ class Operator {
  private:
   const ModelDesc& model_;
   Index mu_;
+  Index rows_;
   int l_;
   Evaluator<T> ev_;
   const double* P_;
@@ -175,21 +179,28 @@ class Fgmres {
 struct Convergence {
   bool converged = false;
   double residual = 0;
+  double grad_residual = 0;
   bool exact = false;
   double probe_rms = 0;  // root mean square of the exact residual at the probe points
 };
 
-// ResidualEvaluator (residual_evaluator.hpp:56-151), value points only.
+// ResidualEvaluator (residual_evaluator.hpp:56-151). With gradient points the values hold
+// mu values then 3 sigma derivatives, and the gradient residual is checked against its own
+// tolerance.
 class ResidualEvaluator {
  public:
   static constexpr Index kDirectTargets = 1024;
 
   ResidualEvaluator(const ModelDesc& model, const double* pts_dev, const double* pts_host, Index mu,
-                    const Bbox3& bbox, double accuracy, const double* values_host, int precision)
-      : model_(model), mu_(mu), l_(model.l()), pts_dev_(pts_dev), bbox_(bbox), accuracy_(accuracy),
+                    const Bbox3& bbox, double accuracy, const double* values_host, int precision,
+                    const double* grad_dev = nullptr, const double* grad_host = nullptr,
+                    Index sigma = 0, double grad_accuracy = INFINITY)
+      : model_(model), mu_(mu), sigma_(sigma), l_(model.l()), pts_dev_(pts_dev),
+        grad_dev_(grad_dev), bbox_(bbox), accuracy_(accuracy), grad_accuracy_(grad_accuracy),
         precision_(precision) {
     // Probe points: std::shuffle with a default-seeded std::mt19937, then the non-zero values
-    // first (residual_evaluator.hpp:119-124).
+    // first (residual_evaluator.hpp:119-124); the gradient points the same way with a fresh
+    // generator, non-zero gradients first (:126-132).
     std::vector<Index> idx(mu_);
     std::iota(idx.begin(), idx.end(), Index{0});
     std::shuffle(idx.begin(), idx.end(), std::mt19937{});
@@ -197,15 +208,30 @@ class ResidualEvaluator {
     n_probe_ = std::min(mu_, kDirectTargets);
     idx.resize(n_probe_);
     probe_idx_.upload(idx);
-    std::vector<double> pp(3 * n_probe_), pv(n_probe_);
+    std::vector<Index> gidx(sigma_);
+    std::iota(gidx.begin(), gidx.end(), Index{0});
+    std::shuffle(gidx.begin(), gidx.end(), std::mt19937{});
+    std::partition(gidx.begin(), gidx.end(), [&](Index j) {
+      const double* g = values_host + mu_ + 3 * j;
+      return g[0] != 0.0 || g[1] != 0.0 || g[2] != 0.0;
+    });
+    n_gprobe_ = std::min(sigma_, kDirectTargets);
+    gidx.resize(n_gprobe_);
+    std::vector<double> pp(3 * n_probe_), pv(n_probe_ + 3 * n_gprobe_), gp(3 * n_gprobe_);
     for (Index i = 0; i < n_probe_; ++i) {
       for (int k = 0; k < 3; ++k) pp[3 * i + k] = pts_host[3 * idx[i] + k];
       pv[i] = values_host[idx[i]];
     }
+    for (Index j = 0; j < n_gprobe_; ++j)
+      for (int k = 0; k < 3; ++k) {
+        gp[3 * j + k] = grad_host[3 * gidx[j] + k];
+        pv[n_probe_ + 3 * j + k] = values_host[mu_ + 3 * gidx[j] + k];
+      }
     probe_pts_.upload(pp);
+    probe_grad_pts_.upload(gp);
     probe_values_.upload(pv);
-    values_.upload(values_host, mu_);
-    fit_.resize(std::max<Index>(mu_, 1));
+    values_.upload(values_host, mu_ + 3 * sigma_);
+    fit_.resize(std::max<Index>(mu_ + 3 * sigma_, 1));
     tmp_.resize(std::max<Index>(n_probe_, 1));
   }
 
@@ -234,7 +260,7 @@ class ResidualEvaluator {
   Index n_probe() const { return n_probe_; }
   const Index* probe_idx() const { return probe_idx_.data(); }
 
-  Convergence converged(const double* w, double tol) {
+  Convergence converged(const double* w, double tol, double grad_tol = INFINITY) {
     Convergence cv;
     const double nugget = model_.nugget;
     // Stage 1: exact FP64 sums at the probe points (both precisions: the convergence test is
@@ -247,10 +273,12 @@ class ResidualEvaluator {
         axpy(n_probe_, nugget, tmp_.data(), fit_.data());
       }
       cv.residual = inf_norm_diff(fit_.data(), probe_values_.data(), n_probe_);
+      cv.grad_residual = inf_norm_diff(fit_.data() + n_probe_, probe_values_.data() + n_probe_,
+                                       3 * n_gprobe_);
       axpby(n_probe_, 1.0, probe_values_.data(), -1.0, fit_.data());
-      cv.probe_rms = norm2(fit_.data(), n_probe_) / std::sqrt(static_cast<double>(n_probe_));
-      cv.exact = n_probe_ == mu_;
-      if (cv.residual > tol) return cv;
+      cv.probe_rms = norm2(fit_.data(), n_probe_) / std::sqrt(static_cast<double>(std::max<Index>(n_probe_, 1)));
+      cv.exact = n_probe_ == mu_ && n_gprobe_ == sigma_;
+      if (cv.residual > tol || cv.grad_residual > grad_tol) return cv;
       if (cv.exact) {
         cv.converged = true;
         return cv;
@@ -261,8 +289,9 @@ class ResidualEvaluator {
     full().evaluate(fit_.data());
     if (nugget != 0.0) axpy(mu_, nugget, w, fit_.data());
     cv.residual = inf_norm_diff(fit_.data(), values_.data(), mu_);
+    cv.grad_residual = inf_norm_diff(fit_.data() + mu_, values_.data() + mu_, 3 * sigma_);
     cv.exact = true;
-    cv.converged = cv.residual <= tol;
+    cv.converged = cv.residual <= tol && cv.grad_residual <= grad_tol;
     return cv;
   }
 
@@ -272,8 +301,8 @@ class ResidualEvaluator {
       p64_ = std::make_unique<Evaluator<double>>(model_, bbox_, INFINITY, INFINITY);
       p64_->force_direct(true);
       p64_->set_ff_direct(precision_ == PGPU_PRECISION_MIXED);
-      p64_->set_sources(pts_dev_, mu_, nullptr, 0);
-      p64_->set_targets(probe_pts_.data(), n_probe_, nullptr, 0);
+      p64_->set_sources(pts_dev_, mu_, grad_dev_, sigma_);
+      p64_->set_targets(probe_pts_.data(), n_probe_, probe_grad_pts_.data(), n_gprobe_);
     }
     return *p64_;
   }
@@ -288,29 +317,33 @@ class ResidualEvaluator {
   }
   Evaluator<double>& full() {
     if (!full_) {
-      full_ = std::make_unique<Evaluator<double>>(model_, bbox_, accuracy_, accuracy_);
+      full_ = std::make_unique<Evaluator<double>>(model_, bbox_, accuracy_, grad_accuracy_);
       full_->set_ff_direct(precision_ == PGPU_PRECISION_MIXED);
       if (order_ > 0) {
         FarFieldConfig c;
         c.order = order_;
         full_->set_far_field(c);
       }
-      full_->set_points(pts_dev_, mu_, nullptr, 0);
+      full_->set_points(pts_dev_, mu_, grad_dev_, sigma_);
     }
     return *full_;
   }
 
   const ModelDesc& model_;
   Index mu_;
+  Index sigma_;
   int l_;
   const double* pts_dev_;
+  const double* grad_dev_;
   Bbox3 bbox_;
   double accuracy_;
+  double grad_accuracy_;
   int precision_;
   int order_ = 0;
   Index n_probe_ = 0;
+  Index n_gprobe_ = 0;
   DevBuf<Index> probe_idx_;
-  DevBuf<double> probe_pts_, probe_values_, values_, fit_, tmp_;
+  DevBuf<double> probe_pts_, probe_grad_pts_, probe_values_, values_, fit_, tmp_;
   std::unique_ptr<Evaluator<double>> p64_;
   std::unique_ptr<Evaluator<float>> p32_;
   std::unique_ptr<Evaluator<double>> full_;
@@ -331,38 +364,43 @@ FitResult fit_impl(const FitRequest& req) {
   FitResult res;
   const ModelDesc& model = *req.model;
   const Index mu = req.mu;
+  const Index sigma = req.sigma;
+  const Index R = mu + 3 * sigma;  // rows: values, then three derivatives per gradient point
   const int l = model.l();
-  const Index M = mu + l;
+  const Index M = R + l;
   double t0 = wall_seconds();
 
-  DevBuf<double> pts;
+  DevBuf<double> pts, gpts;
   pts.upload(req.points_host, 3 * mu);
+  if (sigma > 0) gpts.upload(req.grad_points_host, 3 * sigma);
   if (req.verbose) {
     sync();
     std::printf("fit: upload %.3f s\n", wall_seconds() - t0);
   }
-  const Bbox3 bbox = Bbox3::from_host_points(req.points_host, mu);
+  Bbox3 bbox = Bbox3::from_host_points(req.points_host, mu);
+  if (sigma > 0) bbox = bbox.hull(Bbox3::from_host_points(req.grad_points_host, sigma));
   if (req.verbose) std::printf("fit: bbox %.3f s\n", wall_seconds() - t0);
 
   DevBuf<double> P, Q;
   if (l > 0) {
-    P.resize(mu * l);
-    monomial_basis(model.poly_degree, pts.data(), mu, nullptr, 0, P.data());
-    Q.resize(mu * l);
-    copy(Q.data(), P.data(), mu * l);
+    P.resize(R * l);
+    monomial_basis(model.poly_degree, pts.data(), mu, gpts.data(), sigma, P.data());
+    Q.resize(R * l);
+    copy(Q.data(), P.data(), R * l);
     // Modified Gram-Schmidt (common/orthonormalize.hpp:8-18).
     for (int i = 0; i < l; ++i) {
-      double* ci = Q.data() + static_cast<Index>(i) * mu;
-      scal(mu, 1.0 / norm2(ci, mu), ci);
+      double* ci = Q.data() + static_cast<Index>(i) * R;
+      scal(R, 1.0 / norm2(ci, R), ci);
       for (int j = i + 1; j < l; ++j) {
-        double* cj = Q.data() + static_cast<Index>(j) * mu;
-        axpy(mu, -dot(ci, cj, mu), ci, cj);
+        double* cj = Q.data() + static_cast<Index>(j) * R;
+        axpy(R, -dot(ci, cj, R), ci, cj);
       }
     }
   }
 
   if (req.verbose) std::printf("fit: basis %.3f s\n", wall_seconds() - t0);
-  RasPreconditioner<T> pc(model, req.points_host, pts.data(), mu, bbox);
+  RasPreconditioner<T> pc(model, req.points_host, pts.data(), mu, req.grad_points_host,
+                          gpts.data(), sigma, bbox);
   res.levels = pc.levels();
   res.n_domains = pc.n_domains();
   if (req.verbose) std::printf("fit: preconditioner ready %.3f s\n", wall_seconds() - t0);
@@ -372,22 +410,22 @@ FitResult fit_impl(const FitRequest& req) {
   bool x0_zero = true;
   if (req.initial_weights) {
     w.upload(req.initial_weights, M);
-    project_out(Q.data(), mu, l, w.data());
+    project_out(Q.data(), R, l, w.data());
     x0_zero = false;
   }
   rhs.zero();
-  PGPU_CUDA(cudaMemcpyAsync(rhs.data(), req.values_host, mu * sizeof(double),
+  PGPU_CUDA(cudaMemcpyAsync(rhs.data(), req.values_host, R * sizeof(double),
                             cudaMemcpyHostToDevice, stream()));
   sync();
 
   ResidualEvaluator re(model, pts.data(), req.points_host, mu, bbox, req.accuracy, req.values_host,
-                       req.precision);
+                       req.precision, gpts.data(), req.grad_points_host, sigma, req.grad_accuracy);
   res.setup_seconds = wall_seconds() - t0;
   double t1 = wall_seconds();
 
   if (req.precision == PGPU_PRECISION_PLAIN || req.plain_loop) {
     // Operator at accuracy 0 as interpolation/solver.hpp:40.
-    Operator<double> op(model, pts.data(), mu, bbox, 0.0, P.data());
+    Operator<double> op(model, pts.data(), mu, bbox, 0.0, P.data(), gpts.data(), sigma);
     // Mixed requests below the FP32 threshold: FP64-class float-float direct sums where they
     // exist (odd polyharmonic kernels).
     op.evaluator().set_ff_direct(req.precision == PGPU_PRECISION_MIXED);
@@ -409,15 +447,22 @@ FitResult fit_impl(const FitRequest& req) {
     int base = 0;
     while (true) {
       solver.solution(w.data());
-      Convergence cv = re.converged(w.data(), req.tolerance);
+      Convergence cv = re.converged(w.data(), req.tolerance, req.grad_tolerance);
       const int total = base + solver.iteration_count();
-      if (req.verbose) std::printf("%8d%4s%12.6e\n", total, cv.exact ? "" : "~", cv.residual);
+      if (req.verbose) {
+        if (sigma > 0)
+          std::printf("%8d%4s%12.6e%4s%12.6e\n", total, cv.exact ? "" : "~", cv.residual,
+                      cv.exact ? "" : "~", cv.grad_residual);
+        else
+          std::printf("%8d%4s%12.6e\n", total, cv.exact ? "" : "~", cv.residual);
+      }
       res.residual = cv.residual;
+      res.grad_residual = cv.grad_residual;
       if (sizeof(T) == 4 && !std::isfinite(solver.absolute_residual())) throw NonFinite();
       if (cv.converged) break;
       if (total >= req.max_iter)
         throw Error(PGPU_MAX_ITER, "reached the maximum number of iterations");
-      const double est_rms = solver.absolute_residual() / std::sqrt(static_cast<double>(mu));
+      const double est_rms = solver.absolute_residual() / std::sqrt(static_cast<double>(R));
       if (order < 8 && solver.iteration_count() > 0 && est_rms < 0.1 * cv.probe_rms) {
         order = 8;
         op.set_order(order);
@@ -641,13 +686,25 @@ void check_finite_host(const double* p, Index n, const char* what) {
 }  // namespace
 
 FitResult fit(const FitRequest& req) {
-  if (req.sigma > 0) throw Error(PGPU_NOT_IMPLEMENTED, "gradient data points are not supported yet");
   check_finite_host(req.points_host, 3 * req.mu, "points");
+  if (req.sigma > 0) {
+    check_finite_host(req.grad_points_host, 3 * req.sigma, "grad_points");
+    // The gradient-gradient blocks need the kernel's Hessian (mat_a.hpp:44-58).
+    for (const auto& rb : req.model->rbfs)
+      if (!kind_has_hessian(rb.kind))
+        throw_runtime(std::string(rb.kind == PGPU_RBF_CUB ? "cov_cubic" : "cov_spherical") +
+                      "::evaluate_hessian_isotropic is not implemented");
+  }
   check_finite_host(req.values_host, req.mu + 3 * req.sigma, "values");
   const double mu = static_cast<double>(req.mu);
   FitRequest plain = req;
   plain.precision = PGPU_PRECISION_PLAIN;
   if (req.precision == PGPU_PRECISION_PLAIN) return fit_impl<double>(plain);
+  if (req.sigma > 0) {
+    // Gradient data: the value/gradient/Hessian blocks run in FP64 (the reference's arithmetic)
+    // whatever the requested precision; the result says so.
+    return fit_impl<double>(plain);
+  }
   auto mixed = [](FitResult r) {
     r.precision_used = PGPU_PRECISION_MIXED;
     return r;

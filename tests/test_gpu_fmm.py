@@ -245,3 +245,33 @@ def test_fmm_gradient_sources(cls, params, kernel, precision):
     scale = np.abs(w).sum() / 3 * max(1.0, np.max(np.abs(want)) / (np.abs(w).sum() / 3))
     bound = 1e-4 if cls is pg.Biharmonic3D else 1e-3
     assert np.max(np.abs(got - want)) <= bound * scale, (np.max(np.abs(got - want)), scale)
+
+
+def test_operator_cache_is_bounded():
+    # Every bounding box gives the far field a new cell radius. The homogeneous kernels' operators
+    # are stored at radius 1 and serve every box; the others' are kept within the byte limit,
+    # least recently used first out, and results stay exact to the order's bound throughout.
+    before = pg.operator_cache_stats()
+    for s in (1.0, 0.37, 2.9, 11.0):
+        src, trg, w = sample(60000, 3000, 91)
+        err, scale = check(pg.Biharmonic3D([1.0]), 6, pg.MIXED, s * src, s * trg + 0.1, w,
+                           leaf_level=4)
+        assert err <= BOUND[6] * scale, (s, err, scale)
+        if s == 1.0:
+            first = pg.operator_cache_stats()
+    assert pg.operator_cache_stats()["entries"] == first["entries"]
+    assert first["entries"] - before["entries"] <= 3  # levels 2-4, once
+    limit = before["limit"]
+    try:
+        pg.set_operator_cache_limit(300 << 20)
+        assert pg.operator_cache_stats()["bytes"] <= 300 << 20
+        for s in (1.0, 0.8, 1.3, 0.6, 1.7):
+            src, trg, w = sample(60000, 3000, 92)
+            err, scale = check(pg.CovExponential([1.0, 0.3]), 6, pg.MIXED, s * src, s * trg, w,
+                               leaf_level=4)
+            assert err <= BOUND[6] * scale, (s, err, scale)
+            st = pg.operator_cache_stats()
+            assert st["bytes"] <= st["limit"] or st["entries"] == 1, st
+    finally:
+        pg.set_operator_cache_limit(limit)
+    assert pg.operator_cache_stats()["limit"] == limit
