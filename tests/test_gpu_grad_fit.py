@@ -124,3 +124,29 @@ def test_kernels_without_hessian_are_rejected():
     it = pg.Interpolant(pg.Model(pg.CovCubic([1.0, 0.5]), 0))
     with pytest.raises(pg.PolatoryError, match="cov_cubic::evaluate_hessian_isotropic is not implemented"):
         it.fit(pts, rhs, 1e-4, grad_points=gpts, grad_tolerance=1e-4)
+
+
+def test_fitter_through_the_fmm():
+    # 40,000 points and 40,000 gradient points (160,000 rows): the operator, the residual
+    # check and the preconditioner's residual updates run the FMM's value, gradient, gradient-
+    # transpose and Hessian blocks. The residual is recomputed by the oracle at 2,000 sampled
+    # points and 2,000 sampled gradient points.
+    g = np.random.Generator(np.random.PCG64(105))
+    aniso = random_anisotropy(g)
+    n = 40000
+    pts, gpts, rhs = sample(g, n, n, aniso)
+    model = th3_model(aniso)
+    tol = 1e-3
+    it = pg.Interpolant(model)
+    it.fit(pts, rhs, tol, accuracy=tol / 100, grad_points=gpts, grad_tolerance=tol,
+           grad_accuracy=tol / 100)
+    st = it.fit_stats
+    assert st["levels"] >= 3
+    w = it.weights
+    i = g.choice(n, 2000, replace=False)
+    j = g.choice(n, 2000, replace=False)
+    fit = oracle.direct_evaluate(model, pts, w, pts[i], gsrc=gpts, gtrg=gpts[j])
+    fit[:2000] += model.nugget * w[i]
+    want = np.concatenate([rhs[i], rhs[n:].reshape(-1, 3)[j].reshape(-1)])
+    assert np.max(np.abs(fit[:2000] - want[:2000])) < tol, st
+    assert np.max(np.abs(fit[2000:] - want[2000:])) < tol, st
