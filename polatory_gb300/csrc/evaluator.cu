@@ -280,18 +280,83 @@ __global__ void gather_p4_kernel(const P4<double>* __restrict__ src, const Index
 constexpr double kExactFallbackPairs = 4398046511104.0;
 
 template <class T>
-int Evaluator<T>::estimate_order(Term& t, double accuracy) {
-  const Index ns = std::min<Index>(mu_, 10000);
-  std::vector<Index> idx(mu_);
+int Evaluator<T>::estimate_order(Term& t, double acc_v, double acc_g) {
+  // Sample targets: up to 10,000 source points (the gradient points when there are none).
+  const bool from_grad = mu_ == 0;
+  const Index n_pos = from_grad ? sigma_ : mu_;
+  const Index ns = std::min<Index>(n_pos, 10000);
+  std::vector<Index> idx(n_pos);
   std::iota(idx.begin(), idx.end(), Index{0});
   std::shuffle(idx.begin(), idx.end(), std::mt19937{});
   idx.resize(ns);
   DevBuf<Index> di;
   di.upload(idx);
-  DevBuf<P4<double>> samp(ns);
-  gather_p4_kernel<<<blocks_for(ns, 256), 256, 0, stream()>>>(t.spos_d.data(), di.data(), ns,
-                                                              samp.data());
-  PGPU_LAUNCH_CHECK();
+  DevBuf<P4<double>> samp(std::max<Index>(ns, 1));
+  if (ns > 0) {
+    gather_p4_kernel<<<blocks_for(ns, 256), 256, 0, stream()>>>(
+        from_grad ? t.sgpos_d.data() : t.spos_d.data(), di.data(), ns, samp.data());
+    PGPU_LAUNCH_CHECK();
+  }
+  double rel_min[3];
+  for (int k = 0; k < 3; ++k) rel_min[k] = t.box_min[k] - t.origin[k];
+  if (sigma_ > 0 || mg_ > 0) {
+    // Gradient sources or targets: the four blocks (value/gradient sources x value/gradient
+    // targets) at the sample positions, value outputs against acc_v and gradient outputs
+    // against acc_g (the reference's gradient evaluators estimate their own configuration).
+    const bool want_v = m_ > 0, want_g = mg_ > 0;
+    DevBuf<double> vw64(std::max<Index>(mu_, 1)), gg64(std::max<Index>(3 * sigma_, 1));
+    if (mu_ + sigma_ > 0) {
+      prep_weights_kernel<double><<<blocks_for(mu_ + sigma_, 256), 256, 0, stream()>>>(
+          w_, mu_, sigma_, t.a, vw64.data(), gg64.data());
+      PGPU_LAUNCH_CHECK();
+    }
+    DevBuf<double> ev(std::max<Index>(ns, 1)), eg(std::max<Index>(3 * ns, 1));
+    DevBuf<double> av(std::max<Index>(ns, 1)), ag(std::max<Index>(3 * ns, 1));
+    DevBuf<double> g3(std::max<Index>(3 * ns, 1));
+    ev.zero();
+    eg.zero();
+    {
+      DirectSources<double> src{t.spos_d.data(), vw64.data(), mu_, t.sgpos_d.data(), gg64.data(),
+                                sigma_};
+      DirectTargets<double> trg{want_v ? samp.data() : nullptr, want_v ? ns : 0, ev.data(),
+                                want_g ? samp.data() : nullptr, want_g ? ns : 0, eg.data()};
+      direct_evaluate<double>(t.rbf.kind, t.kp64, t.a, src, trg, stream());
+    }
+    for (int p : {4, 6, 8}) {
+      av.zero();
+      ag.zero();
+      for (int gsrc = 0; gsrc < 2; ++gsrc)
+        for (int gtrg = 0; gtrg < 2; ++gtrg) {
+          const Index ns_b = gsrc ? sigma_ : mu_;
+          if (ns_b == 0 || ns == 0 || !(gtrg ? want_g : want_v)) continue;
+          Fmm<T> f(t.rbf.kind, t.kp, t.a, rel_min, t.box_width, std::min(acc_v, acc_g));
+          FarFieldConfig c;
+          c.order = p;
+          f.set_config(c);
+          f.set_gradient_sources(gsrc != 0);
+          f.set_gradient_targets(gtrg != 0);
+          f.set_sources(gsrc ? t.sgpos_d.data() : t.spos_d.data(), ns_b);
+          f.set_targets(samp.data(), ns);
+          if (gtrg) {
+            g3.zero();
+            f.evaluate(t.vw.data(), t.gg.data(), w_, g3.data(), nullptr);
+            frame_gradient_add(t.a, g3.data(), ns, ag.data());
+          } else {
+            f.evaluate(t.vw.data(), t.gg.data(), w_, av.data(), nullptr);
+          }
+        }
+      const double err_v = want_v ? inf_norm_diff(av.data(), ev.data(), ns) : 0.0;
+      const double err_g = want_g ? inf_norm_diff(ag.data(), eg.data(), 3 * ns) : 0.0;
+      if (verbose())
+        std::printf("fmm accuracy estimate: order %d error %.3e / gradient %.3e (targets %.3e / %.3e)\n",
+                    p, err_v, err_g, acc_v, acc_g);
+      if (err_v <= acc_v && err_g <= acc_g) return p;
+    }
+    const double pairs = static_cast<double>(mu_ + sigma_) * static_cast<double>(m_ + mg_);
+    if (pairs <= kExactFallbackPairs) return -1;
+    throw Error(PGPU_RUNTIME_ERROR, "failed to construct an evaluator that meets the desired accuracy");
+  }
+  const double accuracy = acc_v;
   DevBuf<double> exact(ns), approx(ns);
   exact.zero();
   {
@@ -299,8 +364,6 @@ int Evaluator<T>::estimate_order(Term& t, double accuracy) {
     DirectTargets<double> trg{samp.data(), ns, exact.data(), nullptr, 0, nullptr};
     direct_evaluate<double>(t.rbf.kind, t.kp64, t.a, src, trg, stream());
   }
-  double rel_min[3];
-  for (int k = 0; k < 3; ++k) rel_min[k] = t.box_min[k] - t.origin[k];
   // Split kernels: the compact direct part is exact (near-field sums); its values at the
   // samples are added to the fast part's FMM at each order.
   DevBuf<double> near_part(ns);
@@ -472,7 +535,9 @@ void Evaluator<T>::evaluate(double* out, bool with_poly) {
     const double term_acc = acc / static_cast<double>(terms_.size());
     const bool order_free = !ff_set_ || ff_.order == 0;
     if (use_fmm && has_far && order_free && std::isfinite(acc) && acc > 0.0 && t.order == 0) {
-      t.order = estimate_order(t, term_acc);
+      const double nt = static_cast<double>(terms_.size());
+      t.order = blocks_fmm ? estimate_order(t, accuracy_ / nt, grad_accuracy_ / nt)
+                           : estimate_order(t, term_acc, term_acc);
       t.fmm.reset();
     }
     const bool exact = use_fmm && order_free && t.order < 0;

@@ -107,7 +107,9 @@ class Evaluator {
 
  private:
   struct Term;
-  int estimate_order(Term& t, double accuracy);
+  // acc_v bounds the value outputs' error, acc_g the gradient outputs' (used when the
+  // evaluator has gradient sources or targets).
+  int estimate_order(Term& t, double acc_v, double acc_g);
 
   ModelDesc model_;
   Bbox3 bbox_;

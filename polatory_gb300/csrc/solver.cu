@@ -275,8 +275,9 @@ class ResidualEvaluator {
       cv.residual = inf_norm_diff(fit_.data(), probe_values_.data(), n_probe_);
       cv.grad_residual = inf_norm_diff(fit_.data() + n_probe_, probe_values_.data() + n_probe_,
                                        3 * n_gprobe_);
-      axpby(n_probe_, 1.0, probe_values_.data(), -1.0, fit_.data());
-      cv.probe_rms = norm2(fit_.data(), n_probe_) / std::sqrt(static_cast<double>(std::max<Index>(n_probe_, 1)));
+      const Index np_all = n_probe_ + 3 * n_gprobe_;
+      axpby(np_all, 1.0, probe_values_.data(), -1.0, fit_.data());
+      cv.probe_rms = norm2(fit_.data(), np_all) / std::sqrt(static_cast<double>(std::max<Index>(np_all, 1)));
       cv.exact = n_probe_ == mu_ && n_gprobe_ == sigma_;
       if (cv.residual > tol || cv.grad_residual > grad_tol) return cv;
       if (cv.exact) {
@@ -442,8 +443,13 @@ FitResult fit_impl(const FitRequest& req) {
     // fails, the operator's far-field error is what remains: the order of the operator (and of
     // the full residual check, unless an accuracy was given) is raised to 8 once, FGMRES
     // restarting from the current weights.
-    int order = 6;
+    // Gradient data starts at order 8: the derivative blocks lose accuracy against the values at
+    // the same order. After order 8 the last rung is exact sums (up to 2^42 pairs), where the
+    // reference interpolates at order 12.
+    int order = sigma > 0 ? 8 : 6;
     op.set_order(order);
+    if (order == 8) re.set_default_order(8);
+    const bool exact_ok = static_cast<double>(R) * static_cast<double>(R) <= 4398046511104.0;
     int base = 0;
     while (true) {
       solver.solution(w.data());
@@ -463,11 +469,18 @@ FitResult fit_impl(const FitRequest& req) {
       if (total >= req.max_iter)
         throw Error(PGPU_MAX_ITER, "reached the maximum number of iterations");
       const double est_rms = solver.absolute_residual() / std::sqrt(static_cast<double>(R));
-      if (order < 8 && solver.iteration_count() > 0 && est_rms < 0.1 * cv.probe_rms) {
-        order = 8;
-        op.set_order(order);
-        re.set_default_order(order);
-        if (req.verbose) std::printf("%8d    operator order %d\n", total, order);
+      if ((order < 8 || (order == 8 && exact_ok)) && solver.iteration_count() > 0 &&
+          est_rms < 0.1 * cv.probe_rms) {
+        if (order < 8) {
+          order = 8;
+          op.set_order(order);
+          re.set_default_order(order);
+          if (req.verbose) std::printf("%8d    operator order %d\n", total, order);
+        } else {
+          order = 9;  // exact sums
+          op.evaluator().force_direct(true);
+          if (req.verbose) std::printf("%8d    operator: exact sums\n", total);
+        }
         base = total;
         solver.setup(rhs.data(), w.data(), false, op);
         continue;
