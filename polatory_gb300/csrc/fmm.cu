@@ -909,114 +909,6 @@ __global__ void chunk_fill_kernel(const int* __restrict__ cnt, const int* __rest
     chunk_leaf[2 * (off[l] + c) + 1] = c;
   }
 }
-// Packed FP32 pairs (Blackwell's two-lane f32x2 arithmetic on 64-bit registers): the sums of
-// two targets advance in one instruction per step. The results equal the scalar path's bit for bit
-// (every lane is the same IEEE operation).
-__device__ __forceinline__ unsigned long long pk2(float a, float b) {
-  return static_cast<unsigned long long>(__float_as_uint(a)) |
-         (static_cast<unsigned long long>(__float_as_uint(b)) << 32);
-}
-__device__ __forceinline__ float lo2(unsigned long long v) { return __uint_as_float(static_cast<unsigned>(v)); }
-__device__ __forceinline__ float hi2(unsigned long long v) { return __uint_as_float(static_cast<unsigned>(v >> 32)); }
-__device__ __forceinline__ unsigned long long sub_f32x2(unsigned long long a, unsigned long long b) {
-  unsigned long long d;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ unsigned long long mul_f32x2(unsigned long long a, unsigned long long b) {
-  unsigned long long d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ unsigned long long fma_f32x2(unsigned long long a, unsigned long long b,
-                                                        unsigned long long c) {
-  unsigned long long d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
-
-__device__ __forceinline__ unsigned long long add_f32x2(unsigned long long a, unsigned long long b) {
-  unsigned long long d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-
-// ff_poly_accumulate for two targets at once (lanes: the targets; the source values duplicated
-// in both lanes). Each lane performs the scalar version's operations on the same values, with
-// negated terms carried instead of negated operands (fma(-a, b, c) = -fma(a, b, -c) and
-// x + (-y) = x - y hold exactly in round-to-nearest), so the sums equal the scalar ones bit for
-// bit. nwh: -wh.
-template <int KIND>
-__device__ __forceinline__ void ff_poly_accumulate_x2(
-    unsigned long long txh, unsigned long long txl, unsigned long long tyh, unsigned long long tyl,
-    unsigned long long tzh, unsigned long long tzl, unsigned long long sxh, unsigned long long sxl,
-    unsigned long long syh, unsigned long long syl, unsigned long long szh, unsigned long long szl,
-    unsigned long long wh, unsigned long long wl, bool reg, unsigned long long c_hi,
-    unsigned long long c_lo, unsigned long long& ah, unsigned long long& al) {
-  using u64 = unsigned long long;
-  const u64 kTwo = pk2(2.0f, 2.0f), kNegOne = pk2(-1.0f, -1.0f), kHalf = pk2(0.5f, 0.5f);
-  // One axis: d = t - s as (h, e) by TwoSum, then h^2 and the negated error term of
-  // 2 h e + TwoProd(h, h).
-  auto axis = [&](u64 th, u64 tl, u64 sh, u64 sl, u64& h, u64& p, u64& npe) {
-    h = sub_f32x2(th, sh);
-    const u64 nh = sub_f32x2(sh, th);
-    const u64 v = sub_f32x2(h, th);
-    u64 e = sub_f32x2(sub_f32x2(th, sub_f32x2(h, v)), add_f32x2(sh, v));
-    e = add_f32x2(e, sub_f32x2(tl, sl));
-    p = mul_f32x2(h, h);
-    const u64 q = fma_f32x2(nh, h, p);
-    npe = fma_f32x2(mul_f32x2(kTwo, nh), e, q);
-  };
-  u64 dxh, px, npxe, dyh, py, npye, dzh, pz, npze;
-  axis(txh, txl, sxh, sxl, dxh, px, npxe);
-  axis(tyh, tyl, syh, syl, dyh, py, npye);
-  axis(tzh, tzl, szh, szl, dzh, pz, npze);
-  auto two_sum = [&](u64 a, u64 b, u64& s, u64& e) {
-    s = add_f32x2(a, b);
-    const u64 v = sub_f32x2(s, a);
-    e = add_f32x2(sub_f32x2(a, sub_f32x2(s, v)), sub_f32x2(b, v));
-  };
-  u64 a, ea, r2h, eb;
-  two_sum(px, py, a, ea);
-  two_sum(a, pz, r2h, eb);
-  u64 r2l = sub_f32x2(sub_f32x2(sub_f32x2(add_f32x2(ea, eb), npxe), npye), npze);
-  if (reg) {
-    u64 sh, se2;
-    two_sum(r2h, c_hi, sh, se2);
-    r2h = sh;
-    r2l = add_f32x2(r2l, add_f32x2(se2, c_lo));
-  }
-  {
-    const u64 nh = add_f32x2(r2h, r2l);
-    r2l = sub_f32x2(r2l, sub_f32x2(nh, r2h));
-    r2h = nh;
-  }
-  const u64 rinv = pk2(rsqrtf(fmaxf(lo2(r2h), 1e-30f)), rsqrtf(fmaxf(hi2(r2h), 1e-30f)));
-  const u64 rh = mul_f32x2(r2h, rinv);
-  const u64 nrh = mul_f32x2(r2h, mul_f32x2(kNegOne, rinv));
-  const u64 rl = mul_f32x2(add_f32x2(fma_f32x2(nrh, rh, r2h), r2l), mul_f32x2(kHalf, rinv));
-  u64 ph, pl;
-  if constexpr (KIND == PGPU_RBF_BH3) {
-    ph = rh;
-    pl = rl;
-  } else {
-    ph = mul_f32x2(rh, r2h);
-    const u64 nph = mul_f32x2(kNegOne, ph);
-    pl = add_f32x2(fma_f32x2(rh, r2h, nph), fma_f32x2(rh, r2l, mul_f32x2(rl, r2h)));
-  }
-  const u64 th = mul_f32x2(wh, ph);
-  const u64 g = fma_f32x2(mul_f32x2(kNegOne, wh), ph, th);  // -fma(wh, ph, -th)
-  const u64 tl = sub_f32x2(fma_f32x2(wh, pl, mul_f32x2(wl, ph)), g);
-  u64 sh, e2;
-  two_sum(ah, th, sh, e2);
-  al = add_f32x2(al, add_f32x2(e2, tl));
-  ah = sh;
-}
-
-// The odd polyharmonic FP32 pair terms run packed (pair_term's arithmetic, two targets at once).
-template <int KIND, class T>
-constexpr bool kPackedPairs = sizeof(T) == 4 && (KIND == PGPU_RBF_BH3 || KIND == PGPU_RBF_TH3);
-
 template <int KIND, class T>
 __global__ void __launch_bounds__(128, 12)
     p2p_kernel(KParams<T> kp, const P4<T>* __restrict__ tpos, const Index* __restrict__ tperm,
@@ -1029,10 +921,7 @@ __global__ void __launch_bounds__(128, 12)
   // d = (t - (dx, dy, dz) wleaf) - s involves only leaf-sized numbers.
   // One block per chunk of at most kP2PChunk targets of one leaf (chunk_leaf: per chunk the
   // leaf and the chunk's index within it), so leaves crowded with targets spread over blocks.
-  constexpr bool kPk = kPackedPairs<KIND, T>;
-  __shared__ P4<T> s_p[kPk ? 1 : 128];
-  // Packed staging: per source {x, x, y, y} and {z, z, w, w} (each lane of a pair gets a copy).
-  __shared__ ulonglong2 s_pk[kPk ? 256 : 1];
+  __shared__ P4<T> s_p[128];
   __shared__ int s_nb[27];
   const int leaf = chunk_leaf[2 * blockIdx.x];
   if (threadIdx.x < 27) s_nb[threadIdx.x] = table[static_cast<Index>(leaf) * 27 + threadIdx.x];
@@ -1080,55 +969,22 @@ __global__ void __launch_bounds__(128, 12)
         if (threadIdx.x < cnt) {
           P4<T> p = spos[base + threadIdx.x];
           p.w = sw[base + threadIdx.x] * wscale;
-          if constexpr (kPk) {
-            s_pk[2 * threadIdx.x] = make_ulonglong2(pk2(p.x, p.x), pk2(p.y, p.y));
-            s_pk[2 * threadIdx.x + 1] = make_ulonglong2(pk2(p.z, p.z), pk2(p.w, p.w));
-          } else {
-            s_p[threadIdx.x] = p;
-          }
+          s_p[threadIdx.x] = p;
         }
         __syncthreads();
         if (!warp_busy) continue;
-        if constexpr (kPk && NT == 2) {
-          const unsigned long long TX = pk2(tx[0], tx[1]), TY = pk2(ty[0], ty[1]),
-                                   TZ = pk2(tz[0], tz[1]), C2 = pk2(c2, c2);
-          unsigned long long acc = 0;  // two +0.0f
+        T acc[NT];
+#pragma unroll
+        for (int q = 0; q < NT; ++q) acc[q] = T(0);
 #pragma unroll 4
-          for (int j = 0; j < cnt; ++j) {
-            const ulonglong2 a = s_pk[2 * j], b = s_pk[2 * j + 1];
-            const unsigned long long dx = sub_f32x2(TX, a.x), dy = sub_f32x2(TY, a.y),
-                                     dz = sub_f32x2(TZ, b.x);
-            const unsigned long long rho2 =
-                fma_f32x2(dx, dx, fma_f32x2(dy, dy, fma_f32x2(dz, dz, C2)));
-            const unsigned long long rho =
-                mul_f32x2(rho2, pk2(rsqrtf(lo2(rho2)), rsqrtf(hi2(rho2))));
-            if constexpr (KIND == PGPU_RBF_BH3)
-              acc = fma_f32x2(b.y, rho, acc);
-            else
-              acc = fma_f32x2(b.y, mul_f32x2(rho2, rho), acc);
-          }
-          tot[0] += static_cast<double>(lo2(acc));
-          tot[NT - 1] += static_cast<double>(hi2(acc));
-        } else {
-          T acc[NT];
+        for (int j = 0; j < cnt; ++j) {
+          const P4<T> s4 = s_p[j];
 #pragma unroll
-          for (int q = 0; q < NT; ++q) acc[q] = T(0);
-#pragma unroll 4
-          for (int j = 0; j < cnt; ++j) {
-            P4<T> s4;
-            if constexpr (kPk) {
-              const ulonglong2 a = s_pk[2 * j], b = s_pk[2 * j + 1];
-              s4 = P4<T>{lo2(a.x), lo2(a.y), lo2(b.x), lo2(b.y)};
-            } else {
-              s4 = s_p[j];
-            }
-#pragma unroll
-            for (int q = 0; q < NT; ++q)
-              acc[q] = pair_term<KIND>(tx[q] - s4.x, ty[q] - s4.y, tz[q] - s4.z, s4.w, c2, kp, acc[q]);
-          }
-#pragma unroll
-          for (int q = 0; q < NT; ++q) tot[q] += static_cast<double>(acc[q]);
+          for (int q = 0; q < NT; ++q)
+            acc[q] = pair_term<KIND>(tx[q] - s4.x, ty[q] - s4.y, tz[q] - s4.z, s4.w, c2, kp, acc[q]);
         }
+#pragma unroll
+        for (int q = 0; q < NT; ++q) tot[q] += static_cast<double>(acc[q]);
       }
     }
 #pragma unroll
@@ -1158,9 +1014,8 @@ __global__ void __launch_bounds__(128)
                   const int* __restrict__ table, const P4<double>* __restrict__ spos,
                   const double* __restrict__ sw, const Index* __restrict__ sleaf_start,
                   double wleaf, double* __restrict__ out) {
-  // Sources as (x hi, x lo), (y hi, y lo), (z hi, z lo), (w hi, w lo), each value in both lanes
-  // of a packed pair: four 16-byte loads serve two targets.
-  __shared__ ulonglong2 s_q[4 * 128];
+  // Sources as (x hi, x lo, y hi, y lo) and (z hi, z lo, w hi, w lo): two 16-byte loads a pair.
+  __shared__ float4 s_a[128], s_b[128];
   __shared__ int s_nb[27];
   const Index leaf = blockIdx.x;
   if (threadIdx.x < 27) s_nb[threadIdx.x] = table[leaf * 27 + threadIdx.x];
@@ -1203,47 +1058,29 @@ __global__ void __launch_bounds__(128)
         __syncthreads();
         if (threadIdx.x < cnt) {
           const P4<double> p = spos[base + threadIdx.x];
-          float v[8];
-          ff_split(p.x, v[0], v[1]);
-          ff_split(p.y, v[2], v[3]);
-          ff_split(p.z, v[4], v[5]);
-          ff_split(sw[base + threadIdx.x], v[6], v[7]);
-#pragma unroll
-          for (int k = 0; k < 4; ++k)
-            s_q[4 * threadIdx.x + k] = make_ulonglong2(pk2(v[2 * k], v[2 * k]), pk2(v[2 * k + 1], v[2 * k + 1]));
+          float4 a, b;
+          ff_split(p.x, a.x, a.y);
+          ff_split(p.y, a.z, a.w);
+          ff_split(p.z, b.x, b.y);
+          ff_split(sw[base + threadIdx.x], b.z, b.w);
+          s_a[threadIdx.x] = a;
+          s_b[threadIdx.x] = b;
         }
         __syncthreads();
         if (!warp_busy) continue;
-        if constexpr (NT == 2) {
-          const unsigned long long TXH = pk2(txh[0], txh[1]), TXL = pk2(txl[0], txl[1]),
-                                   TYH = pk2(tyh[0], tyh[1]), TYL = pk2(tyl[0], tyl[1]),
-                                   TZH = pk2(tzh[0], tzh[1]), TZL = pk2(tzl[0], tzl[1]),
-                                   CH = pk2(c_hi, c_hi), CL = pk2(c_lo, c_lo);
-          unsigned long long ah = 0, al = 0;
+        float ah[NT], al[NT];
+#pragma unroll
+        for (int q = 0; q < NT; ++q) ah[q] = al[q] = 0.0f;
 #pragma unroll 2
-          for (int j = 0; j < cnt; ++j) {
-            const ulonglong2 x = s_q[4 * j], y = s_q[4 * j + 1], z = s_q[4 * j + 2], w = s_q[4 * j + 3];
-            ff_poly_accumulate_x2<KIND>(TXH, TXL, TYH, TYL, TZH, TZL, x.x, x.y, y.x, y.y, z.x, z.y,
-                                        w.x, w.y, reg, CH, CL, ah, al);
-          }
-          tot[0] += static_cast<double>(lo2(ah)) + static_cast<double>(lo2(al));
-          tot[NT - 1] += static_cast<double>(hi2(ah)) + static_cast<double>(hi2(al));
-        } else {
-          float ah[NT], al[NT];
+        for (int j = 0; j < cnt; ++j) {
+          const float4 a = s_a[j], b = s_b[j];
 #pragma unroll
-          for (int q = 0; q < NT; ++q) ah[q] = al[q] = 0.0f;
-#pragma unroll 2
-          for (int j = 0; j < cnt; ++j) {
-            const ulonglong2 x = s_q[4 * j], y = s_q[4 * j + 1], z = s_q[4 * j + 2], w = s_q[4 * j + 3];
-#pragma unroll
-            for (int q = 0; q < NT; ++q)
-              ff_poly_accumulate<KIND>(txh[q], txl[q], tyh[q], tyl[q], tzh[q], tzl[q], lo2(x.x),
-                                       lo2(x.y), lo2(y.x), lo2(y.y), lo2(z.x), lo2(z.y), lo2(w.x),
-                                       lo2(w.y), reg, c_hi, c_lo, ah[q], al[q]);
-          }
-#pragma unroll
-          for (int q = 0; q < NT; ++q) tot[q] += static_cast<double>(ah[q]) + static_cast<double>(al[q]);
+          for (int q = 0; q < NT; ++q)
+            ff_poly_accumulate<KIND>(txh[q], txl[q], tyh[q], tyl[q], tzh[q], tzl[q], a.x, a.y, a.z,
+                                     a.w, b.x, b.y, b.z, b.w, reg, c_hi, c_lo, ah[q], al[q]);
         }
+#pragma unroll
+        for (int q = 0; q < NT; ++q) tot[q] += static_cast<double>(ah[q]) + static_cast<double>(al[q]);
       }
     }
     const double scale = KIND == PGPU_RBF_BH3 ? -kp.p0 : kp.p0;
