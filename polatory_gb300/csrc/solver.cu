@@ -580,6 +580,10 @@ FitResult fit_impl(const FitRequest& req) {
     // Ratio of the inf-norm to the root mean square of the last recomputed residual. The next
     // check waits until the estimate times this ratio predicts at most twice the tolerance.
     double peak_ratio = 1.0;
+    // A refinement cycle is checked only once its estimate has fallen ten times below the
+    // residual it started from: a check costs a residual at the current grade (an FP64-class
+    // near field and possibly an FP64 far field), an inner iteration an FP32 operator.
+    double check_below = INFINITY;
     while (true) {
       const double est_rms = solver.absolute_residual() / std::sqrt(static_cast<double>(mu));
       total = base + solver.iteration_count();
@@ -591,7 +595,8 @@ FitResult fit_impl(const FitRequest& req) {
         if (req.verbose) std::printf("%8d    %12.6e\n", total, res.residual);
         if (res.residual <= req.tolerance) break;
       } else if (!fresh && std::isfinite(est_rms) &&
-                 (est_rms > req.tolerance || est_rms * peak_ratio > 2.0 * req.tolerance)) {
+                 (est_rms > req.tolerance || est_rms * peak_ratio > 2.0 * req.tolerance ||
+                  est_rms > check_below)) {
         if (req.verbose) std::printf("%8d   ~%12.6e (estimate)\n", total, est_rms);
       } else {
         current();
@@ -661,6 +666,7 @@ FitResult fit_impl(const FitRequest& req) {
           base = total;
           copy(wb.data(), w.data(), M);
           solver.setup(r.data(), nullptr, true, inner);
+          check_below = 0.1 * solver.absolute_residual() / std::sqrt(static_cast<double>(mu));
         } else if (!std::isfinite(cycle_start_residual)) {
           cycle_start_residual = rinf;
         }
