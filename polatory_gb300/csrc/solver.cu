@@ -580,9 +580,9 @@ FitResult fit_impl(const FitRequest& req) {
     // Ratio of the inf-norm to the root mean square of the last recomputed residual. The next
     // check waits until the estimate times this ratio predicts at most twice the tolerance.
     double peak_ratio = 1.0;
-    // A refinement cycle is checked only once its estimate has fallen ten times below the
-    // residual it started from: a check costs a residual at the current grade (an FP64-class
-    // near field and possibly an FP64 far field), an inner iteration an FP32 operator.
+    // Once residuals need an order-8 or FP64 far field (a check then costs several inner
+    // iterations), a refinement cycle is checked only after its estimate has fallen ten times
+    // below the residual it started from, and again only after a further fourfold drop.
     double check_below = INFINITY;
     while (true) {
       const double est_rms = solver.absolute_residual() / std::sqrt(static_cast<double>(mu));
@@ -666,9 +666,13 @@ FitResult fit_impl(const FitRequest& req) {
           base = total;
           copy(wb.data(), w.data(), M);
           solver.setup(r.data(), nullptr, true, inner);
-          check_below = 0.1 * solver.absolute_residual() / std::sqrt(static_cast<double>(mu));
-        } else if (!std::isfinite(cycle_start_residual)) {
-          cycle_start_residual = rinf;
+          check_below = residual_grade >= kHybrid8
+                            ? 0.1 * solver.absolute_residual() / std::sqrt(static_cast<double>(mu))
+                            : INFINITY;
+        } else {
+          if (!std::isfinite(cycle_start_residual)) cycle_start_residual = rinf;
+          // The same cycle goes on: its next check waits for a fourfold drop of the estimate.
+          check_below = residual_grade >= kHybrid8 ? 0.25 * est_rms : INFINITY;
         }
       }
       if (total >= req.max_iter)
