@@ -346,28 +346,39 @@ template <class T>
 __global__ void potrf_diag_kernel(int kb, const int* __restrict__ lds,
                                   const Index* __restrict__ mat_off, T* __restrict__ mats,
                                   int* __restrict__ info) {
+  // 128 threads: lane = row of the 32 x 32 diagonal block, warp w updates the columns c = w
+  // (mod 4), so the four sub-partitions share the trailing updates of each step (a single warp
+  // would run them all through one sub-partition's FP64 pipe).
   const Index d = blockIdx.x;
   const int ld = lds[d];
   if (kb * NB >= ld) return;
+  constexpr int kWarps = 4;
   __shared__ T a[NB][NB + 1];
+  __shared__ T rpiv, floor_sh;
   T* m = mats + mat_off[d] + static_cast<Index>(kb * NB) * ld + kb * NB;
-  const int lane = threadIdx.x;
-  for (int c = 0; c < NB; ++c) a[lane][c] = m[lane + static_cast<Index>(c) * ld];
-  __syncwarp();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int c = w; c < NB; c += kWarps) a[lane][c] = m[lane + static_cast<Index>(c) * ld];
+  __syncthreads();
   int modified = 0;
   // FP32 factors: pivots below 2^-20 of the block's largest diagonal entry are raised to it, so
   // that an ill-conditioned domain matrix gives a bounded (approximate) factor instead of one
   // that overflows.
-  T floor_d = T(0);
-  if constexpr (sizeof(T) == 4) {
-    if (lane == 0) {
+  if (threadIdx.x == 0) {
+    T floor_d = T(0);
+    if constexpr (sizeof(T) == 4) {
       T dmax = T(0);
       for (int j = 0; j < NB; ++j) dmax = fmax(dmax, fabs(a[j][j]));
       floor_d = dmax * T(9.5367431640625e-07);
     }
+    floor_sh = floor_d;
   }
+  __syncthreads();
+  const T floor_d = floor_sh;
+  // The column below each pivot is scaled by the pivot's reciprocal, formed once: a division
+  // per lane and column would cost a multi-instruction sequence each, and FP64 instructions
+  // issue at 1/64 of the FP32 rate on this part.
   for (int j = 0; j < NB; ++j) {
-    if (lane == 0) {
+    if (threadIdx.x == 0) {
       T dj = a[j][j];
       if (!(dj > floor_d)) {
         // Modified pivot (the matrix lost definiteness to rounding): the preconditioner only
@@ -377,21 +388,24 @@ __global__ void potrf_diag_kernel(int kb, const int* __restrict__ lds,
         if (dj < floor_d) dj = floor_d;
         ++modified;
       }
-      a[j][j] = sqrt(dj);
+      const T sj = sqrt(dj);
+      a[j][j] = sj;
+      rpiv = T(1) / sj;
     }
-    __syncwarp();
-    if (lane > j) a[lane][j] /= a[j][j];
-    __syncwarp();
+    __syncthreads();
+    if (w == 0 && lane > j) a[lane][j] *= rpiv;
+    __syncthreads();
     if (lane > j) {
       const T lj = a[lane][j];
-      for (int c = j + 1; c <= lane; ++c) a[lane][c] -= lj * a[c][j];
+      for (int c = j + 1 + ((w - j - 1) % kWarps + kWarps) % kWarps; c <= lane; c += kWarps)
+        a[lane][c] -= lj * a[c][j];
     }
-    __syncwarp();
+    __syncthreads();
   }
-  for (int c = 0; c < NB; ++c) {
+  for (int c = w; c < NB; c += kWarps) {
     m[lane + static_cast<Index>(c) * ld] = (lane >= c) ? a[lane][c] : T(0);
   }
-  if (lane == 0 && modified) atomicAdd(info + d, modified);
+  if (threadIdx.x == 0 && modified) atomicAdd(info + d, modified);
 }
 
 template <class T>
@@ -401,12 +415,15 @@ __global__ void trsm_panel_kernel(int kb, const int* __restrict__ lds,
   const int ld = lds[d];
   const int r = (kb + 1) * NB + blockIdx.y * blockDim.x + threadIdx.x;
   __shared__ T lkk[NB][NB + 1];
+  __shared__ T rdiag[NB];  // reciprocals of the diagonal block's pivots
   if ((kb + 1) * NB + static_cast<int>(blockIdx.y * blockDim.x) >= ld) return;
   T* m = mats + mat_off[d];
   for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
     int rr = e % NB, cc = e / NB;
     lkk[rr][cc] = m[(kb * NB + rr) + static_cast<Index>(kb * NB + cc) * ld];
   }
+  __syncthreads();
+  if (threadIdx.x < NB) rdiag[threadIdx.x] = T(1) / lkk[threadIdx.x][threadIdx.x];
   __syncthreads();
   if (r >= ld) return;
   T x[NB];
@@ -417,7 +434,7 @@ __global__ void trsm_panel_kernel(int kb, const int* __restrict__ lds,
     T s = x[c];
 #pragma unroll
     for (int k = 0; k < c; ++k) s -= x[k] * lkk[c][k];
-    x[c] = s / lkk[c][c];
+    x[c] = s * rdiag[c];
   }
 #pragma unroll
   for (int c = 0; c < NB; ++c) m[r + static_cast<Index>(kb * NB + c) * ld] = x[c];
@@ -1968,7 +1985,7 @@ void RasPreconditioner<T>::build_batch(DomainBatch<U>& b, const std::vector<Inde
         }
         PGPU_LAUNCH_CHECK();
       }
-      potrf_diag_kernel<U><<<nd, 32, 0, stream()>>>(kb, b.ld.data(), b.mat_off.data(),
+      potrf_diag_kernel<U><<<nd, 128, 0, stream()>>>(kb, b.ld.data(), b.mat_off.data(),
                                                     b.mats.data(), b.info.data());
       PGPU_LAUNCH_CHECK();
       const int rows_below = b.max_n - (kb + 1) * NB;
