@@ -1301,39 +1301,6 @@ bool syrk_tc_enabled() {
   return on;
 }
 
-// A second stream for independent work inside one call: enter() makes it the thread's library
-// stream (after the work already queued on the first), leave() switches back, join() makes the
-// first stream wait for it. The destructor restores the first stream and waits for the second,
-// also when an exception unwinds.
-struct SideStream {
-  cudaStream_t main = nullptr, side = nullptr;
-  cudaEvent_t ready = nullptr, done = nullptr;
-  SideStream() : main(stream()) {
-    PGPU_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
-    PGPU_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
-    PGPU_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
-  }
-  void enter() {
-    PGPU_CUDA(cudaEventRecord(ready, main));
-    PGPU_CUDA(cudaStreamWaitEvent(side, ready, 0));
-    set_stream(side);
-  }
-  void leave() {
-    PGPU_CUDA(cudaEventRecord(done, side));
-    set_stream(main);
-  }
-  void join() { PGPU_CUDA(cudaStreamWaitEvent(main, done, 0)); }
-  ~SideStream() {
-    set_stream(main);
-    if (side) cudaStreamSynchronize(side);
-    if (ready) cudaEventDestroy(ready);
-    if (done) cudaEventDestroy(done);
-    if (side) cudaStreamDestroy(side);
-  }
-  SideStream(const SideStream&) = delete;
-  SideStream& operator=(const SideStream&) = delete;
-};
-
 RbfSet rbf_set(const ModelDesc& m) {
   RbfSet rs{};
   rs.n = static_cast<int>(m.rbfs.size());
@@ -1568,11 +1535,6 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
       build_batch(*fine_[level], ld.sizes, std::move(ld.pts), std::move(ld.inner));
     }
   }
-  // The coarse grid (the FP64 factor and explicit inverse of one domain of ~2,048 rows: long
-  // chains of small launches) runs on a second stream while this one fills the level arrays and
-  // evaluates A P; the streams join before the constructor returns.
-  SideStream side;
-  side.enter();
   {
     Domain cd;
     cd.point_indices = point_idcs_[0];
@@ -1611,7 +1573,6 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
     coarse_out_.resize(48);
     coarse_out_.zero();
   }
-  side.leave();
 
   // Level row sets on the device (for the residual-update evaluators): the level's points,
   // then three rows per gradient point.
@@ -1672,7 +1633,6 @@ RasPreconditioner<T>::RasPreconditioner(const ModelDesc& model, const double* po
   work_tot_.resize(rows_ + l);
   work_fit_.resize(rows_);
   work_src_w_.resize(rows_ + l);
-  side.join();
   sync();
 }
 
