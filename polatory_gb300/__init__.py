@@ -256,6 +256,10 @@ class Interpolant:
         pts = as_points(points)
         gpts = as_points(np.zeros((0, 3)) if grad_points is None else grad_points)
         vals = np.ascontiguousarray(np.asarray(values, dtype=np.float64).reshape(-1))
+        n_rhs = pts.shape[0] + 3 * gpts.shape[0]
+        if vals.shape[0] != n_rhs:
+            # interpolant.hpp:88-91 (the C ABI takes a pointer and cannot check the length).
+            raise PolatoryError(_lib.PGPU_INVALID_ARGUMENT, f"values.rows() must be equal to {n_rhs}")
         check(lib.pgpu_interpolant_fit(
             self._h, ptr(pts), pts.shape[0], ptr(gpts) if gpts.shape[0] else None, gpts.shape[0],
             ptr(vals), float(tolerance), float(grad_tolerance), int(max_iter), float(accuracy),

@@ -108,3 +108,31 @@ def test_server_estimate_and_argument_checks():
     assert _lib.lib.pgpu_server_create(-1, 0, C.byref(h)) == _lib.PGPU_INVALID_ARGUMENT
     assert _lib.lib.pgpu_server_create(2, -5, C.byref(h)) == _lib.PGPU_INVALID_ARGUMENT
     assert _lib.lib.pgpu_server_destroy(None) == _lib.PGPU_OK
+
+
+def test_operator_cache_controls_on_the_host():
+    # The far-field operator cache's statistics and limit are host state: an empty cache, the
+    # default 8 GiB limit (PGPU_M2L_CACHE_MB unset), a limit that can be set and restored, and
+    # a negative limit refused.
+    import os
+
+    st = pg.operator_cache_stats()
+    assert st["bytes"] >= 0 and st["entries"] >= 0
+    if "PGPU_M2L_CACHE_MB" not in os.environ:
+        assert st["limit"] == 8192 << 20
+    pg.set_operator_cache_limit(123 << 20)
+    assert pg.operator_cache_stats()["limit"] == 123 << 20
+    pg.set_operator_cache_limit(st["limit"])
+    assert pg.operator_cache_stats()["limit"] == st["limit"]
+    with pytest.raises(pg.PolatoryError, match="limit must be >= 0"):
+        pg.set_operator_cache_limit(-1)
+
+
+def test_gradient_fit_argument_errors_on_the_host():
+    # Interpolant::fit with gradient points (interpolant.hpp:82-113): the value count must be
+    # mu + 3 sigma (checked before the library is called).
+    it = pg.Interpolant(pg.Model(pg.Triharmonic3D([1.0]), 1))
+    pts = np.random.default_rng(1).random((10, 3))
+    gpts = np.random.default_rng(2).random((4, 3))
+    with pytest.raises(pg.PolatoryError, match="values.rows\\(\\) must be equal to 22"):
+        it.fit(pts, np.zeros(10), 1e-4, grad_points=gpts, grad_tolerance=1e-4)
