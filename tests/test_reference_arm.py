@@ -1,6 +1,6 @@
 """CPU checks of the benchmark's reference arm and of the oracle it times: the arm never loads the
-product library, reports the configurations it cannot run in full as unavailable (with the
-reason), and the oracle's blocked LU solve of the fit system agrees with numpy's LAPACK solve."""
+product library, runs small configurations whole and large ones as a bounded sample that says
+so, and the oracle's blocked LU solve of the fit system agrees with numpy's LAPACK solve."""
 import json
 import subprocess
 import sys
@@ -27,9 +27,27 @@ def run_reference_arm(*args):
     return lines[0], lines[-1]["product_loaded"]
 
 
-@pytest.mark.parametrize("workload", ["c2", "c3", "c4", "c5"])
-def test_reference_arm_reports_oversized_configs_unavailable(workload):
-    line, loaded = run_reference_arm("--workload", workload, "--scale", "0.05")
+def test_reference_arm_samples_large_configs():
+    # c2 at 0.01 scale: 30,000 data points (above the dense limit) -> 12,000 of them and every
+    # one of the 20,000 queries per step, labelled as a sample that does not carry over.
+    line, loaded = run_reference_arm("--workload", "c2", "--scale", "0.01", "--steps", "1",
+                                     "--warmup", "0")
+    assert not loaded
+    assert "unavailable" not in line and line["value"] > 0
+    cb = line["cpu_baseline"]
+    assert cb["comparable"] is False and "12000 of the 30000 data points" in cb["sample"]
+    assert "does not carry over" in cb["sample"]
+
+
+def test_reference_arm_samples_batched_fits():
+    line, loaded = run_reference_arm("--workload", "c4", "--scale", "0.004", "--steps", "1",
+                                     "--warmup", "0")
+    assert not loaded
+    assert line["value"] > 0 and "first" in line["cpu_baseline"]["sample"]
+
+
+def test_reference_arm_reports_serving_unavailable():
+    line, loaded = run_reference_arm("--workload", "c5")
     assert line["impl"] == "reference"
     assert "unavailable" in line and "cannot be built" in line["unavailable"]
     assert not loaded
