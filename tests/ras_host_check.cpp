@@ -6,7 +6,11 @@
 //  3. the level-parallel coarse-point selection returns the same set as a direct sequential
 //     restatement of the priority-queue rule (domain_divider.hpp:54-125) on value points, in
 //     the canonical order (polynomial points, then ascending index);
-//  4. asking for more coarse points than there are points returns every point once.
+//  4. asking for more coarse points than there are points returns every point once;
+//  5. the Lagrange basis of test/polynomial/test_lagrange_basis.cpp:16-31: at a unisolvent
+//     point set (degrees 0-2) the basis evaluates to the identity (to 1e-12), also for the
+//     one-point-plus-one-gradient-point set of degree 1 (lagrange_basis.hpp:36-37), and a
+//     repeated point set is rejected as not unisolvent.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -236,7 +240,60 @@ static void check_parallel_splits(Index n_points, unsigned seed) {
   CHECK(cseq == cpar);
 }
 
+static void check_lagrange() {
+  std::mt19937 gen(11);
+  std::uniform_real_distribution<double> u(-1.0, 1.0);
+  for (int degree = 0; degree <= 2; ++degree) {
+    const int l = (degree + 1) * (degree + 2) * (degree + 3) / 6;
+    std::vector<double> pts(3 * 200);
+    for (auto& v : pts) v = u(gen);
+    const auto idx = pgpu::unisolvent_point_set(pts.data(), 200, degree);
+    CHECK(static_cast<int>(idx.size()) == l);
+    std::vector<double> pp;
+    for (auto i : idx)
+      for (int k = 0; k < 3; ++k) pp.push_back(pts[3 * i + k]);
+    const auto coeffs = pgpu::lagrange_coeffs(degree, pp.data(), l);
+    // L_c(p_r) = sum_k m_k(p_r) coeffs[k][c] = delta_rc.
+    double err = 0;
+    for (int r = 0; r < l; ++r) {
+      double m[10];
+      pgpu::monomial_row(degree, pp.data() + 3 * r, m);
+      for (int c = 0; c < l; ++c) {
+        double v = 0;
+        for (int k = 0; k < l; ++k) v += m[k] * coeffs[k * l + c];
+        err = std::max(err, std::fabs(v - (r == c ? 1.0 : 0.0)));
+      }
+    }
+    CHECK(err < 1e-12);
+  }
+  {
+    // Degree 1 at one point x and one gradient point y: rows m(x), dm/dx(y), dm/dy(y), dm/dz(y).
+    const double x[3] = {0.3, -0.2, 0.7};
+    std::vector<double> rows = {1, x[0], x[1], x[2], 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    const auto coeffs = pgpu::lagrange_coeffs_of(rows, 4);
+    double err = 0;
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c) {
+        double v = 0;
+        for (int k = 0; k < 4; ++k) v += rows[r * 4 + k] * coeffs[k * 4 + c];
+        err = std::max(err, std::fabs(v - (r == c ? 1.0 : 0.0)));
+      }
+    CHECK(err < 1e-12);
+  }
+  {
+    const double same[12] = {0.1, 0.2, 0.3, 0.1, 0.2, 0.3, 0.5, 0.5, 0.5, 0.9, 0.1, 0.4};
+    bool thrown = false;
+    try {
+      pgpu::lagrange_coeffs(1, same, 4);
+    } catch (const pgpu::Error&) {
+      thrown = true;
+    }
+    CHECK(thrown);
+  }
+}
+
 int main() {
+  check_lagrange();
   check_parallel_splits(30000, 7);
   check_divider(10000, 10000, 10, 1);
   check_divider(20000, 0, 4, 2);

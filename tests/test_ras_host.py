@@ -1,7 +1,8 @@
 """CPU test of the RAS host set-up (domain division, coarse points): compiles
 tests/ras_host_check.cpp against polatory_gb300/csrc/ras_host.cpp with g++ and runs it.
-Restates test/preconditioner/test_domain_divider.cpp:18-90 and checks the level-parallel
-coarse-point selection against a sequential priority-queue restatement."""
+Restates test/preconditioner/test_domain_divider.cpp:18-90 and
+test/polynomial/test_lagrange_basis.cpp:16-31, and checks the level-parallel coarse-point
+selection against a sequential priority-queue restatement."""
 import subprocess
 from pathlib import Path
 
