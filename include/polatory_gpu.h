@@ -227,7 +227,10 @@ int pgpu_interpolant_destroy(pgpu_interpolant* it);
 /* precision: PGPU_PRECISION_PLAIN (default) or PGPU_PRECISION_MIXED. */
 int pgpu_interpolant_set_precision(pgpu_interpolant* it, int precision);
 /* Interpolant::fit (interpolant.hpp:82-113). grad_points may be NULL when sigma == 0.
- * values: mu + 3 * sigma entries. initial may be NULL (warm start otherwise). */
+ * values: mu + 3 * sigma entries (the values, then the three derivatives of each gradient
+ * point). initial may be NULL (warm start otherwise: weights of centres and gradient centres
+ * at the same coordinates). Fits with gradient points run in FP64 whatever the precision;
+ * kernels without a Hessian (cub, sph) return PGPU_RUNTIME_ERROR with the reference's message. */
 int pgpu_interpolant_fit(pgpu_interpolant* it, const double* points, int64_t mu,
                          const double* grad_points, int64_t sigma, const double* values,
                          double tolerance, double grad_tolerance, int max_iter, double accuracy,
